@@ -1,0 +1,214 @@
+/*
+ * iss_gpu.h -- C ABI of the GB300 Cooper-Frye sampler (the "FSSW" path of
+ * iSS, MC_sampling = 4).
+ *
+ * Every entry point replaces one public member of the reference's driver class
+ * `iSS` (src/iSS.h:16-102) or one step behind it; the citation next to each
+ * declaration names the reference interface it stands in for.  The ABI uses
+ * plain pointers and sizes only.  Every call returns an iss_status instead of
+ * calling exit() the way the reference does (src/iSS.cpp:45-53,
+ * src/ParameterReader.cpp:150-159, src/readindata.cpp:50-55, 411-415, 933-935,
+ * src/FSSW.cpp:254-259, 897-902, src/MomentumSamplerBase.cpp:35-43); the
+ * message of the last failure is available from iss_gpu_last_error().
+ *
+ * Threading: a handle owns its CUDA stream, its device buffers and its host
+ * copies; handles are independent, one handle must not be used from two
+ * threads at the same time.  There is no CPU fallback: when no CUDA device is
+ * usable, the calls that need one return ISS_ERR_CUDA.
+ */
+#ifndef ISS_GPU_H
+#define ISS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct iss_handle iss_handle;
+
+typedef enum iss_status {
+    ISS_OK = 0,
+    ISS_ERR_INVALID_ARG = 1,   /* NULL handle/pointer, bad index, bad size     */
+    ISS_ERR_IO = 2,            /* a parameter, surface or table file missing   */
+    ISS_ERR_PARAM_MISSING = 3, /* ParameterReader::getVal of an unknown key    */
+    ISS_ERR_UNSUPPORTED = 4,   /* MC_sampling != 4, PCE surfaces, missing 22-moment table, ... */
+    ISS_ERR_CUDA = 5,          /* no device, launch or allocation failure      */
+    ISS_ERR_OUT_OF_RANGE = 6,  /* m/T - mu/T outside the momentum tables, negative yield, NaN */
+    ISS_ERR_NO_SURFACE = 7,    /* generate before a surface was read           */
+    ISS_ERR_NO_SAMPLES = 8,    /* hadron access before generate                */
+    ISS_ERR_CAPACITY = 9,      /* caller buffer too small                      */
+    ISS_ERR_SAMPLING = 10      /* a bounded device loop gave up (counted, see timings) */
+} iss_status;
+
+/* Layout-identical to the reference's iSS_Hadron (src/data_struct.h:79-84):
+ * int pid followed by nine floats, 40 bytes. */
+typedef struct iss_hadron {
+    int32_t pid;
+    float mass;
+    float E, px, py, pz;
+    float t, x, y, z;
+} iss_hadron_t;
+
+/* Output formats of iss_gpu_write_output, as selected in the reference by
+ * use_OSCAR_format / use_gzip_format / use_binary_format (src/FSSW.cpp:354-360). */
+typedef enum iss_output_format {
+    ISS_OUTPUT_OSCAR = 1,   /* FSSW::combine_samples_to_OSCAR,       src/FSSW.cpp:365-494 */
+    ISS_OUTPUT_GZIP = 2,    /* FSSW::combine_samples_to_gzip_file,   src/FSSW.cpp:497-526 */
+    ISS_OUTPUT_BINARY = 3   /* FSSW::combine_samples_to_binary_file, src/FSSW.cpp:529-561 */
+} iss_output_format;
+
+/* Device-side time of the phases of the last iss_gpu_generate, measured with
+ * CUDA events on the handle's stream, plus the counters of the bounded loops. */
+typedef struct iss_timings {
+    double ms_prologue;   /* local-rest-frame transform + per-cell delta-f coefficients */
+    double ms_yields;     /* per (cell, species) yields                               */
+    double ms_cdf;        /* per-species FP64 prefix sums (cell CDF) and totals       */
+    double ms_counts;     /* per (event, species) counts + slot scan                  */
+    double ms_sample;     /* momentum sampling, boost, emission                       */
+    double ms_total;      /* first event to last event of iss_gpu_generate            */
+    int64_t n_hadrons;    /* hadrons written                                          */
+    int64_t n_tries;      /* proposals made by the sampler                            */
+    int64_t n_cell_redraws;  /* cells redrawn after the try cap (src/FSSW.cpp:1017-1021) */
+    int64_t n_failures;   /* hadrons abandoned after the redraw cap (never expected)  */
+    int32_t kernel_launches; /* kernels launched by the last iss_gpu_generate          */
+} iss_timings_t;
+
+/* ---- construction, parameters ------------------------------------------ */
+
+/* iSS::iSS(path, table_path, particle_table_path, inputfile, surface_filename)
+ * (src/iSS.h:43-46, src/iSS.cpp:14-24): reads `param_file` with the
+ * ParameterReader rules (src/ParameterReader.cpp:33-106).  NULL strings take
+ * the reference defaults ("iSS_tables", "iSS_tables", "iSS_parameters.dat",
+ * "surface.dat"); work_path has no default. */
+iss_status iss_gpu_create(const char* work_path, const char* table_path,
+                          const char* particle_table_path, const char* param_file,
+                          const char* surface_filename, iss_handle** out);
+
+/* iSS::~iSS (src/iSS.cpp:27-30); accepts NULL. */
+iss_status iss_gpu_destroy(iss_handle* h);
+
+/* paraRdr_ptr->setVal(name, value) (src/ParameterReader.cpp:130-144). */
+iss_status iss_gpu_set_param(iss_handle* h, const char* key, double value);
+
+/* paraRdr_ptr->getVal(name) (src/ParameterReader.cpp:150-159); an unknown key
+ * returns ISS_ERR_PARAM_MISSING instead of exiting. */
+iss_status iss_gpu_get_param(iss_handle* h, const char* key, double* value);
+
+/* paraRdr_ptr->readFromArguments for one "key=value  # comment" string
+ * (src/ParameterReader.cpp:76-83, 110-116; src/main.cpp:61). */
+iss_status iss_gpu_parse_param_line(iss_handle* h, const char* line);
+
+/* ---- seed, surface, sampling --------------------------------------------- */
+
+/* iSS::set_random_seed(int) (src/iSS.cpp:123-127).  seed == -1 draws a seed
+ * from the OS like std::random_device (src/Random.cpp:10-12). */
+iss_status iss_gpu_set_seed(iss_handle* h, int64_t seed);
+
+/* iSS::set_random_seed() (src/iSS.cpp:116-120): seed from key randomSeed. */
+iss_status iss_gpu_set_seed_from_params(iss_handle* h);
+
+/* iSS::read_in_FO_surface (src/iSS.cpp:86-113): reads <work_path>/music_input
+ * and the MUSIC surface (text or 34-float binary, hydro_mode 1 or 2,
+ * src/readindata.cpp:25-111, 395-546, 626-765), the species tables
+ * (src/readindata.cpp:971-1116) and uploads the cells; the local-rest-frame
+ * transform (src/iSS.cpp:170-293) runs on the device at generate time. */
+iss_status iss_gpu_read_surface(iss_handle* h);
+
+/* In-memory surface: n_cells records in the reference's FO_surf field order
+ * and units (src/data_struct.h:53-63 without the PCE vector: tau, x, y, eta,
+ * da0..da3, u0..u3, Edec, Tdec, Pdec, Bn, muB, muS, muQ, pi00, pi01, pi02,
+ * pi03, pi11, pi12, pi13, pi22, pi23, pi33, bulkPi, qmu0..qmu3 -- 34 floats,
+ * GeV and fm), i.e. what read_FOdata produces before regulate_surface_cells
+ * (src/readindata.cpp:768-842) runs.  Species tables are read as in
+ * iss_gpu_read_surface; music_input is not needed (EOS_to_use = 2). */
+iss_status iss_gpu_set_surface(iss_handle* h, const float* fo_surf_records,
+                               int64_t n_cells);
+
+/* iSS::generate_samples (src/iSS.cpp:130-165) for MC_sampling = 4, i.e.
+ * FSSW::shell (src/FSSW.cpp:344-361) without the optional decays and
+ * spectators: yields, counts, momenta and the hadron lists, all on the GPU. */
+iss_status iss_gpu_generate(iss_handle* h);
+
+/* iSS::shell (src/iSS.cpp:41-56): read_surface + set_seed_from_params +
+ * generate. */
+iss_status iss_gpu_shell(iss_handle* h);
+
+/* iSS::clear (src/iSS.cpp:33-38): drops the surface and the samples. */
+iss_status iss_gpu_clear(iss_handle* h);
+
+/* ---- results --------------------------------------------------------------- */
+
+/* iSS::get_number_of_sampled_events (src/iSS.h:61-67, src/FSSW.h:173). */
+iss_status iss_gpu_num_events(iss_handle* h, int32_t* n_events);
+
+/* iSS::get_number_of_particles(iev) (src/iSS.h:69-75, src/FSSW.h:174-176). */
+iss_status iss_gpu_num_particles(iss_handle* h, int32_t iev, int64_t* n);
+
+/* iSS::get_hadron(iev, ipart) (src/iSS.h:77-83, src/FSSW.h:178-180). */
+iss_status iss_gpu_get_hadron(iss_handle* h, int32_t iev, int64_t ipart,
+                              iss_hadron_t* out);
+
+/* iSS::get_hadron_list_iev(iev) (src/iSS.h:85-91, src/FSSW.h:182-184): copies
+ * event iev (species in mass order, then draw order) into `out`. */
+iss_status iss_gpu_copy_event(iss_handle* h, int32_t iev, iss_hadron_t* out,
+                              int64_t capacity, int64_t* n_written);
+
+/* All events at once: out[0 .. n_total), event_offsets[0 .. n_events]
+ * (event iev is out[event_offsets[iev] .. event_offsets[iev+1])).  Either
+ * output pointer may be NULL to query sizes only. */
+iss_status iss_gpu_copy_all(iss_handle* h, iss_hadron_t* out, int64_t capacity,
+                            int64_t* event_offsets, int64_t* n_total);
+
+/* Writes the hadron lists in one of the reference's output formats
+ * (src/FSSW.cpp:365-561) to `filename` (NULL: the reference's default name in
+ * the current directory: OSCAR.DAT, particle_samples.gz, particle_samples.bin). */
+iss_status iss_gpu_write_output(iss_handle* h, int format, const char* filename);
+
+/* ---- inspection (parity tests, run reports) ---------------------------- */
+
+/* Number of chosen species and their PDG ids in the sampler's mass-sorted
+ * order (src/FSSW.cpp:115-162). */
+iss_status iss_gpu_species(iss_handle* h, int32_t* n_species, int32_t* pids,
+                           int32_t capacity);
+
+/* Per-species FP64 yields dN/dy summed over cells (the value the reference
+ * logs as "Sampling using dN_dy=", src/FSSW.cpp:943-961), in mass order. */
+iss_status iss_gpu_species_yields(iss_handle* h, double* dn_dy, int32_t capacity);
+
+/* Number of cells held on the device (after the T > 0.01 GeV filter of
+ * src/readindata.cpp:751-761; cells dropped by the u.dsigma < 0 rule of
+ * src/iSS.cpp:226 are kept with zero yield). */
+iss_status iss_gpu_num_cells(iss_handle* h, int64_t* n_cells);
+
+/* Local-rest-frame cells, 28 floats per cell in the FO_surf_LRF order of
+ * src/data_struct.h:66-76 (tau, x, y, eta, da_mu_LRF[4], u_tz[4], Edec, Tdec,
+ * Pdec, Bn, muB, muS, muQ, bulkPi, pi_xx, pi_xy, pi_xz, pi_yy, pi_yz, q_x, q_y,
+ * q_z); dropped cells have da_mu_LRF[0] < 0. */
+iss_status iss_gpu_copy_lrf_cells(iss_handle* h, float* out, int64_t capacity_cells);
+
+/* Per-cell yields dN/(dx_t dy) of species `species_index` (mass order), the
+ * vector FSSW::calculate_dN_dxtdy_for_one_particle_species fills
+ * (src/FSSW.cpp:565-715). */
+iss_status iss_gpu_copy_cell_yields(iss_handle* h, int32_t species_index,
+                                    float* out, int64_t capacity_cells);
+
+/* Hadron counts per (event, species), event-major, of the last generate
+ * (src/FSSW.cpp:970-977). */
+iss_status iss_gpu_copy_counts(iss_handle* h, int32_t* out, int64_t capacity);
+
+/* Timings and loop counters of the last iss_gpu_generate. */
+iss_status iss_gpu_get_timings(iss_handle* h, iss_timings_t* out);
+
+/* Message of the last failure on this handle ("" if none). */
+const char* iss_gpu_last_error(const iss_handle* h);
+
+/* Static name of a status code. */
+const char* iss_gpu_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ISS_GPU_H */
