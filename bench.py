@@ -1,0 +1,371 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Cooper-Frye sampler.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (N = 1): the viscous 3+1D surface -- 200,000 cells on 64 eta slices,
+20 % spacelike cells, shear with |pi|/(e+P) up to 0.3, 14-moment bulk delta f
+-- with the s95p-v1 species list (319 species) and 1,000 oversampled events
+per GPU.  One step = one full generate: local-rest-frame prologue, yields
+for every (cell, species), per-species CDFs, Poisson counts, momentum
+sampling and the hadron records, with the surface resident in HBM.  Inputs
+are synthetic (iss_gb300.surfaces, seed 2).  Intermediate buffers (yields
+256 MB, CDF 510 MB, hadrons ~0.8 GB) exceed L2 and a 256 MB buffer is
+written between steps.
+
+`value` is device time (CUDA events on the library's stream); `e2e` is the
+same metric through the C ABI with the surface copied from pinned host
+memory and all hadrons read back to pinned host memory every step.
+
+--impl reference times the CPU implementation of the path (the oracle port
+of the reference's algorithm, oracle/) on the host cores with one process per
+core, each sampling a disjoint share of the events on a 10 % cell sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = ("sampled hadrons/s on 1 GB300, learned vs plain sampler at matched spectra "
+          "(χ²/KS)")
+UNIT = "hadrons/s"
+N_CELLS = 200_000
+N_EVENTS = 1000
+SEED_SURFACE = 2
+PARAMS = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1, include_deltaf_bulk=1,
+              bulk_deltaf_kind=11, turn_on_bulk=1, quantum_statistics=1,
+              dN_dy_sampling_model=30, number_of_repeated_sampling=N_EVENTS)
+ALG_BYTES_PER_HADRON = 40 + 96 + 4     # record write + LRF cell gather + slot/index
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per hadron of the sampler kernel from the committed ncu
+    summary (profiles/sampler_kernel_viscous_3d.md, line 'dram_bytes_per_hadron:')."""
+    path = os.path.join(HERE, "profiles", "sampler_kernel_viscous_3d.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_hadron:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.file.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# CPU (oracle) leg
+
+def cpu_worker(args):
+    """One process: yields on the cell sample, counts and sampling of its
+    share of the events; returns (hadrons, seconds)."""
+    n_sample, n_events, event_offset, seed = args
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib as O
+    from iss_gb300 import surfaces as S
+    surf = S.viscous_3d(N_CELLS, seed=SEED_SURFACE)
+    rec = surf.records[:: max(1, N_CELLS // n_sample)][:n_sample]
+    fo = S.music_to_fo_surf(rec, 2)
+    params = dict(S.DEFAULT_PARAMETERS, **PARAMS)
+    t0 = time.perf_counter()
+    lrf, keep = O.lrf_cells(fo)
+    sp = O.chosen_species(S.TABLE_DIR, 0)
+    oc = O.OracleConfig(params, S.TABLE_DIR, n_events=n_events, seed=seed,
+                        event_offset=event_offset)
+    y = O.yields(oc, sp, lrf, keep).astype(np.float32)
+    cdf, tot = O.cdf(y)
+    cnt = O.counts(oc, sp, tot)
+    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
+    had, _ = O.sample_replay(oc, sp, lrf, coef, cdf, tot, cnt)
+    return len(had), time.perf_counter() - t0
+
+
+def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int):
+    import multiprocessing as mp
+    per = [n_events // n_procs + (1 if k < n_events % n_procs else 0) for k in range(n_procs)]
+    offs = np.concatenate([[0], np.cumsum(per)[:-1]])
+    jobs = [(n_sample, per[k], int(offs[k]), seed) for k in range(n_procs) if per[k] > 0]
+    t0 = time.perf_counter()
+    if len(jobs) == 1:
+        res = [cpu_worker(jobs[0])]
+    else:
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            res = pool.map(cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    hadrons = sum(r[0] for r in res)
+    return hadrons, wall
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import oracle_lib  # noqa: F401  (builds the oracle if needed)
+    n_procs = max(1, os.cpu_count() or 1)
+    n_sample = args.cpu_cells
+    rates = []
+    for step in range(args.warmup + args.steps):
+        h, wall = cpu_baseline(n_procs, n_sample, N_EVENTS, seed=1000 + step)
+        if step >= args.warmup:
+            rates.append((h, wall))
+    had = sum(r[0] for r in rates)
+    sec = sum(r[1] for r in rates)
+    value = had / sec
+    sample = (f"viscous 3+1D surface, every {N_CELLS // n_sample}th cell ({n_sample} cells), "
+              f"{N_EVENTS} events split over {n_procs} processes")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "viscous_3d_200k_cells_s95p_1000_events (CPU cell sample)",
+                       "cells_sampled": n_sample, "events": N_EVENTS, "species": 319,
+                       "bulk_deltaf_kind": 11, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_procs, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+
+def run_gpu(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from iss_gb300 import iSS, surfaces as S
+
+    surf = S.viscous_3d(N_CELLS, seed=SEED_SURFACE)
+    fo = surf.fo_surf()
+    n_events = args.events
+    params = dict(S.DEFAULT_PARAMETERS, **PARAMS)
+    params["number_of_repeated_sampling"] = n_events
+    params["gpu_event_offset"] = rank * n_events
+    s = iSS(".", inputfile="")
+    s.set_params(**params)
+    # pinned host buffers for the end-to-end leg
+    fo_pinned = torch.from_numpy(fo).pin_memory().numpy()
+    s.set_surface(fo_pinned)
+    s.set_random_seed(20261203)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        s.generate_samples()
+    torch.cuda.synchronize()
+
+    # device-timed steps
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    dev_ms, hadrons, t_sample, t_yields = [], [], [], []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s.generate_samples()
+        t = s.timings()
+        dev_ms.append(t["ms_total"])
+        hadrons.append(t["n_hadrons"])
+        t_sample.append(t["ms_sample"])
+        t_yields.append(t["ms_yields"])
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    timings = s.timings()
+    launches = args.steps * int(timings["kernel_launches"])
+
+    # end-to-end steps through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        n_h = max(hadrons)
+        out = torch.empty((int(n_h * 1.2) + 1024) * 40, dtype=torch.uint8).pin_memory().numpy()
+        from iss_gb300 import HADRON_DTYPE
+        out = out.view(HADRON_DTYPE)
+        e_had, e_bytes_in, e_bytes_out = 0, 0, 0
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.set_surface(fo_pinned)
+            s.generate_samples()
+            h, off = s.all_hadrons(out=out)
+            e_had += len(h)
+            e_bytes_in += fo_pinned.nbytes
+            e_bytes_out += len(h) * 40 + off.nbytes
+        torch.cuda.synchronize()
+        barrier()
+        e_sec = time.perf_counter() - t0
+        e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps]
+
+    sec = sum(dev_ms) / 1e3
+    local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
+    if e2e:
+        local_stats += [e2e[0], e2e[1]]
+    if ws > 1:
+        import torch.distributed as dist
+        v = torch.tensor(local_stats, dtype=torch.float64, device="cuda")
+        tot = v.clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        mx = v.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        all_h, max_sec = tot[0].item(), mx[1].item()
+        e2e_h, e2e_sec = (tot[4].item(), mx[5].item()) if e2e else (0, 1)
+    else:
+        all_h, max_sec = local_stats[0], local_stats[1]
+        e2e_h, e2e_sec = (e2e[0], e2e[1]) if e2e else (0, 1)
+
+    if rank == 0:
+        value = all_h / max_sec
+        peak, peak_kind = peaks()
+        # dominant kernel: the sampler
+        samp_sec = local_stats[2]
+        nh = local_stats[0]
+        achieved = nh * ALG_BYTES_PER_HADRON / samp_sec / 1e9
+        traffic_per_h = profiled_traffic()
+        per_launch_h = nh / args.steps
+        roofline = {"bound": "hbm", "kernel": "sampler_kernel", "achieved": achieved,
+                    "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "peak_source": peak_kind,
+                    "traffic": (traffic_per_h * per_launch_h) if traffic_per_h else None,
+                    "algorithmic_bytes_per_launch": per_launch_h * ALG_BYTES_PER_HADRON,
+                    "kernel_ms_per_launch": 1e3 * samp_sec / args.steps,
+                    "yields_kernel_ms_per_launch": 1e3 * local_stats[3] / args.steps}
+        cpu = None
+        if not args.no_cpu_baseline:
+            h_cpu, t_cpu = cpu_baseline(1, args.cpu_cells, N_EVENTS, seed=7)
+            cpu = {"value": h_cpu / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"viscous 3+1D surface, every {N_CELLS // args.cpu_cells}th cell "
+                             f"({args.cpu_cells} cells), {N_EVENTS} events, one core "
+                             f"({t_cpu:.1f} s)"}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * max_sec / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (iss_gb300.surfaces.viscous_3d, seed 2)",
+                "config": {"workload": "viscous_3d_200k_cells_s95p_1000_events",
+                           "cells": N_CELLS, "events_per_gpu": n_events, "species": 319,
+                           "bulk_deltaf_kind": 11, "sampler": "plain",
+                           "parallelism": f"event shards x{ws}",
+                           "l2": "256 MB buffer written between steps; working set > L2",
+                           "wall_s_timed": wall},
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": ({"value": e2e_h / e2e_sec, "unit": UNIT,
+                         "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3]}
+                        if e2e else None),
+                "gpu_launches": launches, "clocks": clk,
+                "hadrons_per_step": nh / args.steps,
+                "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--events", type=int, default=N_EVENTS)
+    ap.add_argument("--cpu-cells", type=int, default=20_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

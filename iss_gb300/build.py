@@ -1,0 +1,103 @@
+"""Builds the native library in-tree: iss_gb300/_native/libiss_gb300.so (the C
+ABI of include/iss_gpu.h, CUDA kernels for sm_103a) and iss_gb300/_native/iSS.e
+(the command-line driver).  Translation units compile in parallel; nothing is
+installed outside the source tree."""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_native")
+OBJ = os.path.join(OUT, "obj")
+LIB = os.path.join(OUT, "libiss_gb300.so")
+CLI = os.path.join(OUT, "iSS.e")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+INCLUDES = [f"-I{CSRC}", f"-I{os.path.join(REPO, 'include')}", f"-I{CUDA_HOME}/include"]
+
+CU_SOURCES = ["kernels_prologue.cu", "kernels_cells.cu", "kernels_sample.cu"]
+# the prologue reproduces the reference's float/double rounding points exactly,
+# so mul+add must not be contracted into FMAs there
+CU_EXTRA = {"kernels_prologue.cu": ["--fmad=false"]}
+CXX_SOURCES = ["api.cpp", "host/params.cpp", "host/tables.cpp", "host/surface_io.cpp",
+               "host/writers.cpp", "shim/iSS.cpp"]
+CLI_SOURCES = ["cli/main.cpp"]
+
+
+def _run(cmd):
+    res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + res.stdout)
+    return res.stdout
+
+
+def _obj(src):
+    return os.path.join(OBJ, src.replace("/", "_") + ".o")
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    out = []
+    for root, _, files in os.walk(CSRC):
+        out += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh"))]
+    out.append(os.path.join(REPO, "include", "iss_gpu.h"))
+    return out
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    if not os.path.exists(NVCC):
+        raise RuntimeError(f"nvcc not found at {NVCC}")
+    os.makedirs(OBJ, exist_ok=True)
+    hdrs = _headers()
+    jobs = []
+    for s in CU_SOURCES:
+        src = os.path.join(CSRC, s)
+        if force or _stale(_obj(s), [src] + hdrs):
+            jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         *CU_EXTRA.get(s, []), "-Xptxas", "-v" if verbose else "-O3",
+                         *INCLUDES, "-c", src, "-o", _obj(s)])
+    for s in CXX_SOURCES + CLI_SOURCES:
+        src = os.path.join(CSRC, s)
+        if force or _stale(_obj(s), [src] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+                         "-Wno-unused-function", *INCLUDES, "-c", src, "-o", _obj(s)])
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        outs = list(ex.map(_run, jobs))
+    if verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    lib_objs = [_obj(s) for s in CU_SOURCES + CXX_SOURCES]
+    cudalib = os.path.join(CUDA_HOME, "lib64")
+    if not os.path.isdir(cudalib):
+        cudalib = os.path.join(CUDA_HOME, "lib")
+    if force or _stale(LIB, lib_objs):
+        _run(["g++", "-shared", "-o", LIB, *lib_objs, f"-L{cudalib}", "-lcudart_static", "-ldl",
+              "-lrt", "-lpthread", "-Wl,--no-undefined"])
+    cli_objs = [_obj(s) for s in CLI_SOURCES]
+    if force or _stale(CLI, cli_objs + [LIB]):
+        _run(["g++", "-o", CLI, *cli_objs, f"-L{OUT}", "-liss_gb300", "-Wl,-rpath,$ORIGIN"])
+    return LIB
+
+
+def clean():
+    shutil.rmtree(OUT, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv, force="-f" in sys.argv)
+    print(LIB)

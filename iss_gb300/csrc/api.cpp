@@ -1,0 +1,882 @@
+// C ABI of the sampler (include/iss_gpu.h): the handle, the host side of
+// iSS::read_in_FO_surface / generate_samples, device memory and the launch
+// sequence of one generate:
+//   upload surface -> cell prologue -> yields -> per-species CDF
+//   -> counts -> slot offsets -> sampler -> event offsets back to the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "host/params.h"
+#include "host/surface_io.h"
+#include "host/tables.h"
+#include "host/writers.h"
+#include "iss_gpu.h"
+#include "kernels.h"
+
+using namespace iss;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;   // elements
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && ptr) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(n, 1);
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&ptr), want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+};
+
+struct TableKey {
+    std::string table_path;
+    int afterburner = -1, bulk_kind = -1, include_bulk = -1, include_diff = -1, neos = -9;
+    int fix_c0 = -1;
+    bool operator==(const TableKey& o) const {
+        return table_path == o.table_path && afterburner == o.afterburner &&
+               bulk_kind == o.bulk_kind && include_bulk == o.include_bulk &&
+               include_diff == o.include_diff && neos == o.neos && fix_c0 == o.fix_c0;
+    }
+};
+
+enum Phase { kEvStart = 0, kEvPrologue, kEvYields, kEvCdf, kEvCounts, kEvSampleStart, kEvSample, kEvCount };
+
+}  // namespace
+
+struct iss_handle {
+    std::string work_path, table_path, particle_table_path, surface_filename;
+    ParamStore params;
+    std::string last_error;
+    int64_t seed = 1;
+    bool seed_set = false;
+
+    // surface (host)
+    std::vector<float> fo34;
+    int64_t n_cells = 0;
+    int hydro_mode = 2;
+    int iEOS = 2;
+    int afterburner = 0;
+    bool surface_loaded = false;
+    bool surface_on_device = false;
+    bool quantum_statistics = true;
+    std::vector<Species> species;
+    std::vector<Species> resonances;
+    int species_afterburner = -1;
+    bool species_qs = true;
+
+    // device
+    bool cuda_ready = false;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[kEvCount] = {};
+    DevBuf<float> d_fo34;
+    DevBuf<float4> d_cells;          // 8 arrays of n_cells float4
+    DevBuf<SpeciesDev> d_species;
+    DevBuf<int32_t> d_pids;
+    DevBuf<float> d_yields;
+    DevBuf<double> d_cdf, d_tile_sum, d_tile_off, d_totals;
+    DevBuf<int32_t> d_counts;
+    DevBuf<int64_t> d_offsets, d_off_tiles;
+    DevBuf<HadronRec> d_hadrons;
+    DevBuf<unsigned long long> d_work;
+    DevBuf<SampleCounters> d_counters;
+    DevBuf<int> d_error;
+    // tables
+    TableKey table_key;
+    DevBuf<float4> d_sfK;
+    DevBuf<float> d_sfE;
+    DevBuf<double> d_b14c0, d_b14c1, d_b14c2, d_ce, d_qmu;
+    Bulk14Table b14;
+
+    // last generate
+    DevConfig cfg{};
+    bool yields_valid = false;
+    bool samples_valid = false;
+    int n_events = 0;
+    int64_t n_hadrons = 0;
+    std::vector<int64_t> event_offsets;
+    std::vector<iss_hadron_t> host_hadrons;
+    bool host_valid = false;
+    std::vector<double> totals;
+    iss_timings_t timings{};
+
+    ~iss_handle() {
+        if (cuda_ready) {
+            DevBuf<float>* fb[] = {&d_fo34, &d_yields, &d_sfE};
+            for (auto* b : fb) b->release();
+            d_cells.release();
+            d_species.release();
+            d_pids.release();
+            DevBuf<double>* db[] = {&d_cdf, &d_tile_sum, &d_tile_off, &d_totals, &d_b14c0,
+                                    &d_b14c1, &d_b14c2, &d_ce, &d_qmu};
+            for (auto* b : db) b->release();
+            d_counts.release();
+            d_offsets.release();
+            d_off_tiles.release();
+            d_hadrons.release();
+            d_work.release();
+            d_counters.release();
+            d_error.release();
+            d_sfK.release();
+            for (auto& e : ev)
+                if (e) cudaEventDestroy(e);
+            if (stream) cudaStreamDestroy(stream);
+        }
+    }
+};
+
+namespace {
+
+iss_status fail(iss_handle* h, iss_status st, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->last_error = buf;
+    return st;
+}
+
+#define CUDA_TRY(h, call)                                                                   \
+    do {                                                                                    \
+        cudaError_t _e = (call);                                                            \
+        if (_e != cudaSuccess)                                                              \
+            return fail((h), ISS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+iss_status ensure_cuda(iss_handle* h) {
+    if (h->cuda_ready) return ISS_OK;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        return fail(h, ISS_ERR_CUDA, "no CUDA device available (%s)",
+                    e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+    }
+    CUDA_TRY(h, cudaGetDevice(&h->device));
+    CUDA_TRY(h, cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (auto& ev : h->ev) CUDA_TRY(h, cudaEventCreate(&ev));
+    h->cuda_ready = true;
+    return ISS_OK;
+}
+
+bool need(iss_handle* h, const char* key, double* v) {
+    if (h->params.get(key, v)) return true;
+    h->last_error = std::string("parameter with name ") + key + " not found";
+    return false;
+}
+
+iss_status load_species(iss_handle* h) {
+    std::string err;
+    std::vector<int32_t> missing;
+    if (!load_chosen_species(h->particle_table_path, h->afterburner, h->quantum_statistics,
+                             &h->species, &missing, &err)) {
+        return fail(h, ISS_ERR_IO, "%s", err.c_str());
+    }
+    if (!load_resonances(h->particle_table_path, h->afterburner, h->quantum_statistics,
+                         &h->resonances, &err)) {
+        return fail(h, ISS_ERR_IO, "%s", err.c_str());
+    }
+    h->species_afterburner = h->afterburner;
+    h->species_qs = h->quantum_statistics;
+    return ISS_OK;
+}
+
+iss_status finish_surface(iss_handle* h) {
+    h->n_cells = static_cast<int64_t>(h->fo34.size() / kFoSurfFloats);
+    if (h->n_cells == 0) return fail(h, ISS_ERR_NO_SURFACE, "no freeze-out fluid cell");
+    h->surface_loaded = true;
+    h->surface_on_device = false;
+    h->yields_valid = false;
+    h->samples_valid = false;
+    h->host_valid = false;
+    return ISS_OK;
+}
+
+// configuration, tables and device buffers for the next generate
+iss_status prepare(iss_handle* h) {
+    double v;
+    if (!need(h, "MC_sampling", &v)) return ISS_ERR_PARAM_MISSING;
+    if (static_cast<int>(v) != 4)
+        return fail(h, ISS_ERR_UNSUPPORTED, "MC_sampling = %d: only the FSSW sampler (4) runs on the GPU",
+                    static_cast<int>(v));
+    DevConfig c{};
+    const char* keys[] = {"hydro_mode", "include_deltaf_shear", "include_deltaf_bulk",
+                          "bulk_deltaf_kind", "include_deltaf_diffusion",
+                          "local_charge_conservation", "number_of_repeated_sampling",
+                          "dN_dy_sampling_model", "dN_dy_sampling_para1",
+                          "sample_upto_desired_particle_number", "y_LB", "y_RB"};
+    double vals[12];
+    for (int i = 0; i < 12; i++)
+        if (!need(h, keys[i], &vals[i])) return ISS_ERR_PARAM_MISSING;
+    c.hydro_mode = static_cast<int>(vals[0]);
+    c.include_shear = static_cast<int>(vals[1]) == 1;
+    c.include_bulk = static_cast<int>(vals[2]) == 1;
+    c.bulk_kind = static_cast<int>(vals[3]);
+    c.include_diff = static_cast<int>(vals[4]) == 1;
+    c.neos_kind = (c.bulk_kind == 21) ? 1 : (c.bulk_kind == 20 ? 0 : -1);
+    if (static_cast<int>(vals[5]) != 0)
+        return fail(h, ISS_ERR_UNSUPPORTED, "local_charge_conservation = 1 is not supported");
+    c.n_events = static_cast<int>(vals[6]);
+    c.sampling_model = static_cast<int>(vals[7]);
+    c.sampling_para1 = vals[8];
+    if (c.sampling_model > 100 ||
+        !(c.sampling_model == 1 || c.sampling_model == 10 || c.sampling_model == 20 ||
+          c.sampling_model == 30))
+        return fail(h, ISS_ERR_UNSUPPORTED, "sampling model %d is not supported", c.sampling_model);
+    c.y_lb = static_cast<float>(vals[10]);
+    c.y_rb = static_cast<float>(vals[11]);
+    c.ymult = (c.hydro_mode != 2) ? (vals[11] - vals[10]) : 1.0;
+    if (h->params.get_or("perform_decays", 0) == 1 && h->afterburner != 2)
+        return fail(h, ISS_ERR_UNSUPPORTED, "perform_decays = 1 is not supported");
+    if (h->params.get_or("include_spectators", 0) != 0)
+        return fail(h, ISS_ERR_UNSUPPORTED, "include_spectators is not supported");
+    if (c.n_events < 0) return fail(h, ISS_ERR_INVALID_ARG, "negative number of events");
+    c.compat_fermion = static_cast<int>(h->params.get_or("gpu_compat_fermion_cdf2", 0)) != 0;
+    c.max_tries = static_cast<int>(h->params.get_or("gpu_max_tries", 10000));
+    c.max_redraws = static_cast<int>(h->params.get_or("gpu_max_redraws", 64));
+    c.event_offset = static_cast<uint32_t>(h->params.get_or("gpu_event_offset", 0));
+    c.key0 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed));
+    c.key1 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed) >> 32);
+    c.n_species = static_cast<int>(h->species.size());
+    c.n_cells = h->n_cells;
+    const int fix_c0 = static_cast<int>(h->params.get_or("gpu_fix_14mom_c0", 0)) != 0;
+
+    // tables
+    TableKey key{h->table_path, h->afterburner, c.bulk_kind, c.include_bulk, c.include_diff,
+                 c.neos_kind, fix_c0};
+    if (!(key == h->table_key)) {
+        std::string err;
+        std::vector<double> K, E;
+        special_function_tables(c.include_bulk != 0, c.include_diff != 0, &K, &E);
+        std::vector<float4> K4(kSfLen);
+        for (int i = 0; i < kSfLen; i++)
+            K4[i] = make_float4(static_cast<float>(K[3 * i]), static_cast<float>(K[3 * i + 1]),
+                                static_cast<float>(K[3 * i + 2]), 0.0f);
+        CUDA_TRY(h, h->d_sfK.reserve(kSfLen));
+        CUDA_TRY(h, cudaMemcpy(h->d_sfK.ptr, K4.data(), sizeof(float4) * kSfLen,
+                               cudaMemcpyHostToDevice));
+        if (c.include_diff) {
+            std::vector<float> E32(E.begin(), E.end());
+            CUDA_TRY(h, h->d_sfE.reserve(E32.size()));
+            CUDA_TRY(h, cudaMemcpy(h->d_sfE.ptr, E32.data(), sizeof(float) * E32.size(),
+                                   cudaMemcpyHostToDevice));
+        }
+        if (c.include_bulk && c.bulk_kind == 11) {
+            if (!load_bulk14(h->table_path, h->afterburner, fix_c0 != 0, &h->b14, &err))
+                return fail(h, ISS_ERR_IO, "%s", err.c_str());
+            const size_t n = h->b14.c1.size();
+            CUDA_TRY(h, h->d_b14c0.reserve(n));
+            CUDA_TRY(h, h->d_b14c1.reserve(n));
+            CUDA_TRY(h, h->d_b14c2.reserve(n));
+            CUDA_TRY(h, cudaMemcpy(h->d_b14c0.ptr, h->b14.c0.data(), 8 * n, cudaMemcpyHostToDevice));
+            CUDA_TRY(h, cudaMemcpy(h->d_b14c1.ptr, h->b14.c1.data(), 8 * n, cudaMemcpyHostToDevice));
+            CUDA_TRY(h, cudaMemcpy(h->d_b14c2.ptr, h->b14.c2.data(), 8 * n, cudaMemcpyHostToDevice));
+        }
+        if (c.neos_kind == 0) {
+            return fail(h, ISS_ERR_IO, "can not find file %s/deltaf_tables/%s/NEoSBQS_22mom_deltafCoeff.dat",
+                        h->table_path.c_str(), h->afterburner == 2 ? "smash" : "urqmd");
+        }
+        if (c.neos_kind == 1) {
+            std::vector<double> ce;
+            if (!load_ce_neos(h->table_path, h->afterburner, &ce, &err))
+                return fail(h, ISS_ERR_IO, "%s", err.c_str());
+            CUDA_TRY(h, h->d_ce.reserve(ce.size()));
+            CUDA_TRY(h, cudaMemcpy(h->d_ce.ptr, ce.data(), 8 * ce.size(), cudaMemcpyHostToDevice));
+        }
+        if (c.include_diff) {
+            std::vector<double> q;
+            if (!load_qmu_coeff(h->table_path, &q, &err)) return fail(h, ISS_ERR_IO, "%s", err.c_str());
+            CUDA_TRY(h, h->d_qmu.reserve(q.size()));
+            CUDA_TRY(h, cudaMemcpy(h->d_qmu.ptr, q.data(), 8 * q.size(), cudaMemcpyHostToDevice));
+        }
+        h->table_key = key;
+    }
+    c.tab.sfK = h->d_sfK.ptr;
+    c.tab.sfE = h->d_sfE.ptr;
+    c.tab.b14c0 = h->d_b14c0.ptr;
+    c.tab.b14c1 = h->d_b14c1.ptr;
+    c.tab.b14c2 = h->d_b14c2.ptr;
+    c.tab.b14_nT = h->b14.nT;
+    c.tab.b14_nmu = h->b14.nmu;
+    c.tab.b14_T0 = h->b14.T0;
+    c.tab.b14_mu0 = h->b14.mu0;
+    c.tab.b14_dT = h->b14.dT;
+    c.tab.b14_dmu = h->b14.dmu;
+    c.tab.ce = h->d_ce.ptr;
+    c.tab.qmu = h->d_qmu.ptr;
+
+    // species
+    std::vector<SpeciesDev> sd(h->species.size());
+    std::vector<int32_t> pids(h->species.size());
+    for (size_t k = 0; k < sd.size(); k++) {
+        const Species& s = h->species[k];
+        sd[k].m_hi = static_cast<float>(s.mass);
+        sd[k].m_lo = static_cast<float>(s.mass - static_cast<double>(sd[k].m_hi));
+        sd[k].degen = static_cast<float>(s.gspin);
+        sd[k].light = s.mass < 0.7 ? 1 : 0;
+        sd[k].baryon = s.baryon;
+        sd[k].strange = s.strange;
+        sd[k].charge = s.charge;
+        sd[k].sign = s.sign;
+        pids[k] = s.pid;
+    }
+    CUDA_TRY(h, h->d_species.reserve(sd.size()));
+    CUDA_TRY(h, h->d_pids.reserve(sd.size()));
+    if (!sd.empty()) {
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_species.ptr, sd.data(), sizeof(SpeciesDev) * sd.size(),
+                                    cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_pids.ptr, pids.data(), 4 * pids.size(),
+                                    cudaMemcpyHostToDevice, h->stream));
+    }
+    h->cfg = c;
+    return ISS_OK;
+}
+
+CellArrays cell_arrays(iss_handle* h) {
+    CellArrays a;
+    float4* b = h->d_cells.ptr;
+    const int64_t n = h->n_cells;
+    a.pos = b;
+    a.da = b + n;
+    a.u = b + 2 * n;
+    a.th = b + 3 * n;
+    a.th2 = b + 4 * n;
+    a.pi1 = b + 5 * n;
+    a.pi2 = b + 6 * n;
+    a.coef = b + 7 * n;
+    return a;
+}
+
+// surface upload + prologue + yields + CDF (the per-cell half of generate)
+iss_status run_cells(iss_handle* h) {
+    const int64_t n = h->n_cells;
+    const int S = static_cast<int>(h->species.size());
+    DevConfig& c = h->cfg;
+    cudaStream_t st = h->stream;
+    if (!h->surface_on_device) {
+        CUDA_TRY(h, h->d_fo34.reserve(static_cast<size_t>(n) * kFoSurfFloats));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_fo34.ptr, h->fo34.data(),
+                                    sizeof(float) * static_cast<size_t>(n) * kFoSurfFloats,
+                                    cudaMemcpyHostToDevice, st));
+        h->surface_on_device = true;
+    }
+    CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 8));
+    CUDA_TRY(h, h->d_yields.reserve(static_cast<size_t>(n) * S));
+    CUDA_TRY(h, h->d_cdf.reserve(static_cast<size_t>(n + 1) * S));
+    const int nt = cdf_num_tiles(n);
+    CUDA_TRY(h, h->d_tile_sum.reserve(static_cast<size_t>(nt) * S));
+    CUDA_TRY(h, h->d_tile_off.reserve(static_cast<size_t>(nt) * S));
+    CUDA_TRY(h, h->d_totals.reserve(static_cast<size_t>(S)));
+    const CellArrays cells = cell_arrays(h);
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
+    CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvPrologue], st));
+    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
+    CUDA_TRY(h, launch_cdf(h->d_yields.ptr, S, n, h->d_tile_sum.ptr, h->d_tile_off.ptr,
+                           h->d_totals.ptr, h->d_cdf.ptr, st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvCdf], st));
+    h->yields_valid = true;
+    return ISS_OK;
+}
+
+float elapsed(iss_handle* h, int a, int b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]);
+    return ms;
+}
+
+iss_status run_generate(iss_handle* h) {
+    if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface: call iss_gpu_read_surface first");
+    iss_status st = ensure_cuda(h);
+    if (st != ISS_OK) return st;
+    st = prepare(h);
+    if (st != ISS_OK) return st;
+    h->samples_valid = false;
+    h->host_valid = false;
+    st = run_cells(h);
+    if (st != ISS_OK) return st;
+    DevConfig& c = h->cfg;
+    const int S = c.n_species;
+    cudaStream_t s = h->stream;
+
+    // number of events from the thermal pi+ yield when asked for
+    // (FSSW::compute_number_of_sampling_needed, src/FSSW.cpp:851-869)
+    if (h->params.get_or("sample_upto_desired_particle_number", 0) == 1) {
+        double needed, max_ev;
+        if (!need(h, "number_of_particles_needed", &needed) ||
+            !need(h, "maximum_sampling_events", &max_ev))
+            return ISS_ERR_PARAM_MISSING;
+        std::vector<double> tot(static_cast<size_t>(S));
+        CUDA_TRY(h, cudaMemcpyAsync(tot.data(), h->d_totals.ptr, 8 * static_cast<size_t>(S),
+                                    cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(h, cudaStreamSynchronize(s));
+        double dn_pion = 0.0;
+        for (int k = 0; k < S; k++)
+            if (h->species[k].real_idx == 1) dn_pion = tot[k];
+        int nev = static_cast<int>(static_cast<long>(needed) / (6. * dn_pion));
+        if (c.hydro_mode == 2) nev *= 10;
+        nev = std::max(1, std::min(static_cast<int>(max_ev), nev));
+        c.n_events = nev;
+    }
+
+    const int64_t nseg = static_cast<int64_t>(c.n_events) * S;
+    CUDA_TRY(h, h->d_counts.reserve(static_cast<size_t>(std::max<int64_t>(nseg, 1))));
+    CUDA_TRY(h, h->d_offsets.reserve(static_cast<size_t>(nseg + 1)));
+    CUDA_TRY(h, h->d_off_tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(nseg), 1))));
+    CUDA_TRY(h, h->d_error.reserve(1));
+    CUDA_TRY(h, h->d_work.reserve(1));
+    CUDA_TRY(h, h->d_counters.reserve(1));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
+    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_counts.ptr, h->d_error.ptr, s));
+    CUDA_TRY(h, launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
+    int64_t n_units = 0;
+    int count_err = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&n_units, h->d_offsets.ptr + nseg, sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(&count_err, h->d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
+    if (count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
+
+    CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long), s));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
+    CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
+                               h->d_totals.ptr, h->d_offsets.ptr, n_units, h->d_hadrons.ptr,
+                               h->d_work.ptr, h->d_counters.ptr, h->num_sms, s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvSample], s));
+    // event offsets: offsets[e * S] for e = 0..n_events
+    h->event_offsets.assign(static_cast<size_t>(c.n_events) + 1, 0);
+    if (S > 0) {
+        CUDA_TRY(h, cudaMemcpy2DAsync(h->event_offsets.data(), sizeof(int64_t), h->d_offsets.ptr,
+                                      sizeof(int64_t) * static_cast<size_t>(S), sizeof(int64_t),
+                                      static_cast<size_t>(c.n_events) + 1, cudaMemcpyDeviceToHost, s));
+    }
+    SampleCounters ctr{};
+    CUDA_TRY(h, cudaMemcpyAsync(&ctr, h->d_counters.ptr, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    CUDA_TRY(h, cudaGetLastError());
+
+    iss_timings_t& t = h->timings;
+    t.ms_prologue = elapsed(h, kEvStart, kEvPrologue);
+    t.ms_yields = elapsed(h, kEvPrologue, kEvYields);
+    t.ms_cdf = elapsed(h, kEvYields, kEvCdf);
+    t.ms_counts = elapsed(h, kEvCdf, kEvCounts);
+    t.ms_sample = elapsed(h, kEvSampleStart, kEvSample);
+    t.ms_total = elapsed(h, kEvStart, kEvSample);
+    t.n_hadrons = n_units;
+    t.n_tries = static_cast<int64_t>(ctr.tries);
+    t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
+    t.n_failures = static_cast<int64_t>(ctr.failures);
+    t.kernel_launches = 10;
+    h->n_events = c.n_events;
+    h->n_hadrons = n_units;
+    h->samples_valid = true;
+    if (ctr.error_code == 1) {
+        const int k = ctr.error_species;
+        return fail(h, ISS_ERR_OUT_OF_RANGE,
+                    "momentum sampler out of range for species %d (m/T - mu/T off the tables)",
+                    (k >= 0 && k < S) ? h->species[k].pid : 0);
+    }
+    if (ctr.failures > 0)
+        return fail(h, ISS_ERR_SAMPLING, "%llu hadrons abandoned after %d cell redraws",
+                    static_cast<unsigned long long>(ctr.failures), c.max_redraws);
+    return ISS_OK;
+}
+
+iss_status ensure_host_copy(iss_handle* h) {
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples: call iss_gpu_generate first");
+    if (h->host_valid) return ISS_OK;
+    h->host_hadrons.resize(static_cast<size_t>(h->n_hadrons));
+    if (h->n_hadrons > 0) {
+        CUDA_TRY(h, cudaMemcpy(h->host_hadrons.data(), h->d_hadrons.ptr,
+                               sizeof(iss_hadron_t) * static_cast<size_t>(h->n_hadrons),
+                               cudaMemcpyDeviceToHost));
+    }
+    h->host_valid = true;
+    return ISS_OK;
+}
+
+}  // namespace
+
+static_assert(sizeof(iss_hadron_t) == 40, "iss_hadron_t must be 40 bytes");
+static_assert(sizeof(HadronRec) == sizeof(iss_hadron_t), "device record layout");
+
+extern "C" {
+
+const char* iss_gpu_status_string(int status) {
+    switch (status) {
+        case ISS_OK: return "ok";
+        case ISS_ERR_INVALID_ARG: return "invalid argument";
+        case ISS_ERR_IO: return "file not found or unreadable";
+        case ISS_ERR_PARAM_MISSING: return "parameter missing";
+        case ISS_ERR_UNSUPPORTED: return "unsupported option";
+        case ISS_ERR_CUDA: return "CUDA error";
+        case ISS_ERR_OUT_OF_RANGE: return "value out of range";
+        case ISS_ERR_NO_SURFACE: return "no surface";
+        case ISS_ERR_NO_SAMPLES: return "no samples";
+        case ISS_ERR_CAPACITY: return "buffer too small";
+        case ISS_ERR_SAMPLING: return "sampling failure";
+        default: return "unknown status";
+    }
+}
+
+const char* iss_gpu_last_error(const iss_handle* h) { return h ? h->last_error.c_str() : ""; }
+
+iss_status iss_gpu_create(const char* work_path, const char* table_path,
+                          const char* particle_table_path, const char* param_file,
+                          const char* surface_filename, iss_handle** out) {
+    if (!out || !work_path) return ISS_ERR_INVALID_ARG;
+    *out = nullptr;
+    std::unique_ptr<iss_handle> h(new iss_handle);
+    h->work_path = work_path;
+    h->table_path = table_path ? table_path : "iSS_tables";
+    h->particle_table_path = particle_table_path ? particle_table_path : "iSS_tables";
+    h->surface_filename = surface_filename ? surface_filename : "surface.dat";
+    const std::string pf = param_file ? param_file : "iSS_parameters.dat";
+    if (!pf.empty() && !h->params.read_file(pf)) {
+        return ISS_ERR_IO;
+    }
+    *out = h.release();
+    return ISS_OK;
+}
+
+iss_status iss_gpu_destroy(iss_handle* h) {
+    delete h;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_set_param(iss_handle* h, const char* key, double value) {
+    if (!h || !key) return ISS_ERR_INVALID_ARG;
+    h->params.set(key, value);
+    return ISS_OK;
+}
+
+iss_status iss_gpu_get_param(iss_handle* h, const char* key, double* value) {
+    if (!h || !key || !value) return ISS_ERR_INVALID_ARG;
+    if (!h->params.get(key, value))
+        return fail(h, ISS_ERR_PARAM_MISSING, "parameter with name %s not found", key);
+    return ISS_OK;
+}
+
+iss_status iss_gpu_parse_param_line(iss_handle* h, const char* line) {
+    if (!h || !line) return ISS_ERR_INVALID_ARG;
+    h->params.parse_line(line);
+    return ISS_OK;
+}
+
+iss_status iss_gpu_set_seed(iss_handle* h, int64_t seed) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (seed == -1) {
+        std::random_device rd;
+        seed = (static_cast<int64_t>(rd()) << 32) ^ rd();
+    }
+    h->seed = seed;
+    h->seed_set = true;
+    h->samples_valid = false;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_set_seed_from_params(iss_handle* h) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    double v;
+    if (!need(h, "randomSeed", &v)) return ISS_ERR_PARAM_MISSING;
+    return iss_gpu_set_seed(h, static_cast<int64_t>(v));
+}
+
+iss_status iss_gpu_read_surface(iss_handle* h) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    double mode, qs;
+    if (!need(h, "hydro_mode", &mode) || !need(h, "quantum_statistics", &qs))
+        return ISS_ERR_PARAM_MISSING;
+    h->hydro_mode = static_cast<int>(mode);
+    h->quantum_statistics = static_cast<int>(qs) == 1;
+    if (h->hydro_mode != 1 && h->hydro_mode != 2)
+        return fail(h, ISS_ERR_UNSUPPORTED, "hydro_mode %d: only MUSIC surfaces (1, 2) are read",
+                    h->hydro_mode);
+    MusicSettings ms;
+    std::string err;
+    if (!read_music_input(h->work_path, h->params, &ms, &err)) return fail(h, ISS_ERR_IO, "%s", err.c_str());
+    if (!eos_is_known(ms.iEOS)) return fail(h, ISS_ERR_INVALID_ARG, "invalid EOS_to_use %d", ms.iEOS);
+    if (!eos_is_chemical_equilibrium(ms.iEOS))
+        return fail(h, ISS_ERR_UNSUPPORTED,
+                    "EOS_to_use %d is partially chemically equilibrated (PCE); not supported", ms.iEOS);
+    h->iEOS = ms.iEOS;
+    h->afterburner = select_afterburner(h->params, ms.iEOS);
+    if (!read_music_surface(h->work_path + "/" + h->surface_filename, h->hydro_mode, ms, &h->fo34,
+                            &err))
+        return fail(h, ISS_ERR_IO, "%s", err.c_str());
+    if (ms.iEOS == 9 || ms.iEOS == 91 || ms.iEOS == 12 || ms.iEOS == 14) {
+        HrgEos eos;
+        if (!load_hrg_eos(h->table_path, ms.iEOS, h->afterburner, &eos, &err))
+            return fail(h, ISS_ERR_IO, "%s", err.c_str());
+        regulate_temperature(eos, &h->fo34);
+    }
+    iss_status st = load_species(h);
+    if (st != ISS_OK) return st;
+    return finish_surface(h);
+}
+
+iss_status iss_gpu_set_surface(iss_handle* h, const float* records, int64_t n_cells) {
+    if (!h || (!records && n_cells > 0) || n_cells < 0) return ISS_ERR_INVALID_ARG;
+    double mode, qs;
+    if (!need(h, "hydro_mode", &mode) || !need(h, "quantum_statistics", &qs))
+        return ISS_ERR_PARAM_MISSING;
+    h->hydro_mode = static_cast<int>(mode);
+    h->quantum_statistics = static_cast<int>(qs) == 1;
+    h->iEOS = 2;
+    h->afterburner = select_afterburner(h->params, 2);
+    if (h->species.empty() || h->species_afterburner != h->afterburner ||
+        h->species_qs != h->quantum_statistics) {
+        iss_status st = load_species(h);
+        if (st != ISS_OK) return st;
+    }
+    if (n_cells == 0) return fail(h, ISS_ERR_NO_SURFACE, "no freeze-out fluid cell");
+    // With a device, the records go straight from the caller's buffer (pinned
+    // or pageable) to HBM; without one a host copy is kept for inspection.
+    if (ensure_cuda(h) == ISS_OK) {
+        const size_t bytes = sizeof(float) * static_cast<size_t>(n_cells) * kFoSurfFloats;
+        CUDA_TRY(h, h->d_fo34.reserve(static_cast<size_t>(n_cells) * kFoSurfFloats));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_fo34.ptr, records, bytes, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        h->fo34.clear();
+        h->n_cells = n_cells;
+        h->surface_loaded = true;
+        h->surface_on_device = true;
+        h->yields_valid = false;
+        h->samples_valid = false;
+        h->host_valid = false;
+        h->last_error.clear();
+        return ISS_OK;
+    }
+    h->last_error.clear();
+    h->fo34.assign(records, records + static_cast<size_t>(n_cells) * kFoSurfFloats);
+    return finish_surface(h);
+}
+
+iss_status iss_gpu_generate(iss_handle* h) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!h->seed_set) {
+        iss_status st = iss_gpu_set_seed_from_params(h);
+        if (st != ISS_OK) return st;
+    }
+    return run_generate(h);
+}
+
+iss_status iss_gpu_shell(iss_handle* h) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    iss_status st = iss_gpu_read_surface(h);
+    if (st != ISS_OK) return st;
+    st = iss_gpu_set_seed_from_params(h);
+    if (st != ISS_OK) return st;
+    return run_generate(h);
+}
+
+iss_status iss_gpu_clear(iss_handle* h) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    h->fo34.clear();
+    h->n_cells = 0;
+    h->surface_loaded = false;
+    h->surface_on_device = false;
+    h->yields_valid = false;
+    h->samples_valid = false;
+    h->host_valid = false;
+    h->host_hadrons.clear();
+    h->event_offsets.clear();
+    h->species.clear();
+    h->species_afterburner = -1;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_num_events(iss_handle* h, int32_t* n) {
+    if (!h || !n) return ISS_ERR_INVALID_ARG;
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples");
+    *n = h->n_events;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_num_particles(iss_handle* h, int32_t iev, int64_t* n) {
+    if (!h || !n) return ISS_ERR_INVALID_ARG;
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples");
+    if (iev < 0 || iev >= h->n_events) return fail(h, ISS_ERR_INVALID_ARG, "event %d out of range", iev);
+    *n = h->event_offsets[iev + 1] - h->event_offsets[iev];
+    return ISS_OK;
+}
+
+iss_status iss_gpu_get_hadron(iss_handle* h, int32_t iev, int64_t ipart, iss_hadron_t* out) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    iss_status st = ensure_host_copy(h);
+    if (st != ISS_OK) return st;
+    if (iev < 0 || iev >= h->n_events) return fail(h, ISS_ERR_INVALID_ARG, "event %d out of range", iev);
+    const int64_t n = h->event_offsets[iev + 1] - h->event_offsets[iev];
+    if (ipart < 0 || ipart >= n) return fail(h, ISS_ERR_INVALID_ARG, "particle %lld out of range",
+                                             static_cast<long long>(ipart));
+    *out = h->host_hadrons[static_cast<size_t>(h->event_offsets[iev] + ipart)];
+    return ISS_OK;
+}
+
+iss_status iss_gpu_copy_event(iss_handle* h, int32_t iev, iss_hadron_t* out, int64_t capacity,
+                              int64_t* n_written) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples");
+    if (iev < 0 || iev >= h->n_events) return fail(h, ISS_ERR_INVALID_ARG, "event %d out of range", iev);
+    const int64_t b = h->event_offsets[iev], n = h->event_offsets[iev + 1] - b;
+    if (n_written) *n_written = n;
+    if (!out) return ISS_OK;
+    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "event %d has %lld hadrons", iev,
+                                  static_cast<long long>(n));
+    if (n == 0) return ISS_OK;
+    if (h->host_valid) {
+        std::memcpy(out, h->host_hadrons.data() + b, sizeof(iss_hadron_t) * static_cast<size_t>(n));
+        return ISS_OK;
+    }
+    CUDA_TRY(h, cudaMemcpy(out, h->d_hadrons.ptr + b, sizeof(iss_hadron_t) * static_cast<size_t>(n),
+                           cudaMemcpyDeviceToHost));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_copy_all(iss_handle* h, iss_hadron_t* out, int64_t capacity,
+                            int64_t* event_offsets, int64_t* n_total) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples");
+    if (n_total) *n_total = h->n_hadrons;
+    if (event_offsets)
+        std::memcpy(event_offsets, h->event_offsets.data(), sizeof(int64_t) * h->event_offsets.size());
+    if (!out) return ISS_OK;
+    if (capacity < h->n_hadrons) return fail(h, ISS_ERR_CAPACITY, "%lld hadrons do not fit",
+                                             static_cast<long long>(h->n_hadrons));
+    if (h->n_hadrons == 0) return ISS_OK;
+    if (h->host_valid) {
+        std::memcpy(out, h->host_hadrons.data(), sizeof(iss_hadron_t) * static_cast<size_t>(h->n_hadrons));
+        return ISS_OK;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_hadrons.ptr,
+                                sizeof(iss_hadron_t) * static_cast<size_t>(h->n_hadrons),
+                                cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_write_output(iss_handle* h, int format, const char* filename) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    iss_status st = ensure_host_copy(h);
+    if (st != ISS_OK) return st;
+    std::string err;
+    bool ok = false;
+    const iss_hadron_t* hd = h->host_hadrons.data();
+    const int64_t* off = h->event_offsets.data();
+    if (format == ISS_OUTPUT_OSCAR) {
+        ok = write_oscar(filename ? filename : "OSCAR.DAT", h->table_path + "/OSCAR_header.txt", hd,
+                         off, h->n_events, &err);
+    } else if (format == ISS_OUTPUT_GZIP) {
+        ok = write_gzip(filename ? filename : "particle_samples.gz", hd, off, h->n_events, &err);
+    } else if (format == ISS_OUTPUT_BINARY) {
+        ok = write_binary(filename ? filename : "particle_samples.bin", hd, off, h->n_events, &err);
+    } else {
+        return fail(h, ISS_ERR_INVALID_ARG, "unknown output format %d", format);
+    }
+    return ok ? ISS_OK : fail(h, ISS_ERR_IO, "%s", err.c_str());
+}
+
+iss_status iss_gpu_species(iss_handle* h, int32_t* n_species, int32_t* pids, int32_t capacity) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface");
+    const int32_t n = static_cast<int32_t>(h->species.size());
+    if (n_species) *n_species = n;
+    if (!pids) return ISS_OK;
+    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "%d species", n);
+    for (int32_t k = 0; k < n; k++) pids[k] = h->species[k].pid;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_species_yields(iss_handle* h, double* dn_dy, int32_t capacity) {
+    if (!h || !dn_dy) return ISS_ERR_INVALID_ARG;
+    if (!h->yields_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no yields: call iss_gpu_generate first");
+    const int32_t n = static_cast<int32_t>(h->species.size());
+    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "%d species", n);
+    CUDA_TRY(h, cudaMemcpy(dn_dy, h->d_totals.ptr, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_num_cells(iss_handle* h, int64_t* n_cells) {
+    if (!h || !n_cells) return ISS_ERR_INVALID_ARG;
+    *n_cells = h->n_cells;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_copy_lrf_cells(iss_handle* h, float* out, int64_t capacity_cells) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    if (!h->yields_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no cells on the device yet");
+    if (capacity_cells < h->n_cells) return fail(h, ISS_ERR_CAPACITY, "too small");
+    const int64_t n = h->n_cells;
+    std::vector<float4> buf(static_cast<size_t>(n) * 8);
+    CUDA_TRY(h, cudaMemcpy(buf.data(), h->d_cells.ptr, sizeof(float4) * buf.size(),
+                           cudaMemcpyDeviceToHost));
+    for (int64_t l = 0; l < n; l++) {
+        const float4 pos = buf[l], da = buf[n + l], u = buf[2 * n + l], th = buf[3 * n + l];
+        const float4 th2 = buf[4 * n + l], p1 = buf[5 * n + l], p2 = buf[6 * n + l];
+        float* o = out + 28 * l;
+        const float v[28] = {pos.x, pos.y, pos.z, pos.w, da.x, da.y, da.z, da.w, u.x, u.y,
+                             u.z, u.w, th2.x, th.x, th2.y, th2.z, th.y, th.z, th.w, th2.w,
+                             p1.x, p1.y, p1.z, p1.w, p2.x, p2.y, p2.z, p2.w};
+        std::memcpy(o, v, sizeof(v));
+    }
+    return ISS_OK;
+}
+
+iss_status iss_gpu_copy_cell_yields(iss_handle* h, int32_t species_index, float* out,
+                                    int64_t capacity_cells) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    if (!h->yields_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no yields yet");
+    if (species_index < 0 || species_index >= static_cast<int32_t>(h->species.size()))
+        return fail(h, ISS_ERR_INVALID_ARG, "species index %d out of range", species_index);
+    if (capacity_cells < h->n_cells) return fail(h, ISS_ERR_CAPACITY, "too small");
+    CUDA_TRY(h, cudaMemcpy(out, h->d_yields.ptr + static_cast<size_t>(species_index) * h->n_cells,
+                           sizeof(float) * static_cast<size_t>(h->n_cells), cudaMemcpyDeviceToHost));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_copy_counts(iss_handle* h, int32_t* out, int64_t capacity) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    if (!h->samples_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no samples");
+    const int64_t n = static_cast<int64_t>(h->n_events) * static_cast<int64_t>(h->species.size());
+    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "need %lld", static_cast<long long>(n));
+    if (n > 0)
+        CUDA_TRY(h, cudaMemcpy(out, h->d_counts.ptr, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_get_timings(iss_handle* h, iss_timings_t* out) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    *out = h->timings;
+    return ISS_OK;
+}
+
+}  // extern "C"

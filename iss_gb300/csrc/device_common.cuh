@@ -1,0 +1,130 @@
+// Device-side building blocks shared by the sampler kernels: the structures
+// the kernels read, the Philox4x32-10 counter-based generator, uniform
+// conversions and double-float ("float-float") helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace iss {
+
+// ---------------------------------------------------------------------------
+// structures passed to kernels by value
+
+struct DevTables {
+    const float4* sfK;      // [kSfLen] (K1, K2, K3, 0) in FP32, grid x = 0.5 + 0.05 i
+    const float* sfE;       // [kSfLen * 9] E_2, E_4, ..., E_18 in FP32
+    const double* b14c0;    // OSU 14-moment tables [iT * nmu + imu]
+    const double* b14c1;
+    const double* b14c2;
+    int b14_nT, b14_nmu;
+    double b14_T0, b14_mu0, b14_dT, b14_dmu;
+    const double* ce;       // NEoS-BQS Chapman-Enskog, 200 * 200 rows of 5
+    const double* qmu;      // RTA diffusion coefficient, 150 * 100
+};
+
+struct DevConfig {
+    int hydro_mode;
+    int include_shear, include_bulk, include_diff;
+    int bulk_kind, neos_kind;
+    int compat_fermion;
+    int sampling_model;
+    double sampling_para1;
+    float y_lb, y_rb;
+    double ymult;            // y_RB - y_LB for boost-invariant surfaces, else 1
+    uint32_t key0, key1;     // Philox key (the seed)
+    int n_species;
+    int n_events;
+    int64_t n_cells;
+    uint32_t event_offset;
+    int max_tries, max_redraws;
+    DevTables tab;
+};
+
+// Species record in the sampler's mass order (32 bytes).
+struct SpeciesDev {
+    float m_hi, m_lo;        // FP64 mass as a float-float pair
+    float degen;             // spin degeneracy
+    int light;               // mass < 0.7 GeV: 10 series terms (src/FSSW.cpp:740-745)
+    int baryon, strange, charge, sign;
+};
+
+// Local-rest-frame cells, structure of arrays of float4.
+struct CellArrays {
+    float4* pos;    // tau, x, y, eta
+    float4* da;     // dsigma_mu in the LRF (lower index); da.x < 0: cell dropped
+    float4* u;      // u^mu in the t-z frame
+    float4* th;     // T, muB, muS, muQ
+    float4* th2;    // E, P, n_B, Pi
+    float4* pi1;    // pi_xx, pi_xy, pi_xz, pi_yy (LRF)
+    float4* pi2;    // pi_yz, q_x, q_y, q_z (LRF)
+    float4* coef;   // per-cell delta-f coefficients vis0, vis1, vis2, kappa_B
+};
+
+// Counters written by the sampler.
+struct SampleCounters {
+    unsigned long long tries;
+    unsigned long long redraws;
+    unsigned long long failures;
+    unsigned long long bound_violations;
+    int error_code;          // 1: m/T - mu/T off the momentum tables
+    int error_species;
+};
+
+// Hadron record, layout of iSS_Hadron / iss_hadron_t.
+struct HadronRec {
+    int pid;
+    float mass, E, px, py, pz, t, x, y, z;
+};
+
+enum : uint32_t { kTagCell = 1u, kTagTry = 2u, kTagCount = 3u };
+
+#if defined(__CUDACC__)
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// [0, 1), 24 bits
+__device__ __forceinline__ float u01f(uint32_t x) {
+    return static_cast<float>(x >> 8) * (1.0f / 16777216.0f);
+}
+// (0, 1], 24 bits
+__device__ __forceinline__ float u01f_pos(uint32_t x) {
+    return static_cast<float>((x >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+// [0, 1), 53 bits
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    return (static_cast<double>(a >> 5) * 67108864.0 + static_cast<double>(b >> 6)) *
+           (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------
+// float-float arithmetic (error-free transformations)
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+#endif  // __CUDACC__
+
+}  // namespace iss

@@ -1,0 +1,655 @@
+// Sampling kernels:
+//   counts_kernel     FSSW::determine_number_to_sample (src/FSSW.cpp:250-309), one
+//                     draw per (event, species) from the Philox stream
+//                     {iteration, 0, event, species | TAG_COUNT << 16}
+//   offsets scan      exclusive int64 prefix sum of the counts: each
+//                     (event, species) segment gets its output slots, events in
+//                     order, species in mass order inside an event (the order of
+//                     src/FSSW.cpp:920-1049)
+//   sampler_kernel    per hadron: cell draw on the species' FP64 CDF
+//                     (RandomVariable1DArray::rand, src/RandomVariable1DArray.cpp:67-70),
+//                     momentum by rejection in the local rest frame with the
+//                     Cooper-Frye / delta-f weight (src/FSSW.cpp:1852-1966),
+//                     boost to the lab and the hadron record
+//                     (src/FSSW.cpp:1969-2010).
+//
+// The |p| proposal is an exact Gamma mixture: with K = (E - m)/T and
+// m~ = m/T the density (E^2 - m^2/2) exp(-(E - mu)/T) is proportional to
+// (K^2 + 2 m~ K + m~^2/2) exp(-K), a mixture of Gamma(3), Gamma(2) and
+// Gamma(1) with weights 2, 2 m~ and m~^2/2.  The quantum-statistics factor
+// f/exp(-(E-mu)/T), the pE/(E^2 - m^2/2) factor of
+// src/MomentumSamplerBase.cpp:45-56 and the Cooper-Frye/delta-f acceptance of
+// src/FSSW.cpp:1939-1945 are applied as one acceptance probability, so every
+// try costs one proposal and the accepted density is the reference's
+// p^2 f(E) x accept.  The support is cut at the end of the reference's
+// momentum table for the selected sampler (src/MomentumSamplerShell.cpp:24-48).
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace iss {
+
+namespace {
+
+constexpr float kTwoOverE10 = 0.0735758882342885f;   // 2 / (10 e)
+
+__device__ __forceinline__ uint4 block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                       uint32_t k0, uint32_t k1) {
+    return philox4x32_10(make_uint4(c0, c1, c2, c3), k0, k1);
+}
+
+// ------------------------------------------------------------------------
+// counts
+
+__device__ int64_t poisson_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t iter0,
+                                double mu) {
+    if (mu < 12.0) {
+        const uint4 w = block(iter0, 0u, c2, c3, k0, k1);
+        const double u = u53(w.x, w.y);
+        double p = exp(-mu);
+        double cdf = p;
+        int64_t k = 0;
+        while (u > cdf && k < 1000) {
+            k++;
+            p *= mu / static_cast<double>(k);
+            cdf += p;
+        }
+        return k;
+    }
+    const double smu = sqrt(mu);
+    const double b = 0.931 + 2.53 * smu;
+    const double a = -0.059 + 0.02483 * b;
+    const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
+    const double vr = 0.9277 - 3.6224 / (b - 2.0);
+    const double log_mu = log(mu);
+    for (uint32_t it = 0; it < 10000u; it++) {
+        const uint4 w = block(iter0 + it, 0u, c2, c3, k0, k1);
+        const double U = u53(w.x, w.y) - 0.5;
+        const double V = u53(w.z, w.w);
+        const double us = 0.5 - fabs(U);
+        const double kd = floor((2.0 * a / us + b) * U + mu + 0.43);
+        if (us >= 0.07 && V <= vr) return static_cast<int64_t>(kd);
+        if (kd < 0.0 || (us < 0.013 && V > us)) continue;
+        if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -mu + kd * log_mu - lgamma(kd + 1.0))
+            return static_cast<int64_t>(kd);
+    }
+    return -1;
+}
+
+__device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t iter0,
+                             double shape) {
+    double boost = 1.0;
+    if (shape < 1.0) {
+        const uint4 w = block(iter0, 0u, c2, c3, k0, k1);
+        boost = pow(static_cast<double>(u01f_pos(w.x)), 1.0 / shape);
+        shape += 1.0;
+        iter0 += 1;
+    }
+    const double d = shape - 1.0 / 3.0;
+    const double cc = 1.0 / sqrt(9.0 * d);
+    for (uint32_t it = 0; it < 10000u; it++) {
+        const uint4 w = block(iter0 + it, 0u, c2, c3, k0, k1);
+        const double r = sqrt(-2.0 * log(static_cast<double>(u01f_pos(w.x))));
+        const double x = r * cos(2.0 * 3.14159265358979323846 * static_cast<double>(u01f(w.y)));
+        double v = 1.0 + cc * x;
+        if (v <= 0.0) continue;
+        v = v * v * v;
+        const double u = u53(w.z, w.w);
+        if (u < 1.0 - 0.0331 * x * x * x * x) return boost * d * v;
+        if (log(u) < 0.5 * x * x + d * (1.0 - v + log(v))) return boost * d * v;
+    }
+    return -1.0;
+}
+
+__global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
+                              int32_t* __restrict__ counts, int* __restrict__ error) {
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
+    if (idx >= total) return;
+    const int e = static_cast<int>(idx / cfg.n_species);
+    const int s = static_cast<int>(idx % cfg.n_species);
+    const uint32_t c2 = cfg.event_offset + static_cast<uint32_t>(e);
+    const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCount << 16);
+    const double dN = totals[s] * cfg.ymult;
+    const int64_t dN_int = static_cast<int64_t>(dN);
+    const double frac = dN - static_cast<double>(dN_int);
+    const double para1 = cfg.sampling_para1;
+    int64_t nsamp = 0;
+    if (dN < 0) {
+        atomicCAS(error, 0, 2);
+    } else if (cfg.sampling_model == 1) {
+        const uint4 w = block(0u, 0u, c2, c3, cfg.key0, cfg.key1);
+        nsamp = dN_int + (u53(w.x, w.y) < frac ? 1 : 0);
+    } else if (cfg.sampling_model == 10 || cfg.sampling_model == 20) {
+        const double kk = (cfg.sampling_model == 10) ? para1 * frac : para1 * dN;
+        const double p = 1.0 / (1.0 + para1);
+        if (kk < 1e-15) {
+            nsamp = dN_int;
+        } else {
+            const double g = gamma_draw(c2, c3, cfg.key0, cfg.key1, 0u, kk);
+            const int64_t nb = poisson_draw(c2, c3, cfg.key0, cfg.key1, 1u << 20, g * (1.0 - p) / p);
+            nsamp = (cfg.sampling_model == 10) ? dN_int + nb : nb;
+            if (g < 0.0 || nb < 0) atomicCAS(error, 0, 3);
+        }
+    } else {
+        nsamp = (dN < 1e-15) ? 0 : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, dN);
+        if (nsamp < 0) atomicCAS(error, 0, 3);
+    }
+    counts[idx] = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
+}
+
+// ------------------------------------------------------------------------
+// exclusive int64 scan of the counts
+
+constexpr int kOffThreads = 256;
+constexpr int kOffPer = 16;
+constexpr int kOffTile = kOffThreads * kOffPer;
+
+__device__ __forceinline__ long long warp_incl_scan_ll(long long v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ long long block_excl_scan_ll(long long v, long long* s_warp, long long* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long inc = warp_incl_scan_ll(v);
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        const long long w = lane < nw ? s_warp[lane] : 0;
+        const long long wi = warp_incl_scan_ll(w);
+        if (lane < nw) s_warp[lane] = wi - w;
+        if (lane == nw - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const long long out = s_warp[wid] + inc - v;
+    *total = s_warp[32];
+    __syncthreads();
+    return out;
+}
+
+__global__ void __launch_bounds__(kOffThreads)
+off_tile_sum_kernel(const int32_t* __restrict__ counts, int64_t n, int64_t* __restrict__ tile_sum) {
+    __shared__ long long s_warp[33];
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kOffTile;
+    long long acc = 0;
+    for (int k = 0; k < kOffPer; k++) {
+        const int64_t i = t0 + k * kOffThreads + threadIdx.x;
+        if (i < n) acc += counts[i];
+    }
+    long long tot;
+    block_excl_scan_ll(acc, s_warp, &tot);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kOffThreads)
+off_tile_offset_kernel(int64_t* __restrict__ tile_sum, int n_tiles, int64_t* __restrict__ offsets,
+                       int64_t n) {
+    __shared__ long long s_warp[33];
+    long long carry = 0;
+    for (int b = 0; b < n_tiles; b += kOffThreads) {
+        const int i = b + threadIdx.x;
+        const long long v = i < n_tiles ? tile_sum[i] : 0;
+        long long tot;
+        const long long ex = block_excl_scan_ll(v, s_warp, &tot);
+        if (i < n_tiles) tile_sum[i] = carry + ex;   // in place: now tile offsets
+        carry += tot;
+    }
+    if (threadIdx.x == 0) offsets[n] = carry;
+}
+
+__global__ void __launch_bounds__(kOffThreads)
+off_tile_scan_kernel(const int32_t* __restrict__ counts, int64_t n,
+                     const int64_t* __restrict__ tile_off, int64_t* __restrict__ offsets) {
+    __shared__ int32_t s_in[kOffThreads * (kOffPer + 1)];
+    __shared__ long long s_warp[33];
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kOffTile;
+    for (int k = 0; k < kOffPer; k++) {
+        const int e = k * kOffThreads + threadIdx.x;
+        const int64_t i = t0 + e;
+        s_in[(e / kOffPer) * (kOffPer + 1) + e % kOffPer] = i < n ? counts[i] : 0;
+    }
+    __syncthreads();
+    const int32_t* mine = s_in + threadIdx.x * (kOffPer + 1);
+    long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < kOffPer; k++) acc += mine[k];
+    long long tot;
+    long long run = tile_off[blockIdx.x] + block_excl_scan_ll(acc, s_warp, &tot);
+    const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kOffPer;
+#pragma unroll
+    for (int k = 0; k < kOffPer; k++) {
+        if (e0 + k < n) offsets[e0 + k] = run;
+        run += mine[k];
+    }
+}
+
+// ------------------------------------------------------------------------
+// sampler
+
+struct Prop {
+    float T, m, a, mt, Kmax, W, w32, w3, qa;
+    float mut, cpoly, rmax;
+    int boson, compat, sign;
+    float4 da;
+    float inv_dsfac;
+    float pxx, pxy, pxz, pyy, pyz, shear_c;
+    int shear_over_p0T;
+    float bi0, b0, b1, b2;
+    float qx, qy, qz, pq, Bq;
+};
+
+struct Unit {
+    int64_t slot;
+    uint32_t i, eg;
+    int s;
+    int cell;
+    int redraw;
+    int tries_cell;
+    uint32_t t;
+};
+
+__device__ __forceinline__ int cell_search(const double* __restrict__ row, int64_t n, double v) {
+    // largest i with row[i] < v <= row[i+1] (binarySearch of src/arsenal.cpp:644-678)
+    int64_t lo = 0, hi = n;
+    if (v > row[n]) return static_cast<int>(n - 1);
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (row[mid] < v) lo = mid; else hi = mid;
+    }
+    return static_cast<int>(lo);
+}
+
+// returns false when m/T - mu/T is outside the reference's momentum tables
+__device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
+                           int l, Prop& p) {
+    const float4 th = cells.th[l];
+    const float4 th2 = cells.th2[l];
+    const float4 pi1 = cells.pi1[l];
+    const float4 pi2 = cells.pi2[l];
+    const float4 cf = cells.coef[l];
+    p.da = cells.da[l];
+    const float T = th.x;
+    const float beta = 1.0f / T;
+    const float m = sp.m_hi + sp.m_lo;
+    const float mu_raw = static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
+                         static_cast<float>(sp.charge) * th.w;
+    const float mu = fminf(m, mu_raw);
+    p.T = T;
+    p.m = m;
+    p.sign = sp.sign;
+    p.mt = m * beta;
+    p.mut = mu * beta;
+    p.a = (m - mu) * beta;
+    p.boson = (sp.sign == -1);
+    const int sampler = p.a < 30.0f ? 0 : (p.a < 50.0f ? 1 : 2);
+    float e0, de;
+    int npts;
+    if (p.boson) {
+        e0 = (sampler == 0 ? 0.05f : (sampler == 1 ? 30.0f : 50.0f)) + 0.05f;
+        de = 0.05f;
+        npts = 1001;
+    } else {
+        e0 = (sampler == 0 ? 0.0f : (sampler == 1 ? 30.0f : 50.0f));
+        de = 0.02f;
+        npts = 2001;
+    }
+    const int idx_min = static_cast<int>((p.a - e0) / de);
+    if (idx_min < 0 || idx_min >= npts - 1) return false;
+    p.Kmax = e0 + (npts - 1) * de - p.a;
+    p.w3 = 2.0f;
+    p.w32 = 2.0f + 2.0f * p.mt;
+    p.W = p.w32 + 0.5f * p.mt * p.mt;
+    p.qa = -expm1f(-p.a);
+    p.compat = (cfg.compat_fermion && sampler == 0) ? 1 : 0;
+    p.cpoly = p.mut * p.mut - 0.5f * p.mt * p.mt;
+    p.rmax = 1.0f;
+    if (p.compat) {
+        const float amu = fabsf(p.mut);
+        if (p.boson) {
+            p.rmax = 1.0f + (p.mut < 0.0f ? 2.0f * amu * kTwoOverE10 / (p.mt * p.mt) : 0.0f);
+        } else {
+            const float r = 1.0f - p.mut / p.mt;
+            const float C = fmaxf(1.0f, 2.0f * r * r);
+            const float aa = fmaxf(p.a, 0.1f);
+            const float x2 = (p.a >= 0.1f) ? aa * expf(-10.0f * aa) : 0.5f * kTwoOverE10;
+            p.rmax = 1.0f + C * 2.0f / expm1f(fmaxf(p.a, 1e-12f)) + 8.0f * amu * x2 / (p.mt * p.mt);
+        }
+    }
+    p.inv_dsfac = 1.0f / (fabsf(p.da.x) + sqrtf(p.da.y * p.da.y + p.da.z * p.da.z + p.da.w * p.da.w));
+    p.pxx = pi1.x;
+    p.pxy = pi1.y;
+    p.pxz = pi1.z;
+    p.pyy = pi1.w;
+    p.pyz = pi2.x;
+    p.shear_c = 0.0f;
+    p.shear_over_p0T = 0;
+    if (cfg.include_shear) {
+        if (cfg.neos_kind == 1) {
+            p.shear_c = 1.0f / (2.0f * cf.z * T);
+            p.shear_over_p0T = 1;
+        } else if (cfg.neos_kind == 0) {
+            p.shear_c = cf.x;
+        } else {
+            p.shear_c = 1.0f / (2.0f * T * T * (th2.x + th2.y));
+        }
+    }
+    p.bi0 = p.b0 = p.b1 = p.b2 = 0.0f;
+    if (cfg.include_bulk) {
+        if (cfg.bulk_kind == 11) {
+            const float Pi = th2.w;
+            p.b0 = Pi * cf.x * m * m;
+            p.b1 = Pi * cf.y * static_cast<float>(sp.baryon);
+            p.b2 = Pi * cf.z;
+        } else if (cfg.bulk_kind == 21 || cfg.bulk_kind == 1) {
+            const float Pi = (cfg.bulk_kind == 1) ? th2.w / 0.197327053f : th2.w;
+            p.bi0 = -cf.x * Pi * m * m / (3.0f * T);
+            p.b1 = cf.x * Pi * cf.y / T;
+        }
+    }
+    p.qx = p.qy = p.qz = p.pq = p.Bq = 0.0f;
+    if (cfg.include_diff) {
+        const float ik = 1.0f / cf.w;
+        p.qx = pi2.y * ik;
+        p.qy = pi2.z * ik;
+        p.qz = pi2.w * ik;
+        p.pq = th2.z / (th2.x + th2.y);
+        p.Bq = static_cast<float>(sp.baryon);
+    }
+    return true;
+}
+
+__device__ float compat_ratio(const Prop& p, float Et) {
+    const float q = expf(-Et);
+    float e = 1.0f, S1 = 0.0f, S2 = 0.0f;
+#pragma unroll
+    for (int n = 1; n <= 10; n++) {
+        e *= q;
+        S2 += e;
+        S1 += (p.boson || (n & 1)) ? e : -e;
+    }
+    const float finf = p.boson ? q / (-expm1f(-Et)) : q / (1.0f + q);
+    const float num = Et * Et * S2 + 2.0f * p.mut * Et * S1 + p.cpoly * finf;
+    const float den = (Et * Et + 2.0f * p.mut * Et + p.cpoly) * finf;
+    return num / den;
+}
+
+// One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
+// the uniform used for the rapidity of boost-invariant surfaces.
+__device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, const Unit& u,
+                                         int s, float4& pl, float& u_rap, unsigned& violations) {
+    const uint32_t c3 = static_cast<uint32_t>(s) | (kTagTry << 16);
+    const uint4 A = block(2u * u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    const float sel = u01f(A.x) * p.W;
+    float prod = u01f_pos(A.y);
+    if (sel < p.w32) prod *= u01f_pos(A.z);
+    if (sel < p.w3) prod *= u01f_pos(A.w);
+    const float K = -logf(prod);
+    if (K > p.Kmax) return false;
+    const uint4 B = block(2u * u.t + 1u, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    const float k2 = K * (K + 2.0f * p.mt);
+    const float Et = K + p.mt;
+    const float ptil = sqrtf(k2);
+    const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
+    const float Etil = p.a + K;
+    const float em = expf(-Etil);
+    const float a_q = p.boson ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
+    float a_c = 1.0f;
+    if (p.compat) {
+        a_c = compat_ratio(p, Etil) / p.rmax;
+        if (a_c > 1.0f) {
+            violations++;
+            a_c = 1.0f;
+        }
+    }
+    const float cth = 2.0f * u01f(B.x) - 1.0f;
+    const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
+    float sphi, cphi;
+    sincospif(2.0f * u01f(B.y), &sphi, &cphi);
+    const float T = p.T;
+    const float pm = T * ptil;
+    const float p0 = T * Et;
+    const float px = pm * sth * cphi;
+    const float py = pm * sth * sphi;
+    const float pz = pm * cth;
+    const float pdsigma = p0 * p.da.x + px * p.da.y + py * p.da.z + pz * p.da.w;
+    const float sgn = static_cast<float>(p.sign);
+    const float f0 = em / (1.0f + sgn * em);
+    const float one_m = 1.0f - sgn * f0;
+    float df = 0.0f;
+    if (cfg.include_shear) {
+        const float Wf = px * px * p.pxx + 2.0f * px * py * p.pxy + 2.0f * px * pz * p.pxz +
+                         py * py * p.pyy + 2.0f * py * pz * p.pyz + pz * pz * (-p.pxx - p.pyy);
+        float ds = one_m * Wf * p.shear_c;
+        if (p.shear_over_p0T) ds /= p0;
+        df += ds;
+    }
+    if (cfg.include_bulk) {
+        df += one_m * (p.bi0 / p0 + p.b0 + p.b1 * p0 + p.b2 * p0 * p0);
+    }
+    if (cfg.include_diff) {
+        const float qf = -(px * p.qx + py * p.qy + pz * p.qz);
+        df += one_m * (p.pq - p.Bq / p0) * qf;
+    }
+    const float fact1 = clamp01(pdsigma / p0 * p.inv_dsfac);
+    const float fact2 = clamp01((1.0f + df) * 0.5f);
+    const float acc = a_pE * a_q * a_c * fact1 * fact2;
+    if (!(u01f(B.z) < acc)) return false;
+    pl = make_float4(p0, px, py, pz);
+    u_rap = u01f(B.w);
+    return true;
+}
+
+__device__ __forceinline__ void write_hadron(HadronRec* out, int64_t slot, int pid, float mass,
+                                             float E, float px, float py, float pz, float t,
+                                             float x, float y, float z) {
+    // 40-byte records are 8-byte aligned: five 8-byte stores
+    float2* o = reinterpret_cast<float2*>(out + slot);
+    o[0] = make_float2(__int_as_float(pid), mass);
+    o[1] = make_float2(E, px);
+    o[2] = make_float2(py, pz);
+    o[3] = make_float2(t, x);
+    o[4] = make_float2(y, z);
+}
+
+__device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& p, int l, int pid,
+                     float4 pl, float u_rap, HadronRec* out, int64_t slot) {
+    const float4 u = cells.u[l];
+    const float4 pos = cells.pos[l];
+    const float pdu = pl.y * u.y + pl.z * u.z + pl.w * u.w;
+    const float c = pdu / (u.x + 1.0f) + pl.x;
+    const float lx = pl.y + c * u.y;
+    const float ly = pl.z + c * u.z;
+    const float lz = pl.w + c * u.w;
+    const float mT2 = p.m * p.m + lx * lx + ly * ly;
+    float eta_s, pz, E;
+    if (cfg.hydro_mode == 2) {
+        eta_s = pos.w;
+        pz = lz;
+        E = sqrtf(mT2 + lz * lz);
+    } else {
+        const float mT = sqrtf(mT2);
+        const float rap = cfg.y_lb + (cfg.y_rb - cfg.y_lb) * u_rap;
+        const float y = asinhf(lz / mT);
+        eta_s = rap - (y - pos.w);
+        float sr, cr;
+        sr = sinhf(rap);
+        cr = coshf(rap);
+        pz = mT * sr;
+        E = mT * cr;
+    }
+    write_hadron(out, slot, pid, p.m, E, lx, ly, pz, pos.x * coshf(eta_s), pos.y, pos.z,
+                 pos.x * sinhf(eta_s));
+}
+
+constexpr int kSampleThreads = 256;
+constexpr int kChunk = 128;
+
+__global__ void __launch_bounds__(kSampleThreads)
+sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
+               const int32_t* __restrict__ pids, const double* __restrict__ cdf,
+               const double* __restrict__ totals, const int64_t* __restrict__ offsets,
+               int64_t n_units, HadronRec* __restrict__ out,
+               unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t nseg = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
+    const int64_t ncell = cfg.n_cells;
+    int64_t next = 0, end = 0;
+    bool exhausted = false;
+    bool active = false;
+    Unit u;
+    Prop p;
+    int pid = 0;
+    unsigned long long n_tries = 0, n_redraws = 0, n_fail = 0;
+    unsigned n_viol = 0;
+
+    for (;;) {
+        // hand out units to the lanes that have none
+        for (;;) {
+            const unsigned need = __ballot_sync(FULL, !active);
+            if (need == 0 || exhausted) break;
+            if (next >= end) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(work_counter, static_cast<unsigned long long>(kChunk));
+                base = __shfl_sync(FULL, base, 0);
+                if (static_cast<int64_t>(base) >= n_units) {
+                    exhausted = true;
+                    break;
+                }
+                next = static_cast<int64_t>(base);
+                end = min(next + kChunk, n_units);
+            }
+            const int64_t avail = end - next;
+            const int rank = __popc(need & ((1u << lane) - 1u));
+            if (!active && rank < avail) {
+                const int64_t h = next + rank;
+                // segment (event, species) of unit h
+                int64_t lo = 0, hi = nseg;
+                while (hi - lo > 1) {
+                    const int64_t mid = (lo + hi) >> 1;
+                    if (offsets[mid] <= h) lo = mid; else hi = mid;
+                }
+                const int e = static_cast<int>(lo / cfg.n_species);
+                u.s = static_cast<int>(lo % cfg.n_species);
+                u.slot = h;
+                u.i = static_cast<uint32_t>(h - offsets[lo]);
+                u.eg = cfg.event_offset + static_cast<uint32_t>(e);
+                u.redraw = 0;
+                u.t = 0;
+                u.tries_cell = 0;
+                u.cell = -1;
+                pid = pids[u.s];
+                active = true;
+            }
+            next += min(static_cast<int64_t>(__popc(need)), avail);
+        }
+        if (__ballot_sync(FULL, active) == 0) break;
+        if (active) {
+            const SpeciesDev sp = species[u.s];
+            if (u.cell < 0 || u.tries_cell >= cfg.max_tries) {
+                if (u.cell >= 0) {
+                    u.redraw++;
+                    n_redraws++;
+                }
+                if (u.redraw > cfg.max_redraws) {
+                    write_hadron(out, u.slot, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                    n_fail++;
+                    active = false;
+                    continue;
+                }
+                const uint4 w = block(static_cast<uint32_t>(u.redraw), u.i, u.eg,
+                                      static_cast<uint32_t>(u.s) | (kTagCell << 16), cfg.key0,
+                                      cfg.key1);
+                const double* row = cdf + static_cast<int64_t>(u.s) * (ncell + 1);
+                const double v = u53(w.x, w.y) * (totals[u.s] - 1e-15);
+                int l = cell_search(row, ncell, v);
+                l = max(0, min(l, static_cast<int>(ncell - 1)));
+                u.cell = l;
+                u.tries_cell = 0;
+                if (!setup_prop(cfg, cells, sp, l, p)) {
+                    atomicCAS(&ctrs->error_code, 0, 1);
+                    ctrs->error_species = u.s;
+                    write_hadron(out, u.slot, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                    n_fail++;
+                    active = false;
+                    continue;
+                }
+            }
+            float4 pl;
+            float u_rap;
+            const bool ok = try_once(cfg, p, u, u.s, pl, u_rap, n_viol);
+            u.t++;
+            u.tries_cell++;
+            n_tries++;
+            if (ok) {
+                emit(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
+                active = false;
+            }
+        }
+    }
+    // warp-aggregated counters
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_tries += __shfl_down_sync(FULL, n_tries, o);
+        n_redraws += __shfl_down_sync(FULL, n_redraws, o);
+        n_fail += __shfl_down_sync(FULL, n_fail, o);
+        n_viol += __shfl_down_sync(FULL, n_viol, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&ctrs->tries, n_tries);
+        if (n_redraws) atomicAdd(&ctrs->redraws, n_redraws);
+        if (n_fail) atomicAdd(&ctrs->failures, n_fail);
+        if (n_viol) atomicAdd(&ctrs->bound_violations, static_cast<unsigned long long>(n_viol));
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_counts(const DevConfig& cfg, const double* totals, int32_t* counts,
+                          int* error, cudaStream_t stream) {
+    const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
+    if (total <= 0) return cudaSuccess;
+    const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
+    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, counts, error);
+    return cudaGetLastError();
+}
+
+int offsets_num_tiles(int64_t n) { return static_cast<int>((n + kOffTile - 1) / kOffTile); }
+
+cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_sum,
+                                int64_t* offsets, cudaStream_t stream) {
+    const int nt = offsets_num_tiles(n);
+    if (nt == 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), stream);
+    off_tile_sum_kernel<<<nt, kOffThreads, 0, stream>>>(counts, n, tile_sum);
+    off_tile_offset_kernel<<<1, kOffThreads, 0, stream>>>(tile_sum, nt, offsets, n);
+    off_tile_scan_kernel<<<nt, kOffThreads, 0, stream>>>(counts, n, tile_sum, offsets);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
+                           const int32_t* pids, const double* cdf, const double* totals,
+                           const int64_t* offsets, int64_t n_units, HadronRec* out,
+                           unsigned long long* work_counter, SampleCounters* counters,
+                           int num_sms, cudaStream_t stream) {
+    if (n_units <= 0) return cudaSuccess;
+    const int per_sm = 4;
+    int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
+    const int64_t needed = (n_units + kChunk - 1) / kChunk;
+    const int64_t warps_needed = needed;
+    const int64_t max_blocks = (warps_needed + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (blocks < 1) blocks = 1;
+    sampler_kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
+        cfg, cells, sp, pids, cdf, totals, offsets, n_units, out, work_counter, counters);
+    return cudaGetLastError();
+}
+
+}  // namespace iss

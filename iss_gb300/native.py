@@ -1,0 +1,278 @@
+"""ctypes binding of the C ABI (include/iss_gpu.h) and a Python class with
+the method names of the reference's driver class iSS (src/iSS.h:16-102).
+
+There is no CPU path: every call runs through iss_gb300/_native/libiss_gb300.so
+and the GPU kernels behind it; if the library is missing the import fails
+with instructions to build it."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_native", "libiss_gb300.so")
+TABLE_DIR = os.path.join(HERE, "data", "iSS_tables")
+
+HADRON_DTYPE = np.dtype([("pid", "<i4"), ("mass", "<f4"), ("E", "<f4"), ("px", "<f4"),
+                         ("py", "<f4"), ("pz", "<f4"), ("t", "<f4"), ("x", "<f4"),
+                         ("y", "<f4"), ("z", "<f4")])
+
+ISS_OK = 0
+STATUS = {0: "ISS_OK", 1: "ISS_ERR_INVALID_ARG", 2: "ISS_ERR_IO", 3: "ISS_ERR_PARAM_MISSING",
+          4: "ISS_ERR_UNSUPPORTED", 5: "ISS_ERR_CUDA", 6: "ISS_ERR_OUT_OF_RANGE",
+          7: "ISS_ERR_NO_SURFACE", 8: "ISS_ERR_NO_SAMPLES", 9: "ISS_ERR_CAPACITY",
+          10: "ISS_ERR_SAMPLING"}
+OUTPUT_OSCAR, OUTPUT_GZIP, OUTPUT_BINARY = 1, 2, 3
+
+EXPORTED = [
+    "iss_gpu_create", "iss_gpu_destroy", "iss_gpu_set_param", "iss_gpu_get_param",
+    "iss_gpu_parse_param_line", "iss_gpu_set_seed", "iss_gpu_set_seed_from_params",
+    "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_generate", "iss_gpu_shell",
+    "iss_gpu_clear", "iss_gpu_num_events", "iss_gpu_num_particles", "iss_gpu_get_hadron",
+    "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output", "iss_gpu_species",
+    "iss_gpu_species_yields", "iss_gpu_num_cells", "iss_gpu_copy_lrf_cells",
+    "iss_gpu_copy_cell_yields", "iss_gpu_copy_counts", "iss_gpu_get_timings",
+    "iss_gpu_last_error", "iss_gpu_status_string",
+]
+
+
+class Timings(C.Structure):
+    _fields_ = [("ms_prologue", C.c_double), ("ms_yields", C.c_double), ("ms_cdf", C.c_double),
+                ("ms_counts", C.c_double), ("ms_sample", C.c_double), ("ms_total", C.c_double),
+                ("n_hadrons", C.c_int64), ("n_tries", C.c_int64),
+                ("n_cell_redraws", C.c_int64), ("n_failures", C.c_int64),
+                ("kernel_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class IssError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded native library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with "
+                              "`python -c 'import __graft_entry__ as g; g.build()'` "
+                              "or `python iss_gb300/build.py`")
+        L = C.CDLL(LIB_PATH)
+        v, h = C.c_void_p, C.c_void_p
+        L.iss_gpu_create.argtypes = [C.c_char_p] * 5 + [C.POINTER(C.c_void_p)]
+        L.iss_gpu_destroy.argtypes = [h]
+        L.iss_gpu_set_param.argtypes = [h, C.c_char_p, C.c_double]
+        L.iss_gpu_get_param.argtypes = [h, C.c_char_p, C.POINTER(C.c_double)]
+        L.iss_gpu_parse_param_line.argtypes = [h, C.c_char_p]
+        L.iss_gpu_set_seed.argtypes = [h, C.c_int64]
+        L.iss_gpu_set_seed_from_params.argtypes = [h]
+        L.iss_gpu_read_surface.argtypes = [h]
+        L.iss_gpu_set_surface.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_generate.argtypes = [h]
+        L.iss_gpu_shell.argtypes = [h]
+        L.iss_gpu_clear.argtypes = [h]
+        L.iss_gpu_num_events.argtypes = [h, C.POINTER(C.c_int32)]
+        L.iss_gpu_num_particles.argtypes = [h, C.c_int32, C.POINTER(C.c_int64)]
+        L.iss_gpu_get_hadron.argtypes = [h, C.c_int32, C.c_int64, v]
+        L.iss_gpu_copy_event.argtypes = [h, C.c_int32, v, C.c_int64, C.POINTER(C.c_int64)]
+        L.iss_gpu_copy_all.argtypes = [h, v, C.c_int64, v, C.POINTER(C.c_int64)]
+        L.iss_gpu_write_output.argtypes = [h, C.c_int, C.c_char_p]
+        L.iss_gpu_species.argtypes = [h, C.POINTER(C.c_int32), v, C.c_int32]
+        L.iss_gpu_species_yields.argtypes = [h, v, C.c_int32]
+        L.iss_gpu_num_cells.argtypes = [h, C.POINTER(C.c_int64)]
+        L.iss_gpu_copy_lrf_cells.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_copy_cell_yields.argtypes = [h, C.c_int32, v, C.c_int64]
+        L.iss_gpu_copy_counts.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_get_timings.argtypes = [h, C.POINTER(Timings)]
+        L.iss_gpu_last_error.argtypes = [h]
+        L.iss_gpu_last_error.restype = C.c_char_p
+        L.iss_gpu_status_string.argtypes = [C.c_int]
+        L.iss_gpu_status_string.restype = C.c_char_p
+        for name in EXPORTED:
+            if name not in ("iss_gpu_last_error", "iss_gpu_status_string"):
+                getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class iSS:
+    """The reference's iSS driver (src/iSS.h), GPU-backed.
+
+    iSS(path, table_path, particle_table_path, inputfile, surface_filename)
+    reads `inputfile` with ParameterReader rules; table paths default to the
+    tables shipped in iss_gb300/data."""
+
+    def __init__(self, path=".", table_path=TABLE_DIR, particle_table_path=None,
+                 inputfile="", surface_filename="surface.dat"):
+        self._L = lib()
+        h = C.c_void_p()
+        pt = particle_table_path or table_path
+        st = self._L.iss_gpu_create(path.encode(), table_path.encode(), pt.encode(),
+                                    inputfile.encode(), surface_filename.encode(), C.byref(h))
+        if st != ISS_OK:
+            raise IssError(st, f"can not create sampler (parameter file {inputfile!r})")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.iss_gpu_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        if st != ISS_OK:
+            raise IssError(st, self._L.iss_gpu_last_error(self._h).decode())
+        return st
+
+    # ParameterReader
+    def setVal(self, key, value):
+        self._check(self._L.iss_gpu_set_param(self._h, key.encode(), float(value)))
+
+    def getVal(self, key, default=None):
+        v = C.c_double()
+        st = self._L.iss_gpu_get_param(self._h, key.encode(), C.byref(v))
+        if st != ISS_OK:
+            if default is not None:
+                return default
+            self._check(st)
+        return v.value
+
+    def readFromArguments(self, args):
+        for a in args:
+            self._check(self._L.iss_gpu_parse_param_line(self._h, a.encode()))
+
+    def set_params(self, **kw):
+        for k, v in kw.items():
+            self.setVal(k, v)
+
+    # iSS
+    def set_random_seed(self, seed=None):
+        if seed is None:
+            self._check(self._L.iss_gpu_set_seed_from_params(self._h))
+        else:
+            self._check(self._L.iss_gpu_set_seed(self._h, int(seed)))
+
+    def read_in_FO_surface(self):
+        return self._check(self._L.iss_gpu_read_surface(self._h))
+
+    def set_surface(self, fo_surf_records):
+        a = np.ascontiguousarray(fo_surf_records, dtype=np.float32)
+        assert a.ndim == 2 and a.shape[1] == 34
+        self._check(self._L.iss_gpu_set_surface(self._h, _ptr(a), a.shape[0]))
+
+    def generate_samples(self):
+        return self._check(self._L.iss_gpu_generate(self._h))
+
+    def shell(self):
+        return self._check(self._L.iss_gpu_shell(self._h))
+
+    def clear(self):
+        self._check(self._L.iss_gpu_clear(self._h))
+
+    def get_number_of_sampled_events(self):
+        n = C.c_int32()
+        self._check(self._L.iss_gpu_num_events(self._h, C.byref(n)))
+        return n.value
+
+    def get_number_of_particles(self, iev):
+        n = C.c_int64()
+        self._check(self._L.iss_gpu_num_particles(self._h, iev, C.byref(n)))
+        return n.value
+
+    def get_hadron(self, iev, ipart):
+        out = np.zeros(1, dtype=HADRON_DTYPE)
+        self._check(self._L.iss_gpu_get_hadron(self._h, iev, ipart, _ptr(out)))
+        return out[0]
+
+    def get_hadron_list_iev(self, iev):
+        n = C.c_int64()
+        self._check(self._L.iss_gpu_copy_event(self._h, iev, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=HADRON_DTYPE)
+        if n.value:
+            self._check(self._L.iss_gpu_copy_event(self._h, iev, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def all_hadrons(self, out=None):
+        """(hadrons, event_offsets): every event in one device->host copy."""
+        n = C.c_int64()
+        nev = self.get_number_of_sampled_events()
+        off = np.zeros(nev + 1, dtype=np.int64)
+        self._check(self._L.iss_gpu_copy_all(self._h, None, 0, _ptr(off), C.byref(n)))
+        if out is None or out.size < n.value:
+            out = np.zeros(n.value, dtype=HADRON_DTYPE)
+        if n.value:
+            self._check(self._L.iss_gpu_copy_all(self._h, _ptr(out), out.size, None, C.byref(n)))
+        return out[:n.value], off
+
+    def write_output(self, fmt, filename=None):
+        self._check(self._L.iss_gpu_write_output(self._h, fmt,
+                                                 filename.encode() if filename else None))
+
+    # inspection
+    def species(self):
+        n = C.c_int32()
+        self._check(self._L.iss_gpu_species(self._h, C.byref(n), None, 0))
+        out = np.zeros(n.value, dtype=np.int32)
+        self._check(self._L.iss_gpu_species(self._h, C.byref(n), _ptr(out), n.value))
+        return out
+
+    def species_yields(self):
+        n = len(self.species())
+        out = np.zeros(n, dtype=np.float64)
+        self._check(self._L.iss_gpu_species_yields(self._h, _ptr(out), n))
+        return out
+
+    def num_cells(self):
+        n = C.c_int64()
+        self._check(self._L.iss_gpu_num_cells(self._h, C.byref(n)))
+        return n.value
+
+    def lrf_cells(self):
+        n = self.num_cells()
+        out = np.zeros((n, 28), dtype=np.float32)
+        self._check(self._L.iss_gpu_copy_lrf_cells(self._h, _ptr(out), n))
+        return out
+
+    def cell_yields(self, species_index=None):
+        n = self.num_cells()
+        if species_index is not None:
+            out = np.zeros(n, dtype=np.float32)
+            self._check(self._L.iss_gpu_copy_cell_yields(self._h, species_index, _ptr(out), n))
+            return out
+        ns = len(self.species())
+        out = np.zeros((ns, n), dtype=np.float32)
+        for k in range(ns):
+            self._check(self._L.iss_gpu_copy_cell_yields(self._h, k, _ptr(out[k]), n))
+        return out
+
+    def counts(self):
+        nev = self.get_number_of_sampled_events()
+        ns = len(self.species())
+        out = np.zeros((nev, ns), dtype=np.int32)
+        self._check(self._L.iss_gpu_copy_counts(self._h, _ptr(out), out.size))
+        return out
+
+    def timings(self):
+        t = Timings()
+        self._check(self._L.iss_gpu_get_timings(self._h, C.byref(t)))
+        return t.as_dict()

@@ -1,0 +1,148 @@
+"""GPU parity against the reference's golden yields and the oracle.
+
+* local-rest-frame cells and per-cell yields against the reference's own
+  FP64 values (golden files made by the reference binary);
+* per-species yields within 1e-6 relative of the FP64 reference;
+* counts bit-exact against the oracle's replay on the same Philox streams;
+* every hadron against the oracle's FP64 replay of the GPU sampler (PDG ids
+  bit-exact, momenta to FP32 rounding; a proposal whose acceptance lands
+  within FP32 rounding of its uniform may flip, which is counted).
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from iss_gb300 import iSS, surfaces as S
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["ideal_boost_invariant", "viscous_14moment", "viscous_rta", "viscous_boltzmann",
+         "viscous_ce_smash", "diffusion_smash"]
+
+# FP32 tolerances (FP64 reference): per cell, and per species summed over cells
+CELL_RTOL = 1e-5
+TOTAL_RTOL = 1e-6
+
+
+def run_golden_case(g, n_events=4, seed=17, extra=None):
+    surf = S.Surface(g["records"], hydro_mode=int(g["hydro_mode"]), eos=int(g["eos"]),
+                     bulk=int(g["music"][0]), rhob=int(g["music"][1]), diff=int(g["music"][2]))
+    d = tempfile.mkdtemp()
+    S.write_music_binary(os.path.join(d, "surface.dat"), surf.records)
+    S.write_music_input(d, surf)
+    s = iSS(d)
+    params = dict(S.DEFAULT_PARAMETERS)
+    params.update(g["params"])
+    params["number_of_repeated_sampling"] = n_events
+    if extra:
+        params.update(extra)
+    s.set_params(**params)
+    s.read_in_FO_surface()
+    s.set_random_seed(seed)
+    s.generate_samples()
+    return s, params
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_lrf_cells_match_reference(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    s, _ = run_golden_case(g)
+    lrf = s.lrf_cells()
+    kept = lrf[lrf[:, 4] >= 0]
+    ref = g["lrf"]
+    assert kept.shape == ref.shape
+    scale = np.maximum(np.abs(ref).max(0), 1e-30)
+    err = np.abs(kept - ref) / scale
+    assert err.max() < 2e-6, f"LRF cells differ by {err.max():.2e} (column {err.max(0).argmax()})"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_yields_match_reference(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    s, _ = run_golden_case(g)
+    lrf = s.lrf_cells()
+    keep = lrf[:, 4] >= 0
+    y = s.cell_yields()[:, keep].astype(np.float64)
+    ref = g["yields"]
+    assert y.shape == ref.shape
+    big = ref > 1e-30 * ref.max()
+    rel = np.abs(y[big] - ref[big]) / ref[big]
+    assert rel.max() < CELL_RTOL, f"per-cell yields differ by {rel.max():.2e}"
+    tot = s.species_yields()
+    rt = ref.sum(1)
+    m = rt > 0
+    trel = np.abs(tot[m] - rt[m]) / rt[m]
+    assert trel.max() < TOTAL_RTOL, f"per-species yields differ by {trel.max():.2e}"
+
+
+@pytest.mark.parametrize("name", ["viscous_14moment", "ideal_boost_invariant", "diffusion_smash",
+                                  "viscous_ce_smash"])
+def test_counts_and_hadrons_match_oracle_replay(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    n_events = 200 if name != "ideal_boost_invariant" else 20
+    s, params = run_golden_case(g, n_events=n_events, seed=2024)
+    lrf = s.lrf_cells()
+    tot = s.species_yields()
+    cnt = s.counts()
+    sp = g["species"]
+    oc = O.OracleConfig(params, S.TABLE_DIR, afterburner=(2 if int(g["eos"]) == 91 else None),
+                        n_events=n_events, seed=2024)
+    assert np.array_equal(cnt, O.counts(oc, sp, tot))
+    y = s.cell_yields()
+    cdf, tot_o = O.cdf(y)
+    assert np.allclose(tot_o, tot, rtol=1e-12, atol=0)
+    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
+    had, off = s.all_hadrons()
+    rep, st = O.sample_replay(oc, sp, lrf, coef, cdf, tot, cnt)
+    assert len(had) == len(rep) == cnt.sum() > 0
+    assert np.array_equal(had["pid"], rep["pid"])
+    assert np.array_equal(off[1:] - off[:-1], cnt.sum(1))
+    same = np.ones(len(had), dtype=bool)
+    for k in ("E", "px", "py", "pz", "t", "x", "y", "z"):
+        same &= np.isclose(had[k], rep[k], rtol=2e-4, atol=2e-4)
+    frac = 1.0 - same.mean()
+    assert frac < 2e-3, f"{frac:.2e} of {len(had)} hadrons differ from the replay"
+    t = s.timings()
+    assert t["n_failures"] == 0
+
+
+def test_run_to_run_reproducible():
+    g = O.load_golden("yields_viscous_14moment.npz")
+    a, _ = run_golden_case(g, n_events=50, seed=77)
+    b, _ = run_golden_case(g, n_events=50, seed=77)
+    ha, _ = a.all_hadrons()
+    hb, _ = b.all_hadrons()
+    assert ha.tobytes() == hb.tobytes()
+    c, _ = run_golden_case(g, n_events=50, seed=78)
+    hc, _ = c.all_hadrons()
+    assert ha.tobytes() != hc.tobytes()
+
+
+def test_event_offset_sharding_reproduces_single_run():
+    """Events [0, 40) in one run equal events [0, 20) + [20, 40) run as two
+    shards with gpu_event_offset (the multi-GPU partitioning)."""
+    g = O.load_golden("yields_viscous_14moment.npz")
+    full, _ = run_golden_case(g, n_events=40, seed=5)
+    h_full, off_full = full.all_hadrons()
+    parts = []
+    for e0 in (0, 20):
+        s, _ = run_golden_case(g, n_events=20, seed=5, extra={"gpu_event_offset": e0})
+        parts.append(s.all_hadrons()[0])
+    assert np.concatenate(parts).tobytes() == h_full.tobytes()
+
+
+def test_reference_accessors():
+    g = O.load_golden("yields_viscous_14moment.npz")
+    s, _ = run_golden_case(g, n_events=5, seed=3)
+    nev = s.get_number_of_sampled_events()
+    assert nev == 5
+    h_all, off = s.all_hadrons()
+    for iev in range(nev):
+        ev = s.get_hadron_list_iev(iev)
+        assert len(ev) == s.get_number_of_particles(iev) == off[iev + 1] - off[iev]
+        assert ev.tobytes() == h_all[off[iev]:off[iev + 1]].tobytes()
+        if len(ev):
+            assert s.get_hadron(iev, len(ev) - 1).tobytes() == ev[-1].tobytes()

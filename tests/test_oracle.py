@@ -1,0 +1,123 @@
+"""The oracle pinned against the reference (CPU only).
+
+The golden files in tests/golden were produced by the reference compiled from
+its own sources (tests/golden/make_golden.py); the oracle must reproduce its
+local-rest-frame cells and its per-cell FP64 yields bit for bit."""
+import numpy as np
+import pytest
+import scipy.special as sp
+
+import oracle_lib as O
+from iss_gb300 import surfaces as S
+
+CASES = ["ideal_boost_invariant", "viscous_14moment", "viscous_rta", "viscous_boltzmann",
+         "viscous_ce_smash", "diffusion_smash"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_yields_bit_exact_vs_reference(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    p = g["params"]
+    oc = O.OracleConfig(p, S.TABLE_DIR, n_events=1)
+    y = O.yields(oc, g["species"], g["lrf"])
+    assert np.array_equal(y, g["yields"]), "oracle yields differ from the reference"
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if c != "viscous_ce_smash"])
+def test_lrf_cells_bit_exact_vs_reference(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    fo = S.music_to_fo_surf(g["records"], int(g["hydro_mode"]))
+    lrf, keep = O.lrf_cells(fo)
+    kept = lrf[keep == 1]
+    assert np.array_equal(kept.view(np.uint32), g["lrf"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_species_order_vs_reference(name):
+    g = O.load_golden(f"yields_{name}.npz")
+    p = g["params"]
+    ab = 2 if int(g["eos"]) == 91 else int(p.get("afterburner_type", 0))
+    sp_ = O.chosen_species(S.TABLE_DIR, ab, int(p.get("quantum_statistics", 1)))
+    assert np.array_equal(sp_, g["species"])
+
+
+def test_special_function_tables_vs_scipy():
+    K = np.zeros(O.SF_LEN * 3)
+    E = np.zeros(O.SF_LEN * 9)
+    O.lib().orc_sf_tables(1, 1, O._p(K), O._p(E))
+    x = 0.5 + 0.05 * np.arange(O.SF_LEN)
+    K = K.reshape(-1, 3)
+    E = E.reshape(-1, 9)
+    for j, n in enumerate((1, 2, 3)):
+        ref = sp.kn(n, x)
+        m = ref > 1e-300
+        assert np.max(np.abs(K[m, j] / ref[m] - 1)) < 1e-13
+    for j, n in enumerate([2, 4, 6, 8, 10, 12, 14, 16, 18]):
+        ref = sp.expn(n, x)
+        m = ref > 1e-300
+        assert np.max(np.abs(E[m, j] / ref[m] - 1)) < 1e-13
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 known-answer vectors of the Random123 distribution."""
+    import ctypes as C
+    code = r"""
+#include <stdio.h>
+#include "philox.h"
+int main(void) {
+  uint32_t k1[2] = {0, 0}, c1[4] = {0, 0, 0, 0}, o[4];
+  orc_philox4x32_10(c1, k1, o); printf("%08x %08x %08x %08x\n", o[0], o[1], o[2], o[3]);
+  uint32_t k2[2] = {0xffffffffu, 0xffffffffu}, c2[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+  orc_philox4x32_10(c2, k2, o); printf("%08x %08x %08x %08x\n", o[0], o[1], o[2], o[3]);
+  uint32_t k3[2] = {0xa4093822u, 0x299f31d0u}, c3[4] = {0x243f6a88u, 0x85a308d3u, 0x13198a2eu, 0x03707344u};
+  orc_philox4x32_10(c3, k3, o); printf("%08x %08x %08x %08x\n", o[0], o[1], o[2], o[3]);
+  return 0;
+}
+"""
+    import os
+    import subprocess
+    import tempfile
+    d = tempfile.mkdtemp()
+    src = os.path.join(d, "kat.c")
+    open(src, "w").write(code)
+    subprocess.check_call(["gcc", "-O1", "-I", O.ORACLE_DIR, src, "-o", os.path.join(d, "kat")])
+    out = subprocess.check_output([os.path.join(d, "kat")]).decode().split("\n")
+    assert out[0] == "6627e8d5 e169c58d bc57ac4c 9b00dbd8"
+    assert out[1] == "408f276d 41c83b0e a20bc7c6 6d5451fd"
+    assert out[2] == "d16cfe09 94fdcceb 5001e420 24126ea1"
+
+
+def test_oracle_counts_are_poisson():
+    """Counts drawn on the Philox streams follow Poisson(mean) for small and
+    large means (inversion and PTRS branches)."""
+    sp_ = O.chosen_species(S.TABLE_DIR, 0)[:4]
+    totals = np.array([0.7, 5.0, 40.0, 900.0])
+    params = dict(S.DEFAULT_PARAMETERS, hydro_mode=2)
+    oc = O.OracleConfig(params, S.TABLE_DIR, n_events=20000, seed=99)
+    c = O.counts(oc, sp_, totals)
+    for k, mu in enumerate(totals):
+        m, v = c[:, k].mean(), c[:, k].var()
+        se = np.sqrt(mu / c.shape[0])
+        assert abs(m - mu) < 5 * se
+        assert abs(v / mu - 1) < 0.1
+
+
+def test_oracle_replay_respects_counts_and_order():
+    g = O.load_golden("yields_viscous_14moment.npz")
+    p = dict(g["params"], number_of_repeated_sampling=3)
+    oc = O.OracleConfig(p, S.TABLE_DIR, n_events=3, seed=5)
+    lrf = g["lrf"]
+    y = g["yields"].astype(np.float32)
+    cdf, tot = O.cdf(y)
+    cnt = O.counts(oc, g["species"], tot)
+    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
+    had, st = O.sample_replay(oc, g["species"], lrf, coef, cdf, tot, cnt)
+    assert len(had) == cnt.sum()
+    assert st.n_failures == 0
+    # species in mass order inside each event
+    pids = g["species"]["pid"]
+    expected = np.concatenate([np.repeat(pids, cnt[e]) for e in range(3)])
+    assert np.array_equal(had["pid"], expected)
+    # on-shell
+    m2 = had["E"].astype(float) ** 2 - (had["px"].astype(float) ** 2 + had["py"] ** 2 + had["pz"] ** 2)
+    assert np.allclose(np.sqrt(np.maximum(m2, 0)), had["mass"], rtol=1e-3, atol=1e-3)
