@@ -216,7 +216,7 @@ def run_gpu(args, ws, rank, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from iss_gb300 import iSS, surfaces as S
 
-    surf = S.viscous_3d(N_CELLS, seed=SEED_SURFACE)
+    surf = S.viscous_3d(args.cells, seed=SEED_SURFACE)
     fo = surf.fo_surf()
     n_events = args.events
     params = dict(S.DEFAULT_PARAMETERS, **PARAMS)
@@ -330,8 +330,9 @@ def run_gpu(args, ws, rank, local):
                 "ms_per_step": 1e3 * max_sec / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (iss_gb300.surfaces.viscous_3d, seed 2)",
-                "config": {"workload": "viscous_3d_200k_cells_s95p_1000_events",
-                           "cells": N_CELLS, "events_per_gpu": n_events, "species": 319,
+                "config": {"workload": f"viscous_3d_{args.cells // 1000}k_cells_s95p_"
+                                       f"{n_events}_events",
+                           "cells": args.cells, "events_per_gpu": n_events, "species": 319,
                            "bulk_deltaf_kind": 11, "sampler": "plain",
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
@@ -356,6 +357,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--events", type=int, default=N_EVENTS)
+    ap.add_argument("--cells", type=int, default=N_CELLS,
+                    help="surface size (profiling runs use a smaller surface)")
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
