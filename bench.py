@@ -178,7 +178,9 @@ def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int):
 def run_reference(args, ws, rank):
     if rank != 0:
         return
-    import oracle_lib  # noqa: F401  (builds the oracle if needed)
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib
+    oracle_lib.lib()
     n_procs = max(1, os.cpu_count() or 1)
     n_sample = args.cpu_cells
     rates = []
