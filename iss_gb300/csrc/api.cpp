@@ -98,8 +98,8 @@ struct iss_handle {
     DevBuf<int32_t> d_pids;
     DevBuf<float> d_yields;
     DevBuf<double> d_cdf, d_tile_sum, d_tile_off, d_totals;
-    DevBuf<int32_t> d_counts;
-    DevBuf<int64_t> d_offsets, d_off_tiles;
+    DevBuf<int32_t> d_counts, d_items, d_item_seg, d_guide;
+    DevBuf<int64_t> d_offsets, d_off_tiles, d_item_off;
     DevBuf<HadronRec> d_hadrons;
     DevBuf<unsigned long long> d_work;
     DevBuf<SampleCounters> d_counters;
@@ -134,8 +134,12 @@ struct iss_handle {
                                     &d_b14c1, &d_b14c2, &d_ce, &d_qmu};
             for (auto* b : db) b->release();
             d_counts.release();
+            d_items.release();
+            d_item_seg.release();
+            d_guide.release();
             d_offsets.release();
             d_off_tiles.release();
+            d_item_off.release();
             d_hadrons.release();
             d_work.release();
             d_counters.release();
@@ -391,6 +395,7 @@ iss_status run_cells(iss_handle* h) {
     CUDA_TRY(h, h->d_tile_sum.reserve(static_cast<size_t>(nt) * S));
     CUDA_TRY(h, h->d_tile_off.reserve(static_cast<size_t>(nt) * S));
     CUDA_TRY(h, h->d_totals.reserve(static_cast<size_t>(S)));
+    CUDA_TRY(h, h->d_guide.reserve(static_cast<size_t>(cdf_guide_len(n) + 1) * S));
     const CellArrays cells = cell_arrays(h);
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
     CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
@@ -398,7 +403,7 @@ iss_status run_cells(iss_handle* h) {
     CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
     CUDA_TRY(h, launch_cdf(h->d_yields.ptr, S, n, h->d_tile_sum.ptr, h->d_tile_off.ptr,
-                           h->d_totals.ptr, h->d_cdf.ptr, st));
+                           h->d_totals.ptr, h->d_cdf.ptr, h->d_guide.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCdf], st));
     h->yields_valid = true;
     return ISS_OK;
@@ -446,31 +451,40 @@ iss_status run_generate(iss_handle* h) {
 
     const int64_t nseg = static_cast<int64_t>(c.n_events) * S;
     CUDA_TRY(h, h->d_counts.reserve(static_cast<size_t>(std::max<int64_t>(nseg, 1))));
+    CUDA_TRY(h, h->d_items.reserve(static_cast<size_t>(std::max<int64_t>(nseg, 1))));
     CUDA_TRY(h, h->d_offsets.reserve(static_cast<size_t>(nseg + 1)));
+    CUDA_TRY(h, h->d_item_off.reserve(static_cast<size_t>(nseg + 1)));
     CUDA_TRY(h, h->d_off_tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(nseg), 1))));
     CUDA_TRY(h, h->d_error.reserve(1));
     CUDA_TRY(h, h->d_work.reserve(1));
     CUDA_TRY(h, h->d_counters.reserve(1));
     CUDA_TRY(h, cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
-    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_counts.ptr, h->d_error.ptr, s));
+    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_counts.ptr, h->d_items.ptr, h->d_error.ptr, s));
     CUDA_TRY(h, launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
-    CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
-    int64_t n_units = 0;
+    CUDA_TRY(h, launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
+    int64_t sizes[2] = {0, 0};   // hadrons, work items
     int count_err = 0;
-    CUDA_TRY(h, cudaMemcpyAsync(&n_units, h->d_offsets.ptr + nseg, sizeof(int64_t),
+    CUDA_TRY(h, cudaMemcpyAsync(&sizes[0], h->d_offsets.ptr + nseg, sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(&sizes[1], h->d_item_off.ptr + nseg, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(&count_err, h->d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaStreamSynchronize(s));
+    const int64_t n_units = sizes[0], n_items = sizes[1];
     if (count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
     if (count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
+    CUDA_TRY(h, h->d_item_seg.reserve(static_cast<size_t>(std::max<int64_t>(n_items, 1))));
+    CUDA_TRY(h, launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
 
     CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
     CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long), s));
     CUDA_TRY(h, cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
     CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
-                               h->d_totals.ptr, h->d_offsets.ptr, n_units, h->d_hadrons.ptr,
-                               h->d_work.ptr, h->d_counters.ptr, h->num_sms, s));
+                               h->d_guide.ptr, cdf_guide_len(h->n_cells), h->d_totals.ptr,
+                               h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr, n_items,
+                               h->d_hadrons.ptr, h->d_work.ptr, h->d_counters.ptr, h->num_sms, s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSample], s));
     // event offsets: offsets[e * S] for e = 0..n_events
     h->event_offsets.assign(static_cast<size_t>(c.n_events) + 1, 0);
@@ -495,7 +509,7 @@ iss_status run_generate(iss_handle* h) {
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures);
-    t.kernel_launches = 10;
+    t.kernel_launches = 14;
     h->n_events = c.n_events;
     h->n_hadrons = n_units;
     h->samples_valid = true;

@@ -300,8 +300,9 @@ cdf_tile_sum_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_offset_kernel(const double* __restrict__ tile_sum, int n_tiles,
-                       double* __restrict__ tile_off, double* __restrict__ totals) {
+cdf_tile_offset_kernel(const double* __restrict__ tile_sum, int n_tiles, int64_t n, int guide_len,
+                       double* __restrict__ tile_off, double* __restrict__ totals,
+                       int32_t* __restrict__ guide) {
     __shared__ double s_warp[33];
     const int s = blockIdx.x;
     double carry = 0.0;
@@ -313,18 +314,32 @@ cdf_tile_offset_kernel(const double* __restrict__ tile_sum, int n_tiles,
         if (i < n_tiles) tile_off[static_cast<int64_t>(s) * n_tiles + i] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) totals[s] = carry;
+    if (threadIdx.x == 0) {
+        totals[s] = carry;
+        int32_t* g = guide + static_cast<int64_t>(s) * (guide_len + 1);
+        g[0] = 0;
+        g[guide_len] = static_cast<int32_t>(n - 1);
+    }
 }
 
+// Writes the FP64 CDF row of species s and scatters its guide table
+// (indexed search, Chen & Asau 1974): bucket j of guide_len covers
+// v in [j, j+1) * total / guide_len and guide[j] is the cell whose CDF
+// interval contains the bucket's left edge, so the cell of any v in bucket j
+// lies in [guide[j], guide[j+1]].  Entries at tile seams may stay unset (-1);
+// the sampler then falls back to a full binary search.
 __global__ void __launch_bounds__(kScanThreads)
 cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
-                     const double* __restrict__ tile_off, double* __restrict__ cdf) {
+                     const double* __restrict__ tile_off, const double* __restrict__ totals,
+                     int guide_len, double* __restrict__ cdf, int32_t* __restrict__ guide) {
     __shared__ float s_in[kScanThreads * (kScanPer + 1)];
     __shared__ double s_warp[33];
+    __shared__ double s_last[kScanThreads];
     const int s = blockIdx.y;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
     const float* row = yields + static_cast<int64_t>(s) * n;
     double* out = cdf + static_cast<int64_t>(s) * (n + 1);
+    int32_t* g = guide + static_cast<int64_t>(s) * (guide_len + 1);
     // coalesced load into a padded layout: element e -> (e / 16) * 17 + e % 16
     for (int k = 0; k < kScanPer; k++) {
         const int e = k * kScanThreads + threadIdx.x;
@@ -338,12 +353,35 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
     for (int k = 0; k < kScanPer; k++) acc += static_cast<double>(mine[k]);
     double tot;
     const double ex = block_excl_scan(acc, s_warp, &tot);
-    double run = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x] + ex;
-    const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kScanPer;
+    const double base = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x];
+    double run = base + ex;
+    double vals[kScanPer];
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
         run += static_cast<double>(mine[k]);
-        if (e0 + k < n) out[e0 + k + 1] = run;
+        vals[k] = run;
+    }
+    s_last[threadIdx.x] = run;
+    __syncthreads();
+    const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kScanPer;
+    // value written just before this thread's first element
+    double prev = threadIdx.x == 0 ? base : s_last[threadIdx.x - 1];
+    const double total = totals[s];
+    const double scale = total > 0.0 ? static_cast<double>(guide_len) / total : 0.0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        const int64_t i = e0 + k;
+        if (i < n) {
+            out[i + 1] = vals[k];
+            if (scale > 0.0 && vals[k] > prev) {
+                int64_t jl = static_cast<int64_t>(floor(prev * scale)) + 1;
+                int64_t jh = static_cast<int64_t>(floor(vals[k] * scale));
+                jl = max(jl, static_cast<int64_t>(1));
+                jh = min(jh, static_cast<int64_t>(guide_len - 1));
+                for (int64_t j = jl; j <= jh; j++) g[j] = static_cast<int32_t>(i);
+            }
+        }
+        prev = vals[k];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = 0.0;
 }
@@ -370,14 +408,24 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
 
 int cdf_num_tiles(int64_t n) { return static_cast<int>((n + kScanTile - 1) / kScanTile); }
 
+int cdf_guide_len(int64_t n) { return static_cast<int>(n < 4 ? 1 : (n + 3) / 4); }
+
 cudaError_t launch_cdf(const float* yields, int n_species, int64_t n, double* tile_sum,
-                       double* tile_off, double* totals, double* cdf, cudaStream_t stream) {
+                       double* tile_off, double* totals, double* cdf, int32_t* guide,
+                       cudaStream_t stream) {
     const int nt = cdf_num_tiles(n);
     if (nt == 0 || n_species == 0) return cudaSuccess;
+    const int glen = cdf_guide_len(n);
+    cudaError_t e = cudaMemsetAsync(guide, 0xFF,
+                                    sizeof(int32_t) * static_cast<size_t>(glen + 1) * n_species,
+                                    stream);
+    if (e != cudaSuccess) return e;
     dim3 grid(static_cast<unsigned>(nt), static_cast<unsigned>(n_species));
     cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, nt, tile_sum);
-    cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, nt, tile_off, totals);
-    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, nt, tile_off, cdf);
+    cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, nt, n, glen, tile_off,
+                                                                   totals, guide);
+    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, nt, tile_off, totals, glen,
+                                                           cdf, guide);
     return cudaGetLastError();
 }
 

@@ -102,8 +102,11 @@ __device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
     return -1.0;
 }
 
+constexpr int kItem = 64;   // hadrons per work item (one (event, species) segment)
+
 __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
-                              int32_t* __restrict__ counts, int* __restrict__ error) {
+                              int32_t* __restrict__ counts, int32_t* __restrict__ items,
+                              int* __restrict__ error) {
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (idx >= total) return;
@@ -136,7 +139,19 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
         nsamp = (dN < 1e-15) ? 0 : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, dN);
         if (nsamp < 0) atomicCAS(error, 0, 3);
     }
-    counts[idx] = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
+    const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
+    counts[idx] = c;
+    items[idx] = (c + kItem - 1) / kItem;
+}
+
+// item -> segment map: item_seg[item_off[seg] + k] = seg for k < items[seg]
+__global__ void item_map_kernel(const int32_t* __restrict__ items, const int64_t* __restrict__ item_off,
+                                int64_t nseg, int32_t* __restrict__ item_seg) {
+    const int64_t seg = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (seg >= nseg) return;
+    const int64_t b = item_off[seg];
+    const int32_t k = items[seg];
+    for (int32_t j = 0; j < k; j++) item_seg[b + j] = static_cast<int32_t>(seg);
 }
 
 // ------------------------------------------------------------------------
@@ -256,10 +271,25 @@ struct Unit {
     uint32_t t;
 };
 
-__device__ __forceinline__ int cell_search(const double* __restrict__ row, int64_t n, double v) {
-    // largest i with row[i] < v <= row[i+1] (binarySearch of src/arsenal.cpp:644-678)
-    int64_t lo = 0, hi = n;
+// largest i with row[i] < v <= row[i+1] (binarySearch of src/arsenal.cpp:644-678),
+// started from the guide table's bucket; falls back to the full range when
+// the bucket is unset or does not bracket v
+__device__ __forceinline__ int cell_search(const double* __restrict__ row, int64_t n,
+                                           const int32_t* __restrict__ g, int glen, double total,
+                                           double v) {
     if (v > row[n]) return static_cast<int>(n - 1);
+    int64_t lo = 0, hi = n;
+    const double scale = total > 0.0 ? static_cast<double>(glen) / total : 0.0;
+    int64_t j = static_cast<int64_t>(floor(v * scale));
+    j = min(max(j, static_cast<int64_t>(0)), static_cast<int64_t>(glen - 1));
+    const int g0 = g[j], g1 = g[j + 1];
+    if (g0 >= 0 && g1 >= g0) {
+        const int64_t a = g0, b = static_cast<int64_t>(g1) + 1;
+        if (row[a] < v && v <= row[b]) {
+            lo = a;
+            hi = b;
+        }
+    }
     while (hi - lo > 1) {
         const int64_t mid = (lo + hi) >> 1;
         if (row[mid] < v) lo = mid; else hi = mid;
@@ -490,19 +520,21 @@ __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& 
 }
 
 constexpr int kSampleThreads = 256;
-constexpr int kChunk = 128;
 
-__global__ void __launch_bounds__(kSampleThreads)
+__global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const double* __restrict__ cdf,
+               const int32_t* __restrict__ guide, int guide_len,
                const double* __restrict__ totals, const int64_t* __restrict__ offsets,
-               int64_t n_units, HadronRec* __restrict__ out,
+               const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
+               int64_t n_items, HadronRec* __restrict__ out,
                unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int64_t nseg = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     const int64_t ncell = cfg.n_cells;
-    int64_t next = 0, end = 0;
+    // the warp's current work item: units [next, end) of segment cur_seg
+    int64_t next = 0, end = 0, seg_base = 0;
+    int cur_seg = 0;
     bool exhausted = false;
     bool active = false;
     Unit u;
@@ -517,31 +549,27 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
             const unsigned need = __ballot_sync(FULL, !active);
             if (need == 0 || exhausted) break;
             if (next >= end) {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(work_counter, static_cast<unsigned long long>(kChunk));
-                base = __shfl_sync(FULL, base, 0);
-                if (static_cast<int64_t>(base) >= n_units) {
+                long long k = 0;
+                if (lane == 0) k = static_cast<long long>(atomicAdd(work_counter, 1ull));
+                k = __shfl_sync(FULL, k, 0);
+                if (k >= n_items) {
                     exhausted = true;
                     break;
                 }
-                next = static_cast<int64_t>(base);
-                end = min(next + kChunk, n_units);
+                cur_seg = item_seg[k];
+                const int64_t j = k - item_off[cur_seg];
+                seg_base = offsets[cur_seg];
+                next = seg_base + j * kItem;
+                end = min(next + kItem, offsets[cur_seg + 1]);
             }
             const int64_t avail = end - next;
             const int rank = __popc(need & ((1u << lane) - 1u));
             if (!active && rank < avail) {
                 const int64_t h = next + rank;
-                // segment (event, species) of unit h
-                int64_t lo = 0, hi = nseg;
-                while (hi - lo > 1) {
-                    const int64_t mid = (lo + hi) >> 1;
-                    if (offsets[mid] <= h) lo = mid; else hi = mid;
-                }
-                const int e = static_cast<int>(lo / cfg.n_species);
-                u.s = static_cast<int>(lo % cfg.n_species);
+                u.s = cur_seg % cfg.n_species;
                 u.slot = h;
-                u.i = static_cast<uint32_t>(h - offsets[lo]);
-                u.eg = cfg.event_offset + static_cast<uint32_t>(e);
+                u.i = static_cast<uint32_t>(h - seg_base);
+                u.eg = cfg.event_offset + static_cast<uint32_t>(cur_seg / cfg.n_species);
                 u.redraw = 0;
                 u.t = 0;
                 u.tries_cell = 0;
@@ -553,7 +581,6 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
         }
         if (__ballot_sync(FULL, active) == 0) break;
         if (active) {
-            const SpeciesDev sp = species[u.s];
             if (u.cell < 0 || u.tries_cell >= cfg.max_tries) {
                 if (u.cell >= 0) {
                     u.redraw++;
@@ -569,12 +596,14 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                                       static_cast<uint32_t>(u.s) | (kTagCell << 16), cfg.key0,
                                       cfg.key1);
                 const double* row = cdf + static_cast<int64_t>(u.s) * (ncell + 1);
-                const double v = u53(w.x, w.y) * (totals[u.s] - 1e-15);
-                int l = cell_search(row, ncell, v);
+                const double tot = totals[u.s];
+                const double v = u53(w.x, w.y) * (tot - 1e-15);
+                int l = cell_search(row, ncell, guide + static_cast<int64_t>(u.s) * (guide_len + 1),
+                                    guide_len, tot, v);
                 l = max(0, min(l, static_cast<int>(ncell - 1)));
                 u.cell = l;
                 u.tries_cell = 0;
-                if (!setup_prop(cfg, cells, sp, l, p)) {
+                if (!setup_prop(cfg, cells, species[u.s], l, p)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     write_hadron(out, u.slot, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
@@ -614,11 +643,11 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
 }  // namespace
 
 cudaError_t launch_counts(const DevConfig& cfg, const double* totals, int32_t* counts,
-                          int* error, cudaStream_t stream) {
+                          int32_t* items, int* error, cudaStream_t stream) {
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (total <= 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
-    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, counts, error);
+    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, counts, items, error);
     return cudaGetLastError();
 }
 
@@ -634,21 +663,29 @@ cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_
     return cudaGetLastError();
 }
 
+cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64_t nseg,
+                            int32_t* item_seg, cudaStream_t stream) {
+    if (nseg <= 0) return cudaSuccess;
+    item_map_kernel<<<static_cast<unsigned>((nseg + 255) / 256), 256, 0, stream>>>(items, item_off,
+                                                                                 nseg, item_seg);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                           const int32_t* pids, const double* cdf, const double* totals,
-                           const int64_t* offsets, int64_t n_units, HadronRec* out,
-                           unsigned long long* work_counter, SampleCounters* counters,
-                           int num_sms, cudaStream_t stream) {
-    if (n_units <= 0) return cudaSuccess;
-    const int per_sm = 4;
+                           const int32_t* pids, const double* cdf, const int32_t* guide,
+                           int guide_len, const double* totals, const int64_t* offsets,
+                           const int64_t* item_off, const int32_t* item_seg, int64_t n_items,
+                           HadronRec* out, unsigned long long* work_counter,
+                           SampleCounters* counters, int num_sms, cudaStream_t stream) {
+    if (n_items <= 0) return cudaSuccess;
+    const int per_sm = 3;
     int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
-    const int64_t needed = (n_units + kChunk - 1) / kChunk;
-    const int64_t warps_needed = needed;
-    const int64_t max_blocks = (warps_needed + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
+    const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
     sampler_kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
-        cfg, cells, sp, pids, cdf, totals, offsets, n_units, out, work_counter, counters);
+        cfg, cells, sp, pids, cdf, guide, guide_len, totals, offsets, item_off, item_seg, n_items,
+        out, work_counter, counters);
     return cudaGetLastError();
 }
 

@@ -331,4 +331,4 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
     return w;
 }
 
-/* Part 3 is implemented in oracle_refsampler.c. */
+

@@ -307,3 +307,20 @@ def load_golden(name):
     d = {k: z[k] for k in z.files}
     d["params"] = json.loads(str(d["params"]))
     return d
+
+
+def reference_sampler(oc: OracleConfig, sp, lrf, keep, seed=1, capacity=None):
+    """The reference's own sampling algorithm (oracle part 3); returns
+    (hadrons, seconds)."""
+    arr = species_array(sp)
+    lrf = np.ascontiguousarray(lrf, dtype=np.float32)
+    kp = np.ascontiguousarray(keep, dtype=np.int32)
+    cap = int(capacity) if capacity is not None else 0
+    out = np.zeros(max(cap, 1), dtype=HADRON_DTYPE)
+    sec = C.c_double()
+    n = lib().orc_reference_sampler(C.byref(oc.cfg), C.cast(arr, C.c_void_p), len(sp), _p(lrf),
+                                    _p(kp), lrf.shape[0], 1, seed, _p(out) if cap else None, cap,
+                                    C.byref(sec))
+    if n < 0:
+        raise RuntimeError(f"orc_reference_sampler status {n}")
+    return out[:min(n, cap)], n, sec.value

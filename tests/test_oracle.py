@@ -121,3 +121,33 @@ def test_oracle_replay_respects_counts_and_order():
     # on-shell
     m2 = had["E"].astype(float) ** 2 - (had["px"].astype(float) ** 2 + had["py"] ** 2 + had["pz"] ** 2)
     assert np.allclose(np.sqrt(np.maximum(m2, 0)), had["mass"], rtol=1e-3, atol=1e-3)
+
+
+def test_reference_algorithm_port_matches_reference_samples():
+    """Oracle part 3 (the reference's sampling algorithm in C) against
+    hadrons sampled by the reference binary: same spectra and multiplicities
+    (two-sample chi-square, Bonferroni at 0.01)."""
+    from scipy import stats
+    g = O.load_golden("samples_static_viscous.npz")
+    fo = S.music_to_fo_surf(g["records"], int(g["hydro_mode"]))
+    lrf, keep = O.lrf_cells(fo)
+    p = dict(S.DEFAULT_PARAMETERS, **g["params"])
+    n_ev = 8000
+    oc = O.OracleConfig(p, S.TABLE_DIR, n_events=n_ev)
+    sp_ = O.chosen_species(S.TABLE_DIR, 0)
+    had, n, sec = O.reference_sampler(oc, sp_, lrf, keep, seed=3, capacity=2_000_000)
+    assert n == len(had) > 0
+    pvals = []
+    for pid in (211, 321, 2212, -2212):
+        h = had[had["pid"] == pid]
+        pT = np.hypot(h["px"].astype(float), h["py"].astype(float))
+        a = np.histogram(pT, g["pt_edges"])[0].astype(float)
+        b = g[f"pt_{pid}"].astype(float)
+        m = (a + b) >= 10
+        k1, k2 = np.sqrt(b[m].sum() / a[m].sum()), np.sqrt(a[m].sum() / b[m].sum())
+        chi2 = np.sum((k1 * a[m] - k2 * b[m]) ** 2 / (a[m] + b[m]))
+        pvals.append(stats.chi2.sf(chi2, m.sum() - 1))
+        ma, mb = len(h) / n_ev, g[f"n_{pid}"].mean()
+        z = (ma - mb) / np.sqrt(ma / n_ev + mb / int(g["n_events"]))
+        pvals.append(2 * stats.norm.sf(abs(z)))
+    assert min(pvals) > 0.01 / len(pvals), pvals
