@@ -247,6 +247,7 @@ def run_gpu(args, ws, rank, local):
     barrier()
     torch.cuda.synchronize()
     dev_ms, hadrons, t_sample, t_yields = [], [], [], []
+    phases = {k: 0.0 for k in ("ms_prologue", "ms_yields", "ms_cdf", "ms_counts", "ms_sample")}
     wall0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
@@ -257,6 +258,8 @@ def run_gpu(args, ws, rank, local):
         hadrons.append(t["n_hadrons"])
         t_sample.append(t["ms_sample"])
         t_yields.append(t["ms_yields"])
+        for k in phases:
+            phases[k] += t[k] / args.steps
     torch.cuda.synchronize()
     barrier()
     wall = time.perf_counter() - wall0
@@ -345,6 +348,7 @@ def run_gpu(args, ws, rank, local):
                         if e2e else None),
                 "gpu_launches": launches, "clocks": clk,
                 "hadrons_per_step": nh / args.steps,
+                "phase_ms_per_step": phases,
                 "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
         print(json.dumps(line), flush=True)
     if ws > 1:
