@@ -16,12 +16,16 @@
 // The |p| proposal is an exact Gamma mixture: with K = (E - m)/T and
 // m~ = m/T the density (E^2 - m^2/2) exp(-(E - mu)/T) is proportional to
 // (K^2 + 2 m~ K + m~^2/2) exp(-K), a mixture of Gamma(3), Gamma(2) and
-// Gamma(1) with weights 2, 2 m~ and m~^2/2.  The quantum-statistics factor
-// f/exp(-(E-mu)/T), the pE/(E^2 - m^2/2) factor of
-// src/MomentumSamplerBase.cpp:45-56 and the Cooper-Frye/delta-f acceptance of
-// src/FSSW.cpp:1939-1945 are applied as one acceptance probability, so every
-// try costs one proposal and the accepted density is the reference's
-// p^2 f(E) x accept.  The support is cut at the end of the reference's
+// Gamma(1) with weights 2, 2 m~ and m~^2/2.  The direction is proposed from
+// the Cooper-Frye flux factor clamp01(p.dsigma / (p0 dsigma_fac)) of
+// src/FSSW.cpp:1939-1941 itself: with dsigma_mu = (d0, D n) in the rest frame
+// the factor is linear in cos(angle to n), so cos is drawn from that linear
+// density (cut at its zero for spacelike cells) by inverse CDF, and the part of
+// the flux weight that depends on |p| is left to the acceptance.  The
+// quantum-statistics factor f/exp(-(E-mu)/T), the pE/(E^2 - m^2/2) factor of
+// src/MomentumSamplerBase.cpp:45-56, that flux remainder and the delta-f factor
+// clamp01((1 + delta f)/2) of src/FSSW.cpp:1942 are applied as one acceptance
+// probability, so the accepted density is the reference's p^2 f(E) x accept.  The support is cut at the end of the reference's
 // momentum table for the selected sampler (src/MomentumSamplerShell.cpp:24-48).
 #include <cuda_runtime.h>
 
@@ -253,8 +257,8 @@ struct Prop {
     float T, m, a, mt, Kmax, W, w32, w3, qa;
     float mut, cpoly, rmax;
     int boson, compat, sign;
-    float4 da;
-    float inv_dsfac;
+    // flux geometry in the LRF: dsigma_mu = (d0, D n), e1 _|_ n
+    float d0, D, nx, ny, nz, e1x, e1y, e1z;
     float pxx, pxy, pxz, pyy, pyz, shear_c;
     int shear_over_p0T;
     float bi0, b0, b1, b2;
@@ -305,7 +309,7 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
     const float4 pi1 = cells.pi1[l];
     const float4 pi2 = cells.pi2[l];
     const float4 cf = cells.coef[l];
-    p.da = cells.da[l];
+    const float4 da = cells.da[l];
     const float T = th.x;
     const float beta = 1.0f / T;
     const float m = sp.m_hi + sp.m_lo;
@@ -352,8 +356,35 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
             const float x2 = (p.a >= 0.1f) ? aa * expf(-10.0f * aa) : 0.5f * kTwoOverE10;
             p.rmax = 1.0f + C * 2.0f / expm1f(fmaxf(p.a, 1e-12f)) + 8.0f * amu * x2 / (p.mt * p.mt);
         }
+        // the bound is attained (fermions at threshold, bosons as E -> inf):
+        // a relative margin keeps rounding from crossing it
+        p.rmax *= 1.0f + 1e-5f;
     }
-    p.inv_dsfac = 1.0f / (fabsf(p.da.x) + sqrtf(p.da.y * p.da.y + p.da.z * p.da.z + p.da.w * p.da.w));
+    // Cooper-Frye flux geometry: p.dsigma = p0 d0 + |p| D cos(alpha), alpha
+    // measured from n; directions are proposed from this flux exactly
+    p.d0 = fabsf(da.x);
+    p.D = sqrtf(da.y * da.y + da.z * da.z + da.w * da.w);
+    if (p.D > 1e-30f) {
+        const float inv = 1.0f / p.D;
+        p.nx = da.y * inv;
+        p.ny = da.z * inv;
+        p.nz = da.w * inv;
+    } else {
+        p.D = 0.0f;
+        p.nx = 0.0f;
+        p.ny = 0.0f;
+        p.nz = 1.0f;
+    }
+    // e1 = normalised (t x n) with t the coordinate axis least parallel to n
+    {
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        if (fabsf(p.nz) < 0.9f) tz = 1.f; else tx = 1.f;
+        float ex = ty * p.nz - tz * p.ny, ey = tz * p.nx - tx * p.nz, ez = tx * p.ny - ty * p.nx;
+        const float inv = rsqrtf(ex * ex + ey * ey + ez * ez);
+        p.e1x = ex * inv;
+        p.e1y = ey * inv;
+        p.e1z = ez * inv;
+    }
     p.pxx = pi1.x;
     p.pxy = pi1.y;
     p.pxz = pi1.z;
@@ -439,17 +470,35 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
             a_c = 1.0f;
         }
     }
-    const float cth = 2.0f * u01f(B.x) - 1.0f;
+    // direction: cos(alpha) from the density max(0, d0 + beta D cos(alpha))
+    // (inverse CDF, stable root), azimuth uniform around n
+    const float beta = ptil / Et;
+    const float bD = beta * p.D;
+    float c_lo = -1.0f, r_flux = 1.0f;
+    if (bD > p.d0) {
+        c_lo = -p.d0 / bD;
+        const float s0 = p.d0 + p.D;
+        r_flux = (p.d0 + bD) * (p.d0 + bD) / (beta * s0 * s0);
+    } else if (p.D > p.d0) {
+        const float s0 = p.d0 + p.D;
+        r_flux = 4.0f * p.d0 * p.D / (s0 * s0);
+    }
+    const float a_lin = p.d0 + bD * c_lo;
+    const float L = 1.0f - c_lo;
+    const float uZ = u01f(B.x) * (a_lin * L + 0.5f * bD * L * L);
+    const float cth = fminf(c_lo + 2.0f * uZ / (a_lin + sqrtf(a_lin * a_lin + 2.0f * bD * uZ)), 1.0f);
     const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
     float sphi, cphi;
     sincospif(2.0f * u01f(B.y), &sphi, &cphi);
+    const float e2x = p.ny * p.e1z - p.nz * p.e1y;
+    const float e2y = p.nz * p.e1x - p.nx * p.e1z;
+    const float e2z = p.nx * p.e1y - p.ny * p.e1x;
     const float T = p.T;
     const float pm = T * ptil;
     const float p0 = T * Et;
-    const float px = pm * sth * cphi;
-    const float py = pm * sth * sphi;
-    const float pz = pm * cth;
-    const float pdsigma = p0 * p.da.x + px * p.da.y + py * p.da.z + pz * p.da.w;
+    const float px = pm * (cth * p.nx + sth * (cphi * p.e1x + sphi * e2x));
+    const float py = pm * (cth * p.ny + sth * (cphi * p.e1y + sphi * e2y));
+    const float pz = pm * (cth * p.nz + sth * (cphi * p.e1z + sphi * e2z));
     const float sgn = static_cast<float>(p.sign);
     const float f0 = em / (1.0f + sgn * em);
     const float one_m = 1.0f - sgn * f0;
@@ -468,9 +517,8 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
         const float qf = -(px * p.qx + py * p.qy + pz * p.qz);
         df += one_m * (p.pq - p.Bq / p0) * qf;
     }
-    const float fact1 = clamp01(pdsigma / p0 * p.inv_dsfac);
     const float fact2 = clamp01((1.0f + df) * 0.5f);
-    const float acc = a_pE * a_q * a_c * fact1 * fact2;
+    const float acc = a_pE * a_q * a_c * r_flux * fact2;
     if (!(u01f(B.z) < acc)) return false;
     pl = make_float4(p0, px, py, pz);
     u_rap = u01f(B.w);

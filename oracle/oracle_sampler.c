@@ -10,9 +10,11 @@
  *   FSSW::add_one_sampled_particle,       src/FSSW.cpp:1969-1996
  *
  * The GPU proposes |p| from an exact Gamma mixture matching (E^2 - m^2/2)
- * exp(-(E - mu)/T) and folds the quantum-statistics, pE/(E^2 - m^2/2) and
- * Cooper-Frye/delta-f acceptances into one uniform per try; the resulting
- * density is the reference's p^2 f(E) x accept.  This file restates that
+ * exp(-(E - mu)/T), the direction from the Cooper-Frye flux factor itself
+ * (linear in the cosine of the angle to the spatial part of dsigma in the rest
+ * frame, inverse CDF), and folds the quantum-statistics, pE/(E^2 - m^2/2),
+ * |p|-dependent flux remainder and delta-f acceptances into one uniform per
+ * try; the resulting density is the reference's p^2 f(E) x accept.  This file restates that
  * algorithm draw for draw so that the GPU output can be compared hadron by
  * hadron. */
 #include <math.h>
@@ -118,6 +120,9 @@ static void orc_setup(const orc_cfg* cfg, double m, int sign, double mu_raw, dou
             p->rmax = 1.0 + C * 2.0 / expm1(p->a > 1e-12 ? p->a : 1e-12)
                       + 8.0 * amu * x2 / (p->mt * p->mt);
         }
+        /* the bound is attained (fermions at threshold, bosons as E -> inf):
+         * a relative margin keeps rounding from crossing it */
+        p->rmax *= 1.0 + 1e-5;
     }
 }
 
@@ -176,17 +181,50 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
             a_c = 1.0;
         }
     }
-    const double cth = 2.0 * orc_u01(Bw[0]) - 1.0;
+    /* direction from the flux density max(0, d0 + beta D cos(alpha)) */
+    const double d0 = fabs(c->da[0]);
+    double D = sqrt(c->da[1] * c->da[1] + c->da[2] * c->da[2] + c->da[3] * c->da[3]);
+    double n[3] = {0.0, 0.0, 1.0};
+    if (D > 1e-30) {
+        n[0] = c->da[1] / D; n[1] = c->da[2] / D; n[2] = c->da[3] / D;
+    } else {
+        D = 0.0;
+    }
+    double e1[3];
+    {
+        double t[3] = {0.0, 0.0, 0.0};
+        if (fabs(n[2]) < 0.9) t[2] = 1.0; else t[0] = 1.0;
+        double ex = t[1] * n[2] - t[2] * n[1], ey = t[2] * n[0] - t[0] * n[2];
+        double ez = t[0] * n[1] - t[1] * n[0];
+        const double nn = sqrt(ex * ex + ey * ey + ez * ez);
+        e1[0] = ex / nn; e1[1] = ey / nn; e1[2] = ez / nn;
+    }
+    const double e2[3] = {n[1] * e1[2] - n[2] * e1[1], n[2] * e1[0] - n[0] * e1[2],
+                          n[0] * e1[1] - n[1] * e1[0]};
+    const double beta = ptil / Et;
+    const double bD = beta * D;
+    double c_lo = -1.0, r_flux = 1.0;
+    if (bD > d0) {
+        c_lo = -d0 / bD;
+        r_flux = (d0 + bD) * (d0 + bD) / (beta * (d0 + D) * (d0 + D));
+    } else if (D > d0) {
+        r_flux = 4.0 * d0 * D / ((d0 + D) * (d0 + D));
+    }
+    const double a_lin = d0 + bD * c_lo;
+    const double L = 1.0 - c_lo;
+    const double uZ = orc_u01(Bw[0]) * (a_lin * L + 0.5 * bD * L * L);
+    double cth = c_lo + 2.0 * uZ / (a_lin + sqrt(a_lin * a_lin + 2.0 * bD * uZ));
+    if (cth > 1.0) cth = 1.0;
     double sth2 = 1.0 - cth * cth;
     const double sth = sth2 > 0 ? sqrt(sth2) : 0.0;
     const double phi = 2.0 * ORC_PI * orc_u01(Bw[1]);
+    const double cph = cos(phi), sph = sin(phi);
     const double T = c->T;
     const double pm = T * ptil;
     const double p0 = T * Et;
-    const double px = pm * sth * cos(phi);
-    const double py = pm * sth * sin(phi);
-    const double pz = pm * cth;
-    const double pdsigma = p0 * c->da[0] + px * c->da[1] + py * c->da[2] + pz * c->da[3];
+    const double px = pm * (cth * n[0] + sth * (cph * e1[0] + sph * e2[0]));
+    const double py = pm * (cth * n[1] + sth * (cph * e1[1] + sph * e2[1]));
+    const double pz = pm * (cth * n[2] + sth * (cph * e1[2] + sph * e2[2]));
     const double f0 = em / (1.0 + sign * em);
     const double one_m = 1.0 - sign * f0;
     double df_s = 0.0, df_b = 0.0, df_q = 0.0;
@@ -217,13 +255,9 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
         const double qf = (-px * c->qx - py * c->qy - pz * c->qz);
         df_q = one_m * (c->nB / (c->E + c->P) - B / p0) * qf / c->kappa;
     }
-    double fact1 = pdsigma / p0 / (fabs(c->da[0])
-                                   + sqrt(c->da[1] * c->da[1] + c->da[2] * c->da[2]
-                                          + c->da[3] * c->da[3]));
     double fact2 = (1. + df_s + df_b + df_q) / 2.;
-    fact1 = fact1 < 0 ? 0 : (fact1 > 1 ? 1 : fact1);
     fact2 = fact2 < 0 ? 0 : (fact2 > 1 ? 1 : fact2);
-    const double acc = a_pE * a_q * a_c * fact1 * fact2;
+    const double acc = a_pE * a_q * a_c * r_flux * fact2;
     if (!(orc_u01(Bw[2]) < acc)) return 0;
     pl[0] = p0; pl[1] = px; pl[2] = py; pl[3] = pz;
     *u_rap = orc_u01(Bw[3]);

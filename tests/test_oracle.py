@@ -151,3 +151,41 @@ def test_reference_algorithm_port_matches_reference_samples():
         z = (ma - mb) / np.sqrt(ma / n_ev + mb / int(g["n_events"]))
         pvals.append(2 * stats.norm.sf(abs(z)))
     assert min(pvals) > 0.01 / len(pvals), pvals
+
+
+@pytest.mark.parametrize("name,n_ev", [("static_viscous", 8000), ("viscous_14moment", 20000)])
+def test_gpu_algorithm_replay_matches_reference_samples(name, n_ev):
+    """The GPU algorithm (flux-exact directions, Gamma-mixture |p|, one
+    combined acceptance), replayed in FP64 on the CPU, against hadrons sampled
+    by the reference binary: pT, rapidity and multiplicities per species
+    (two-sample chi-square, Bonferroni at 0.01)."""
+    from scipy import stats
+    g = O.load_golden(f"samples_{name}.npz")
+    fo = S.music_to_fo_surf(g["records"], int(g["hydro_mode"]))
+    lrf, keep = O.lrf_cells(fo)
+    p = dict(S.DEFAULT_PARAMETERS, **g["params"])
+    oc = O.OracleConfig(p, S.TABLE_DIR, n_events=n_ev, seed=8, compat_fermion=1)
+    sp_ = O.chosen_species(S.TABLE_DIR, 0)
+    y = O.yields(oc, sp_, lrf, keep).astype(np.float32)
+    cdf, tot = O.cdf(y)
+    cnt = O.counts(oc, sp_, tot)
+    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
+    had, st = O.sample_replay(oc, sp_, lrf, coef, cdf, tot, cnt)
+    assert st.n_failures == 0 and st.n_bound_violations == 0
+    pvals = []
+    for pid in (211, 321, 2212, -2212):
+        h = had[had["pid"] == pid]
+        E, pz = h["E"].astype(float), h["pz"].astype(float)
+        obs = {"pt": np.hypot(h["px"].astype(float), h["py"].astype(float)),
+               "y": 0.5 * np.log((E + pz) / (E - pz))}
+        for key, edges in (("pt", g["pt_edges"]), ("y", g["y_edges"])):
+            a = np.histogram(obs[key], edges)[0].astype(float)
+            b = g[f"{key}_{pid}"].astype(float)
+            m = (a + b) >= 10
+            k1, k2 = np.sqrt(b[m].sum() / a[m].sum()), np.sqrt(a[m].sum() / b[m].sum())
+            chi2 = np.sum((k1 * a[m] - k2 * b[m]) ** 2 / (a[m] + b[m]))
+            pvals.append(stats.chi2.sf(chi2, m.sum() - 1))
+        ma, mb = len(h) / n_ev, g[f"n_{pid}"].mean()
+        z = (ma - mb) / np.sqrt(ma / n_ev + mb / int(g["n_events"]))
+        pvals.append(2 * stats.norm.sf(abs(z)))
+    assert min(pvals) > 0.01 / len(pvals), pvals
