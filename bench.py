@@ -136,8 +136,11 @@ def dist_setup():
 # CPU (oracle) leg
 
 def cpu_worker(args):
-    """One process: yields on the cell sample, counts and sampling of its
-    share of the events; returns (hadrons, seconds)."""
+    """One process: the reference's sampling algorithm (oracle part 3:
+    per-species yields, Poisson counts, cell draws from the cumulative
+    yields, momentum rejection and boost, with MT19937 as in the reference)
+    on the cell sample for its share of the events; returns (hadrons,
+    seconds)."""
     n_sample, n_events, event_offset, seed = args
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib as O
@@ -149,14 +152,9 @@ def cpu_worker(args):
     t0 = time.perf_counter()
     lrf, keep = O.lrf_cells(fo)
     sp = O.chosen_species(S.TABLE_DIR, 0)
-    oc = O.OracleConfig(params, S.TABLE_DIR, n_events=n_events, seed=seed,
-                        event_offset=event_offset)
-    y = O.yields(oc, sp, lrf, keep).astype(np.float32)
-    cdf, tot = O.cdf(y)
-    cnt = O.counts(oc, sp, tot)
-    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
-    had, _ = O.sample_replay(oc, sp, lrf, coef, cdf, tot, cnt)
-    return len(had), time.perf_counter() - t0
+    oc = O.OracleConfig(params, S.TABLE_DIR, n_events=n_events, seed=seed)
+    _, n, _ = O.reference_sampler(oc, sp, lrf, keep, seed=seed + event_offset)
+    return int(n), time.perf_counter() - t0
 
 
 def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int):
@@ -164,15 +162,15 @@ def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int):
     per = [n_events // n_procs + (1 if k < n_events % n_procs else 0) for k in range(n_procs)]
     offs = np.concatenate([[0], np.cumsum(per)[:-1]])
     jobs = [(n_sample, per[k], int(offs[k]), seed) for k in range(n_procs) if per[k] > 0]
-    t0 = time.perf_counter()
     if len(jobs) == 1:
         res = [cpu_worker(jobs[0])]
     else:
         with mp.get_context("spawn").Pool(len(jobs)) as pool:
             res = pool.map(cpu_worker, jobs)
-    wall = time.perf_counter() - t0
+    # the processes run side by side: the step takes as long as the slowest
+    # (process start-up and building the synthetic surface are not timed)
     hadrons = sum(r[0] for r in res)
-    return hadrons, wall
+    return hadrons, max(r[1] for r in res)
 
 
 def run_reference(args, ws, rank):

@@ -5,7 +5,7 @@
 algorithm (oracle part 3, the CPU baseline of bench.py) on the same cells,
 species, parameters and number of events, single-threaded on this host.
 
-    python oracle/calibrate_cpu_baseline.py [--cells-every 10] [--events 100]
+    python oracle/calibrate_cpu_baseline.py [--cells-every 10] [--events 100] [--bulk-kind 1]
 
 Needs the reference tree (ISS_REFERENCE, default /root/reference) for its
 iSS_tables; prints one JSON line."""
@@ -31,6 +31,9 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--cells-every", type=int, default=10)
     ap.add_argument("--events", type=int, default=100)
+    ap.add_argument("--bulk-kind", type=int, default=1,
+                    help="bulk delta-f kind; the default 1 avoids kind 11, whose c0 "
+                         "table the reference leaves unread (uninitialised memory)")
     args = ap.parse_args()
     import oracle_lib as O
     from iss_gb300 import surfaces as S
@@ -41,7 +44,7 @@ def main():
     surf = S.viscous_3d(200_000, seed=2)
     surf.records = surf.records[::args.cells_every].copy()
     params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
-                  include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1,
+                  include_deltaf_bulk=1, bulk_deltaf_kind=args.bulk_kind, turn_on_bulk=1,
                   number_of_repeated_sampling=args.events, randomSeed=5)
     root = tempfile.mkdtemp(prefix="iss_calib_")
     try:
@@ -65,7 +68,7 @@ def main():
     t0 = time.perf_counter()
     _, n_port, t_port_inner = O.reference_sampler(oc, sp, lrf, keep, seed=5)
     t_port = time.perf_counter() - t0
-    out = {"cells": int(fo.shape[0]), "events": args.events,
+    out = {"cells": int(fo.shape[0]), "events": args.events, "bulk_deltaf_kind": args.bulk_kind,
            "reference_binary": {"hadrons": n_ref, "wall_s": t_ref,
                                 "sampling_phase_cpu_s": t_ref_sampling,
                                 "hadrons_per_s_wall": n_ref / t_ref},
