@@ -207,6 +207,31 @@ const char* iss_gpu_last_error(const iss_handle* h);
 /* Static name of a status code. */
 const char* iss_gpu_status_string(int status);
 
+/* ---- count-to-slot scan without allocation ----------------------------- */
+
+/* No counterpart in the reference.  Callers that cannot allocate device
+ * memory use it: a program whose memory pool already holds the device, or a
+ * pipeline where cudaFree's device-wide wait would stall other streams.
+ *
+ * Exclusive prefix sum of n hadron counts (device pointer d_counts) into
+ * d_offsets[0 .. n] (device pointer; d_offsets[n] = total).  It is the scan
+ * iss_gpu_generate uses to turn per-(event, species) counts into output
+ * slots.  Its tile partial sums live in one fixed device array of 128 KiB
+ * instead of a handle buffer, so it allocates nothing.
+ *   - n > ISS_GPU_NOALLOC_SCAN_MAX_SEGMENTS returns ISS_ERR_CAPACITY before
+ *     any device work.
+ *   - The work is enqueued on `stream` (a cudaStream_t; NULL is the legacy
+ *     default stream).  The results are ready when that stream reaches this
+ *     point.
+ *   - Nothing has to be zeroed before the call.
+ *   - The fixed array is shared by all calls on one device.  Calls on one
+ *     device must not overlap in time; issue them on one stream.
+ *   - The first call on each device looks up the array's address.  Make that
+ *     call before starting any stream capture on that device. */
+#define ISS_GPU_NOALLOC_SCAN_MAX_SEGMENTS ((int64_t)16384 * 4096)
+iss_status iss_gpu_scan_counts_noalloc(const int32_t* d_counts, int64_t n,
+                                       int64_t* d_offsets, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

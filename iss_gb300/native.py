@@ -34,7 +34,7 @@ EXPORTED = [
     "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output", "iss_gpu_species",
     "iss_gpu_species_yields", "iss_gpu_num_cells", "iss_gpu_copy_lrf_cells",
     "iss_gpu_copy_cell_yields", "iss_gpu_copy_counts", "iss_gpu_get_timings",
-    "iss_gpu_last_error", "iss_gpu_status_string",
+    "iss_gpu_last_error", "iss_gpu_status_string", "iss_gpu_scan_counts_noalloc",
 ]
 
 
@@ -97,6 +97,7 @@ def lib():
         L.iss_gpu_last_error.restype = C.c_char_p
         L.iss_gpu_status_string.argtypes = [C.c_int]
         L.iss_gpu_status_string.restype = C.c_char_p
+        L.iss_gpu_scan_counts_noalloc.argtypes = [v, C.c_int64, v, v]
         for name in EXPORTED:
             if name not in ("iss_gpu_last_error", "iss_gpu_status_string"):
                 getattr(L, name).restype = C.c_int
