@@ -15,7 +15,9 @@ written between steps.
 
 `value` is device time (CUDA events on the library's stream); `e2e` is the
 same metric through the C ABI with the surface copied from pinned host
-memory and all hadrons read back to pinned host memory every step.
+memory and all hadrons read back to pinned host memory every step
+(iss_gpu_set_surface + iss_gpu_generate_into, whose device->host copies of
+finished events overlap the sampling of later ones).
 
 --impl reference times the CPU implementation of the path (the oracle port
 of the reference's algorithm, oracle/) on the host cores with one process per
@@ -273,20 +275,26 @@ def run_gpu(args, ws, rank, local):
         from iss_gb300 import HADRON_DTYPE
         out = out.view(HADRON_DTYPE)
         e_had, e_bytes_in, e_bytes_out = 0, 0, 0
+        parts = [0.0, 0.0]   # set_surface, generate_into (host clock)
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ta = time.perf_counter()
             s.set_surface(fo_pinned)
-            s.generate_samples()
-            h, off = s.all_hadrons(out=out)
+            tb = time.perf_counter()
+            h, off = s.generate_into(out)
+            tc = time.perf_counter()
+            parts[0] += tb - ta
+            parts[1] += tc - tb
             e_had += len(h)
             e_bytes_in += fo_pinned.nbytes
             e_bytes_out += len(h) * 40 + off.nbytes
         torch.cuda.synchronize()
         barrier()
         e_sec = time.perf_counter() - t0
-        e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps]
+        e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps,
+               [1e3 * x / args.steps for x in parts]]
 
     sec = sum(dev_ms) / 1e3
     local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
@@ -342,7 +350,9 @@ def run_gpu(args, ws, rank, local):
                            "wall_s_timed": wall},
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": ({"value": e2e_h / e2e_sec, "unit": UNIT,
-                         "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3]}
+                         "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3],
+                         "host_ms_per_step": {"set_surface": e2e[4][0],
+                                              "generate_into": e2e[4][1]}}
                         if e2e else None),
                 "gpu_launches": launches, "clocks": clk,
                 "hadrons_per_step": nh / args.steps,

@@ -64,7 +64,7 @@ typedef enum iss_output_format {
 typedef struct iss_timings {
     double ms_prologue;   /* local-rest-frame transform + per-cell delta-f coefficients */
     double ms_yields;     /* per (cell, species) yields                               */
-    double ms_cdf;        /* per-species FP64 prefix sums (cell CDF) and totals       */
+    double ms_cdf;        /* per-species fixed-point prefix sums (cell CDF), totals   */
     double ms_counts;     /* per (event, species) counts + slot scan                  */
     double ms_sample;     /* momentum sampling, boost, emission                       */
     double ms_total;      /* first event to last event of iss_gpu_generate            */
@@ -130,6 +130,21 @@ iss_status iss_gpu_set_surface(iss_handle* h, const float* fo_surf_records,
  * FSSW::shell (src/FSSW.cpp:344-361) without the optional decays and
  * spectators: yields, counts, momenta and the hadron lists, all on the GPU. */
 iss_status iss_gpu_generate(iss_handle* h);
+
+/* iSS::generate_samples followed by reading every event's hadron list
+ * (get_hadron_list_iev for iev = 0 .. n_events-1, src/iSS.h:85-91) in one call.
+ *   - The sampler runs in up to 8 chunks of consecutive events.
+ *   - Each chunk's records are copied into out[0 .. n_total) while the next
+ *     chunk is sampled.
+ *   - `out` should be page-locked (cudaHostAlloc or cudaHostRegister). Then
+ *     the copies run beside the sampling.
+ *   - The hadrons and their order are those of iss_gpu_generate followed by
+ *     iss_gpu_copy_all.
+ *   - If capacity is too small, the samples stay on the device. The call
+ *     returns ISS_ERR_CAPACITY and sets *n_total to the size needed.
+ *   - Event offsets come from iss_gpu_copy_all(h, NULL, 0, offsets, NULL). */
+iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capacity,
+                                 int64_t* n_total);
 
 /* iSS::shell (src/iSS.cpp:41-56): read_surface + set_seed_from_params +
  * generate. */

@@ -91,14 +91,18 @@ struct iss_handle {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;     // device->host copies of iss_gpu_generate_into
+    std::vector<cudaEvent_t> chunk_ev;      // end of each sampling chunk
     cudaEvent_t ev[kEvCount] = {};
     DevBuf<float> d_fo34;
     DevBuf<float4> d_cells;          // 8 arrays of n_cells float4
     DevBuf<SpeciesDev> d_species;
     DevBuf<int32_t> d_pids;
     DevBuf<float> d_yields;
-    DevBuf<double> d_cdf, d_tile_sum, d_tile_off, d_totals;
-    DevBuf<int32_t> d_counts, d_items, d_item_seg, d_guide;
+    DevBuf<unsigned long long> d_cdf, d_tile_sum, d_tile_off, d_qtot;
+    DevBuf<double> d_totals;
+    DevBuf<uint32_t> d_ymax;
+    DevBuf<int32_t> d_counts, d_items, d_item_seg, d_guide, d_cell_of;
     DevBuf<int64_t> d_offsets, d_off_tiles, d_item_off;
     DevBuf<HadronRec> d_hadrons;
     DevBuf<unsigned long long> d_work;
@@ -130,13 +134,16 @@ struct iss_handle {
             d_cells.release();
             d_species.release();
             d_pids.release();
-            DevBuf<double>* db[] = {&d_cdf, &d_tile_sum, &d_tile_off, &d_totals, &d_b14c0,
-                                    &d_b14c1, &d_b14c2, &d_ce, &d_qmu};
+            DevBuf<double>* db[] = {&d_totals, &d_b14c0, &d_b14c1, &d_b14c2, &d_ce, &d_qmu};
             for (auto* b : db) b->release();
+            DevBuf<unsigned long long>* ub[] = {&d_cdf, &d_tile_sum, &d_tile_off, &d_qtot};
+            for (auto* b : ub) b->release();
+            d_ymax.release();
             d_counts.release();
             d_items.release();
             d_item_seg.release();
             d_guide.release();
+            d_cell_of.release();
             d_offsets.release();
             d_off_tiles.release();
             d_item_off.release();
@@ -147,6 +154,9 @@ struct iss_handle {
             d_sfK.release();
             for (auto& e : ev)
                 if (e) cudaEventDestroy(e);
+            for (auto& e : chunk_ev)
+                if (e) cudaEventDestroy(e);
+            if (copy_stream) cudaStreamDestroy(copy_stream);
             if (stream) cudaStreamDestroy(stream);
         }
     }
@@ -395,15 +405,18 @@ iss_status run_cells(iss_handle* h) {
     CUDA_TRY(h, h->d_tile_sum.reserve(static_cast<size_t>(nt) * S));
     CUDA_TRY(h, h->d_tile_off.reserve(static_cast<size_t>(nt) * S));
     CUDA_TRY(h, h->d_totals.reserve(static_cast<size_t>(S)));
-    CUDA_TRY(h, h->d_guide.reserve(static_cast<size_t>(cdf_guide_len(n) + 1) * S));
+    CUDA_TRY(h, h->d_qtot.reserve(static_cast<size_t>(S)));
+    CUDA_TRY(h, h->d_ymax.reserve(static_cast<size_t>(S)));
+    CUDA_TRY(h, h->d_guide.reserve(((size_t(1) << cdf_guide_bits(n)) + 1) * S));
     const CellArrays cells = cell_arrays(h);
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
     CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvPrologue], st));
-    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
+    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, h->d_ymax.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
-    CUDA_TRY(h, launch_cdf(h->d_yields.ptr, S, n, h->d_tile_sum.ptr, h->d_tile_off.ptr,
-                           h->d_totals.ptr, h->d_cdf.ptr, h->d_guide.ptr, st));
+    CUDA_TRY(h, launch_cdf(h->d_yields.ptr, h->d_ymax.ptr, S, n, h->d_tile_sum.ptr,
+                           h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
+                           h->d_guide.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCdf], st));
     h->yields_valid = true;
     return ISS_OK;
@@ -415,7 +428,14 @@ float elapsed(iss_handle* h, int a, int b) {
     return ms;
 }
 
-iss_status run_generate(iss_handle* h) {
+// host_out != nullptr: iss_gpu_generate_into -- the sampler runs in chunks of
+// consecutive events and each chunk's records are copied to host_out on a
+// second stream while the next chunk is sampled.
+constexpr int kMaxChunks = 8;
+
+iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
+                        bool* copied = nullptr) {
+    if (copied) *copied = false;
     if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface: call iss_gpu_read_surface first");
     iss_status st = ensure_cuda(h);
     if (st != ISS_OK) return st;
@@ -455,8 +475,13 @@ iss_status run_generate(iss_handle* h) {
     CUDA_TRY(h, h->d_offsets.reserve(static_cast<size_t>(nseg + 1)));
     CUDA_TRY(h, h->d_item_off.reserve(static_cast<size_t>(nseg + 1)));
     CUDA_TRY(h, h->d_off_tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(nseg), 1))));
+    // sampling chunks: one without a host destination, else up to kMaxChunks
+    const int E = c.n_events;
+    int n_chunks = host_out ? std::min(kMaxChunks, std::max(E, 1)) : 1;
+    c.chunk_events = std::max(1, (E + n_chunks - 1) / n_chunks);
+    n_chunks = std::max(1, (E + c.chunk_events - 1) / c.chunk_events);
     CUDA_TRY(h, h->d_error.reserve(1));
-    CUDA_TRY(h, h->d_work.reserve(1));
+    CUDA_TRY(h, h->d_work.reserve(static_cast<size_t>(n_chunks)));
     CUDA_TRY(h, h->d_counters.reserve(1));
     CUDA_TRY(h, cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
     CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_counts.ptr, h->d_items.ptr, h->d_error.ptr, s));
@@ -464,38 +489,75 @@ iss_status run_generate(iss_handle* h) {
     CUDA_TRY(h, launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
     int64_t sizes[2] = {0, 0};   // hadrons, work items
     int count_err = 0;
+    std::vector<int64_t> chunk_item(static_cast<size_t>(n_chunks) + 1, 0);
+    h->event_offsets.assign(static_cast<size_t>(E) + 1, 0);
     CUDA_TRY(h, cudaMemcpyAsync(&sizes[0], h->d_offsets.ptr + nseg, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(&sizes[1], h->d_item_off.ptr + nseg, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(&count_err, h->d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (S > 0) {
+        // event offsets: offsets[e * S] for e = 0..n_events
+        CUDA_TRY(h, cudaMemcpy2DAsync(h->event_offsets.data(), sizeof(int64_t), h->d_offsets.ptr,
+                                      sizeof(int64_t) * static_cast<size_t>(S), sizeof(int64_t),
+                                      static_cast<size_t>(E) + 1, cudaMemcpyDeviceToHost, s));
+        // first work item of each chunk: item_off at segment c * chunk_events * S
+        CUDA_TRY(h, cudaMemcpy2DAsync(chunk_item.data(), sizeof(int64_t), h->d_item_off.ptr,
+                                      sizeof(int64_t) * static_cast<size_t>(c.chunk_events) * S,
+                                      sizeof(int64_t), static_cast<size_t>(n_chunks),
+                                      cudaMemcpyDeviceToHost, s));
+    }
     CUDA_TRY(h, cudaStreamSynchronize(s));
     const int64_t n_units = sizes[0], n_items = sizes[1];
+    chunk_item[n_chunks] = n_items;
     if (count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
     if (count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
     CUDA_TRY(h, h->d_item_seg.reserve(static_cast<size_t>(std::max<int64_t>(n_items, 1))));
     CUDA_TRY(h, launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
 
+    const bool to_host = host_out != nullptr && n_units <= capacity && n_units > 0;
+    if (to_host) {
+        if (!h->copy_stream)
+            CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        while (static_cast<int>(h->chunk_ev.size()) < n_chunks) {
+            cudaEvent_t e;
+            CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            h->chunk_ev.push_back(e);
+        }
+    }
     CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
-    CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long), s));
+    CUDA_TRY(h, h->d_cell_of.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long) * n_chunks, s));
     CUDA_TRY(h, cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
-    CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
-                               h->d_guide.ptr, cdf_guide_len(h->n_cells), h->d_totals.ptr,
-                               h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr, n_items,
-                               h->d_hadrons.ptr, h->d_work.ptr, h->d_counters.ptr, h->num_sms, s));
-    CUDA_TRY(h, cudaEventRecord(h->ev[kEvSample], s));
-    // event offsets: offsets[e * S] for e = 0..n_events
-    h->event_offsets.assign(static_cast<size_t>(c.n_events) + 1, 0);
-    if (S > 0) {
-        CUDA_TRY(h, cudaMemcpy2DAsync(h->event_offsets.data(), sizeof(int64_t), h->d_offsets.ptr,
-                                      sizeof(int64_t) * static_cast<size_t>(S), sizeof(int64_t),
-                                      static_cast<size_t>(c.n_events) + 1, cudaMemcpyDeviceToHost, s));
+    for (int ch = 0; ch < n_chunks; ch++) {
+        CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
+                                   h->d_guide.ptr, cdf_guide_bits(h->n_cells), h->d_qtot.ptr,
+                                   h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr,
+                                   chunk_item[ch], chunk_item[ch + 1], h->d_cell_of.ptr,
+                                   h->d_hadrons.ptr, h->d_work.ptr + ch, h->d_counters.ptr,
+                                   h->num_sms, s));
+        if (to_host) {
+            // records of events [e0, e1) are final: copy them while the next chunk runs
+            const int e0 = ch * c.chunk_events, e1 = std::min(E, e0 + c.chunk_events);
+            const int64_t b = h->event_offsets[e0], n = h->event_offsets[e1] - b;
+            CUDA_TRY(h, cudaEventRecord(h->chunk_ev[ch], s));
+            CUDA_TRY(h, cudaStreamWaitEvent(h->copy_stream, h->chunk_ev[ch], 0));
+            if (n > 0)
+                CUDA_TRY(h, cudaMemcpyAsync(host_out + b, h->d_hadrons.ptr + b,
+                                            sizeof(iss_hadron_t) * static_cast<size_t>(n),
+                                            cudaMemcpyDeviceToHost, h->copy_stream));
+        }
     }
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvSample], s));
     SampleCounters ctr{};
     CUDA_TRY(h, cudaMemcpyAsync(&ctr, h->d_counters.ptr, sizeof(ctr), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (to_host) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->copy_stream));
+        if (copied) *copied = true;
+    }
     CUDA_TRY(h, cudaGetLastError());
 
     iss_timings_t& t = h->timings;
@@ -509,7 +571,7 @@ iss_status run_generate(iss_handle* h) {
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures);
-    t.kernel_launches = 14;
+    t.kernel_launches = 13 + 2 * n_chunks;
     h->n_events = c.n_events;
     h->n_hadrons = n_units;
     h->samples_valid = true;
@@ -702,6 +764,26 @@ iss_status iss_gpu_generate(iss_handle* h) {
         if (st != ISS_OK) return st;
     }
     return run_generate(h);
+}
+
+iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capacity,
+                                 int64_t* n_total) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (n_total) *n_total = 0;
+    if (capacity < 0 || (capacity > 0 && !out)) return fail(h, ISS_ERR_INVALID_ARG, "bad output buffer");
+    if (!h->seed_set) {
+        iss_status st = iss_gpu_set_seed_from_params(h);
+        if (st != ISS_OK) return st;
+    }
+    bool copied = false;
+    const iss_status st = run_generate(h, out, capacity, &copied);
+    if (n_total && h->samples_valid) *n_total = h->n_hadrons;
+    if (st != ISS_OK) return st;
+    if (!copied && h->n_hadrons > 0)
+        return fail(h, ISS_ERR_CAPACITY, "%lld hadrons do not fit in %lld records (samples kept "
+                    "on the device)", static_cast<long long>(h->n_hadrons),
+                    static_cast<long long>(capacity));
+    return ISS_OK;
 }
 
 iss_status iss_gpu_shell(iss_handle* h) {

@@ -38,6 +38,7 @@ struct DevConfig {
     int64_t n_cells;
     uint32_t event_offset;
     int max_tries, max_redraws;
+    int chunk_events;        // events per sampling chunk (work-item order, see item_index)
     DevTables tab;
 };
 
@@ -78,6 +79,58 @@ struct HadronRec {
 };
 
 enum : uint32_t { kTagCell = 1u, kTagTry = 2u, kTagCount = 3u };
+
+// ---------------------------------------------------------------------------
+// Fixed-point cell CDF.
+//
+// The reference draws a cell by a binary search in the FP64 running sum of
+// the per-cell yields (RandomVariable1DArray, src/RandomVariable1DArray.cpp:25-74,
+// used at src/FSSW.cpp:1003-1006).  Here every FP32 yield y of species s is
+// truncated to the integer q = floor(y * 2^E_s), with E_s chosen from the
+// species' largest yield and the cell count so that the sum Q_s of all q
+// stays below 2^62.  Integer prefix sums are exact in any order: the tiles of
+// the scan need no particular order, and a CPU replay gets the same bits.
+// A cell is drawn from 64 random bits r: v = floor(r * Q_s / 2^64) is uniform
+// on [0, Q_s), and the cell is the i with C[i] <= v < C[i+1].  Cells whose
+// q is 0 are never drawn, as cells of zero yield are never drawn in the
+// reference.  The per-species total yield is Q_s * 2^-E_s.
+#if defined(__CUDACC__)
+#define ISS_HD __host__ __device__
+#else
+#define ISS_HD
+#endif
+
+// ceil(log2 n), 0 for n <= 1
+ISS_HD inline int cdf_log2_cells(int64_t n) {
+    int L = 0;
+    while (L < 62 && (int64_t(1) << L) < n) ++L;
+    return L;
+}
+
+// 2^g guide buckets per species, g = clamp(ceil(log2 n), 1, 24)
+ISS_HD inline int cdf_guide_bits(int64_t n) {
+    const int L = cdf_log2_cells(n);
+    return L < 1 ? 1 : (L > 24 ? 24 : L);
+}
+
+// q(y) = mantissa(y) * 2^(exponent(y) + base) with base = 38 - L - e_max,
+// e_max the biased exponent of the species' largest yield; E_s = 150 + base.
+// Every q is below 2^(62 - L), so the sum over at most 2^L cells is below 2^62.
+ISS_HD inline int cdf_quant_base(uint32_t ymax_bits, int L) {
+    int ex = static_cast<int>((ymax_bits >> 23) & 0xFFu);
+    if (ex == 0) ex = 1;
+    return 38 - L - ex;
+}
+
+ISS_HD inline uint64_t cdf_quantize(uint32_t y_bits, int base) {
+    int e = static_cast<int>((y_bits >> 23) & 0xFFu);
+    uint32_t m = y_bits & 0x7FFFFFu;
+    if (e) m |= 0x800000u; else e = 1;
+    const int sh = e + base;
+    if (sh >= 0) return static_cast<uint64_t>(m) << sh;
+    if (sh <= -24) return 0;
+    return static_cast<uint64_t>(m >> (-sh));
+}
 
 #if defined(__CUDACC__)
 // ---------------------------------------------------------------------------

@@ -12,13 +12,14 @@ namespace iss {
 cudaError_t launch_cell_prologue(const DevConfig& cfg, const float* fo34, int64_t n,
                                  const CellArrays& cells, cudaStream_t stream);
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, cudaStream_t stream);
+                          float* yields, uint32_t* ymax, cudaStream_t stream);
 int cdf_num_tiles(int64_t n);
-// buckets of the per-species guide table (guide_len + 1 entries per species)
-int cdf_guide_len(int64_t n);
-cudaError_t launch_cdf(const float* yields, int n_species, int64_t n, double* tile_sum,
-                       double* tile_off, double* totals, double* cdf, int32_t* guide,
-                       cudaStream_t stream);
+// fixed-point cell CDF (cdf_quantize): row s holds n + 1 entries C[0..n],
+// the guide table 2^g + 1 entries per species, g = cdf_guide_bits(n)
+cudaError_t launch_cdf(const float* yields, const uint32_t* ymax, int n_species, int64_t n,
+                       unsigned long long* tile_sum, unsigned long long* tile_off,
+                       unsigned long long* qtot, double* totals, unsigned long long* cdf,
+                       int32_t* guide, cudaStream_t stream);
 
 // kernels_sample.cu
 cudaError_t launch_counts(const DevConfig& cfg, const double* totals, int32_t* counts,
@@ -28,11 +29,16 @@ cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_
                                 int64_t* offsets, cudaStream_t stream);
 cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64_t nseg,
                             int32_t* item_seg, cudaStream_t stream);
+// work items [k_begin, k_end) in two launches: the first-draw cell of every
+// hadron (cell_of, one int32 per slot), then the sampler; work_counter must
+// be zero
 cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                           const int32_t* pids, const double* cdf, const int32_t* guide,
-                           int guide_len, const double* totals, const int64_t* offsets,
-                           const int64_t* item_off, const int32_t* item_seg, int64_t n_items,
-                           HadronRec* out, unsigned long long* work_counter,
-                           SampleCounters* counters, int num_sms, cudaStream_t stream);
+                           const int32_t* pids, const unsigned long long* cdf,
+                           const int32_t* guide, int guide_bits, const unsigned long long* qtot,
+                           const int64_t* offsets,
+                           const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
+                           int64_t k_end, int32_t* cell_of, HadronRec* out,
+                           unsigned long long* work_counter, SampleCounters* counters, int num_sms,
+                           cudaStream_t stream);
 
 }  // namespace iss

@@ -3,7 +3,7 @@
 //                         + calculate_dN_analytic (src/FSSW.cpp:565-848) for every
 //                           (cell, species) pair
 //   cdf kernels           RandomVariable1DArray (src/RandomVariable1DArray.cpp:25-74):
-//                         per-species FP64 prefix sums of the cell yields
+//                         per-species fixed-point prefix sums of the cell yields
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
@@ -92,22 +92,11 @@ __device__ __forceinline__ GridPos grid_pos(float xh, float xl) {
 // ------------------------------------------------------------------------
 constexpr int kYieldThreads = 128;
 
-__global__ void __launch_bounds__(kYieldThreads)
-yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
-              float* __restrict__ yields) {
-    extern __shared__ SpeciesDev s_sp[];
-    const int nsp = cfg.n_species;
-    for (int k = threadIdx.x; k < nsp; k += blockDim.x) s_sp[k] = species[k];
-    __syncthreads();
-    const int64_t n = cfg.n_cells;
-    const int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (l >= n) return;
-
-    const float4 da = cells.da[l];
-    if (da.x < 0.0f) {
-        for (int k = 0; k < nsp; k++) yields[static_cast<int64_t>(k) * n + l] = 0.0f;
-        return;
-    }
+// Yields of every species in cell l (not dropped: u.dsigma >= 0).
+__device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArrays& cells,
+                                            const SpeciesDev* s_sp, int nsp, int64_t n,
+                                            int64_t l, float4 da, float* __restrict__ yields,
+                                            uint32_t* s_max) {
     const float4 th = cells.th[l];
     const float4 th2 = cells.th2[l];
     const float4 cf = cells.coef[l];
@@ -241,149 +230,213 @@ yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ sp
             const float r5 = (T * T * T / 3.0f) * q2;
             total += ug * dsq * inv_kappa * (-pref_q * r4 - static_cast<float>(sp.baryon) * r5);
         }
-        yields[static_cast<int64_t>(k) * n + l] = fmaxf(total, 0.0f);
+        // negative -> 0 (FSSW::calculate_dN_dxtdy_for_one_particle_species,
+        // src/FSSW.cpp:707); NaN -> 0; +inf -> FLT_MAX so the cell CDF stays
+        // finite; -0 -> +0 so the bits order as the values
+        const float yv = __uint_as_float(
+            __float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
+        yields[static_cast<int64_t>(k) * n + l] = yv;
+        const unsigned am = __activemask();
+        const uint32_t wm = __reduce_max_sync(am, __float_as_uint(yv));
+        if ((threadIdx.x & 31) == __ffs(am) - 1 && wm) atomicMax(s_max + k, wm);
+    }
+}
+
+__global__ void __launch_bounds__(kYieldThreads)
+yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
+              float* __restrict__ yields, uint32_t* __restrict__ ymax) {
+    extern __shared__ SpeciesDev s_sp[];
+    const int nsp = cfg.n_species;
+    // per-species maximum yield of this block, as float bits (yields are >= 0,
+    // so the unsigned order of the bits is the order of the values)
+    uint32_t* s_max = reinterpret_cast<uint32_t*>(s_sp + nsp);
+    for (int k = threadIdx.x; k < nsp; k += blockDim.x) {
+        s_sp[k] = species[k];
+        s_max[k] = 0u;
+    }
+    __syncthreads();
+    const int64_t n = cfg.n_cells;
+    const int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (l < n) {
+        const float4 da = cells.da[l];
+        if (da.x < 0.0f) {
+            for (int k = 0; k < nsp; k++) yields[static_cast<int64_t>(k) * n + l] = 0.0f;
+        } else {
+            cell_yields(cfg, cells, s_sp, nsp, n, l, da, yields, s_max);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nsp; k += blockDim.x) {
+        const uint32_t v = s_max[k];
+        if (v) atomicMax(ymax + k, v);
     }
 }
 
 // ------------------------------------------------------------------------
-// per-species FP64 prefix sums over cells: tile sums, tile offsets, tile scan
+// per-species fixed-point prefix sums over cells (cdf_quantize): tile sums,
+// tile offsets and totals, tile scan with the guide-table scatter
 
 constexpr int kScanThreads = 256;
 constexpr int kScanPer = 16;
 constexpr int kScanTile = kScanThreads * kScanPer;
 
-__device__ __forceinline__ double warp_incl_scan(double v) {
+__device__ __forceinline__ unsigned long long warp_incl_scan_u64(unsigned long long v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, v, o);
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += t;
     }
     return v;
 }
 
-// exclusive block scan of one double per thread; returns the block total
-__device__ double block_excl_scan(double v, double* s_warp, double* total) {
+// exclusive block scan of one value per thread; returns the block total
+__device__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned long long* s_warp,
+                                                  unsigned long long* total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const double inc = warp_incl_scan(v);
+    const unsigned long long inc = warp_incl_scan_u64(v);
     if (lane == 31) s_warp[wid] = inc;
     __syncthreads();
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
-        double w = lane < nw ? s_warp[lane] : 0.0;
-        const double wi = warp_incl_scan(w);
+        const unsigned long long w = lane < nw ? s_warp[lane] : 0ull;
+        const unsigned long long wi = warp_incl_scan_u64(w);
         if (lane < nw) s_warp[lane] = wi - w;
         if (lane == nw - 1) s_warp[32] = wi;
     }
     __syncthreads();
-    const double out = s_warp[wid] + inc - v;
+    const unsigned long long out = s_warp[wid] + inc - v;
     *total = s_warp[32];
     __syncthreads();
     return out;
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_sum_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
-                    double* __restrict__ tile_sum) {
-    __shared__ double s_warp[33];
+cdf_tile_sum_kernel(const float* __restrict__ yields, const uint32_t* __restrict__ ymax, int64_t n,
+                    int n_tiles, unsigned long long* __restrict__ tile_sum) {
+    __shared__ unsigned long long s_warp[33];
     const int s = blockIdx.y;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
-    const float* row = yields + static_cast<int64_t>(s) * n;
-    double acc = 0.0;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
+    const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
+    unsigned long long acc = 0;
     for (int k = 0; k < kScanPer; k++) {
         const int64_t i = t0 + k * kScanThreads + threadIdx.x;
-        if (i < n) acc += static_cast<double>(fmaxf(row[i], 0.0f));
+        if (i < n) acc += cdf_quantize(row[i], base);
     }
-    double tot;
-    block_excl_scan(acc, s_warp, &tot);
+    unsigned long long tot;
+    block_excl_scan_u64(acc, s_warp, &tot);
     if (threadIdx.x == 0) tile_sum[static_cast<int64_t>(s) * n_tiles + blockIdx.x] = tot;
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_offset_kernel(const double* __restrict__ tile_sum, int n_tiles, int64_t n, int guide_len,
-                       double* __restrict__ tile_off, double* __restrict__ totals,
+cdf_tile_offset_kernel(const unsigned long long* __restrict__ tile_sum,
+                       const uint32_t* __restrict__ ymax, int n_tiles, int64_t n, int guide_bits,
+                       unsigned long long* __restrict__ tile_off, unsigned long long* __restrict__ qtot,
+                       double* __restrict__ totals, unsigned long long* __restrict__ cdf,
                        int32_t* __restrict__ guide) {
-    __shared__ double s_warp[33];
+    __shared__ unsigned long long s_warp[33];
     const int s = blockIdx.x;
-    double carry = 0.0;
+    unsigned long long carry = 0;
     for (int b = 0; b < n_tiles; b += kScanThreads) {
         const int i = b + threadIdx.x;
-        const double v = i < n_tiles ? tile_sum[static_cast<int64_t>(s) * n_tiles + i] : 0.0;
-        double tot;
-        const double ex = block_excl_scan(v, s_warp, &tot);
+        const unsigned long long v = i < n_tiles ? tile_sum[static_cast<int64_t>(s) * n_tiles + i] : 0ull;
+        unsigned long long tot;
+        const unsigned long long ex = block_excl_scan_u64(v, s_warp, &tot);
         if (i < n_tiles) tile_off[static_cast<int64_t>(s) * n_tiles + i] = carry + ex;
         carry += tot;
     }
     if (threadIdx.x == 0) {
-        totals[s] = carry;
-        int32_t* g = guide + static_cast<int64_t>(s) * (guide_len + 1);
-        g[0] = 0;
-        g[guide_len] = static_cast<int32_t>(n - 1);
+        const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
+        qtot[s] = carry;
+        totals[s] = carry ? ldexp(static_cast<double>(carry), -(150 + base)) : 0.0;
+        cdf[static_cast<int64_t>(s) * (n + 1) + n] = carry;
+        guide[(static_cast<int64_t>(s) << guide_bits) + s + (int64_t(1) << guide_bits)] =
+            static_cast<int32_t>(n - 1);
     }
 }
 
-// Writes the FP64 CDF row of species s and scatters its guide table
-// (indexed search, Chen & Asau 1974): bucket j of guide_len covers
-// v in [j, j+1) * total / guide_len and guide[j] is the cell whose CDF
-// interval contains the bucket's left edge, so the cell of any v in bucket j
-// lies in [guide[j], guide[j+1]].  Entries at tile seams may stay unset (-1);
-// the sampler then falls back to a full binary search.
+// f(j) = floor(j * Q / 2^g): the smallest v of guide bucket j (r >> (64 - g) == j)
+__device__ __forceinline__ unsigned long long bucket_start(unsigned long long j, int g,
+                                                           unsigned long long Q) {
+    return __umul64hi(j << (64 - g), Q);
+}
+
+// Writes row s of the cell CDF, C[i] = sum of q over cells < i, and scatters
+// the guide table (indexed search, Chen & Asau 1974): guide[j] is the cell
+// whose interval [C[i], C[i+1]) holds f(j).  The intervals partition [0, Q),
+// so every bucket j < 2^g gets exactly one writer; the cell of any v drawn
+// in bucket j lies in [guide[j], guide[j+1]].
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
-                     const double* __restrict__ tile_off, const double* __restrict__ totals,
-                     int guide_len, double* __restrict__ cdf, int32_t* __restrict__ guide) {
-    __shared__ float s_in[kScanThreads * (kScanPer + 1)];
-    __shared__ double s_warp[33];
-    __shared__ double s_last[kScanThreads];
+cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restrict__ ymax, int64_t n,
+                     int n_tiles, const unsigned long long* __restrict__ tile_off,
+                     const unsigned long long* __restrict__ qtot, int guide_bits,
+                     unsigned long long* __restrict__ cdf, int32_t* __restrict__ guide) {
+    // padded tile buffer: element e of the tile sits at (e / 16) * 17 + e % 16;
+    // it holds the FP32 yield bits on the way in and the CDF values on the way out
+    __shared__ unsigned long long s_buf[kScanThreads * (kScanPer + 1)];
+    __shared__ unsigned long long s_warp[33];
+    uint32_t* s_in = reinterpret_cast<uint32_t*>(s_buf);
     const int s = blockIdx.y;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
-    const float* row = yields + static_cast<int64_t>(s) * n;
-    double* out = cdf + static_cast<int64_t>(s) * (n + 1);
-    int32_t* g = guide + static_cast<int64_t>(s) * (guide_len + 1);
-    // coalesced load into a padded layout: element e -> (e / 16) * 17 + e % 16
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
+    unsigned long long* out = cdf + static_cast<int64_t>(s) * (n + 1);
+    const int g = guide_bits;
+    const int64_t G = int64_t(1) << g;
+    int32_t* gd = guide + s * (G + 1);
+    const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
+    const unsigned long long Q = qtot[s];
+    // coalesced load
     for (int k = 0; k < kScanPer; k++) {
         const int e = k * kScanThreads + threadIdx.x;
         const int64_t i = t0 + e;
-        s_in[(e / kScanPer) * (kScanPer + 1) + e % kScanPer] = i < n ? fmaxf(row[i], 0.0f) : 0.0f;
+        s_in[(e / kScanPer) * (kScanPer + 1) + e % kScanPer] = i < n ? row[i] : 0u;
     }
     __syncthreads();
-    const float* mine = s_in + threadIdx.x * (kScanPer + 1);
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < kScanPer; k++) acc += static_cast<double>(mine[k]);
-    double tot;
-    const double ex = block_excl_scan(acc, s_warp, &tot);
-    const double base = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x];
-    double run = base + ex;
-    double vals[kScanPer];
+    const uint32_t* mine = s_in + threadIdx.x * (kScanPer + 1);
+    unsigned long long q[kScanPer];
+    unsigned long long acc = 0;
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-        run += static_cast<double>(mine[k]);
-        vals[k] = run;
+        q[k] = cdf_quantize(mine[k], base);
+        acc += q[k];
     }
-    s_last[threadIdx.x] = run;
-    __syncthreads();
+    unsigned long long tot;
+    // (its barriers also order the reads of s_in above before the writes below)
+    const unsigned long long ex = block_excl_scan_u64(acc, s_warp, &tot);
+    const unsigned long long start = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x] + ex;
     const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kScanPer;
-    // value written just before this thread's first element
-    double prev = threadIdx.x == 0 ? base : s_last[threadIdx.x - 1];
-    const double total = totals[s];
-    const double scale = total > 0.0 ? static_cast<double>(guide_len) / total : 0.0;
+    unsigned long long run = start;
+    unsigned long long* mine_out = s_buf + threadIdx.x * (kScanPer + 1);
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-        const int64_t i = e0 + k;
-        if (i < n) {
-            out[i + 1] = vals[k];
-            if (scale > 0.0 && vals[k] > prev) {
-                int64_t jl = static_cast<int64_t>(floor(prev * scale)) + 1;
-                int64_t jh = static_cast<int64_t>(floor(vals[k] * scale));
-                jl = max(jl, static_cast<int64_t>(1));
-                jh = min(jh, static_cast<int64_t>(guide_len - 1));
-                for (int64_t j = jl; j <= jh; j++) g[j] = static_cast<int32_t>(i);
-            }
-        }
-        prev = vals[k];
+        mine_out[k] = run;
+        run += q[k];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = 0.0;
+    __syncthreads();
+    // coalesced store of C[t0 .. t0 + 4096)
+    for (int k = 0; k < kScanPer; k++) {
+        const int e = k * kScanThreads + threadIdx.x;
+        const int64_t i = t0 + e;
+        if (i < n) out[i] = s_buf[(e / kScanPer) * (kScanPer + 1) + e % kScanPer];
+    }
+    if (Q == 0 || e0 >= n || acc == 0) return;
+    // first bucket whose start lies at or after this thread's first cell:
+    // a float estimate of ceil(start * G / Q), then exact integer steps
+    int64_t j = static_cast<int64_t>(static_cast<float>(start) *
+                                     (static_cast<float>(G) / static_cast<float>(Q)));
+    j = j < 0 ? 0 : (j > G ? G : j);
+    while (j > 0 && bucket_start(static_cast<unsigned long long>(j - 1), g, Q) >= start) --j;
+    while (j < G && bucket_start(static_cast<unsigned long long>(j), g, Q) < start) ++j;
+    unsigned long long hi = start;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        hi += q[k];
+        while (j < G && bucket_start(static_cast<unsigned long long>(j), g, Q) < hi) {
+            gd[j] = static_cast<int32_t>(e0 + k);
+            ++j;
+        }
+    }
 }
 
 }  // namespace
@@ -392,39 +445,38 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t n, int n_tiles,
 // launch wrappers
 
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, cudaStream_t stream) {
+                          float* yields, uint32_t* ymax, cudaStream_t stream) {
+    if (cfg.n_species > 0) {
+        cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * cfg.n_species, stream);
+        if (e != cudaSuccess) return e;
+    }
     if (cfg.n_cells <= 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>((cfg.n_cells + kYieldThreads - 1) / kYieldThreads);
-    const size_t smem = sizeof(SpeciesDev) * static_cast<size_t>(cfg.n_species);
+    const size_t smem = (sizeof(SpeciesDev) + sizeof(uint32_t)) * static_cast<size_t>(cfg.n_species);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(yields_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    yields_kernel<<<blocks, kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
+    yields_kernel<<<blocks, kYieldThreads, smem, stream>>>(cfg, cells, sp, yields, ymax);
     return cudaGetLastError();
 }
 
 int cdf_num_tiles(int64_t n) { return static_cast<int>((n + kScanTile - 1) / kScanTile); }
 
-int cdf_guide_len(int64_t n) { return static_cast<int>(n < 4 ? 1 : (n + 3) / 4); }
-
-cudaError_t launch_cdf(const float* yields, int n_species, int64_t n, double* tile_sum,
-                       double* tile_off, double* totals, double* cdf, int32_t* guide,
-                       cudaStream_t stream) {
+cudaError_t launch_cdf(const float* yields, const uint32_t* ymax, int n_species, int64_t n,
+                       unsigned long long* tile_sum, unsigned long long* tile_off,
+                       unsigned long long* qtot, double* totals, unsigned long long* cdf,
+                       int32_t* guide, cudaStream_t stream) {
     const int nt = cdf_num_tiles(n);
     if (nt == 0 || n_species == 0) return cudaSuccess;
-    const int glen = cdf_guide_len(n);
-    cudaError_t e = cudaMemsetAsync(guide, 0xFF,
-                                    sizeof(int32_t) * static_cast<size_t>(glen + 1) * n_species,
-                                    stream);
-    if (e != cudaSuccess) return e;
+    const int g = cdf_guide_bits(n);
     dim3 grid(static_cast<unsigned>(nt), static_cast<unsigned>(n_species));
-    cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, nt, tile_sum);
-    cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, nt, n, glen, tile_off,
-                                                                   totals, guide);
-    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, nt, tile_off, totals, glen,
+    cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, ymax, n, nt, tile_sum);
+    cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, ymax, nt, n, g, tile_off,
+                                                                   qtot, totals, cdf, guide);
+    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, ymax, n, nt, tile_off, qtot, g,
                                                            cdf, guide);
     return cudaGetLastError();
 }

@@ -108,6 +108,28 @@ __device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
 
 constexpr int kItem = 64;   // hadrons per work item (one (event, species) segment)
 
+// Work items are ordered by event chunk (cfg.chunk_events consecutive events),
+// then species, then event: warps that run at the same time mostly sample one
+// species, whose cell CDF and guide table stay in L2, and the items of one
+// chunk are contiguous, so a chunk can be sampled (and its records copied
+// out) before the next.  The output slots stay event-major.
+__device__ __forceinline__ int64_t item_index(const DevConfig& cfg, int e, int s) {
+    const int c = e / cfg.chunk_events;
+    const int e0 = c * cfg.chunk_events;
+    const int ne = min(cfg.chunk_events, cfg.n_events - e0);
+    return static_cast<int64_t>(e0) * cfg.n_species + static_cast<int64_t>(s) * ne + (e - e0);
+}
+
+__device__ __forceinline__ void item_decode(const DevConfig& cfg, int q, int& e, int& s) {
+    const int per = cfg.chunk_events * cfg.n_species;
+    const int c = q / per;
+    const int e0 = c * cfg.chunk_events;
+    const int ne = min(cfg.chunk_events, cfg.n_events - e0);
+    const int r = q - c * per;
+    s = r / ne;
+    e = e0 + (r - s * ne);
+}
+
 __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
                               int32_t* __restrict__ counts, int32_t* __restrict__ items,
                               int* __restrict__ error) {
@@ -145,10 +167,11 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
     counts[idx] = c;
-    items[idx] = (c + kItem - 1) / kItem;
+    items[item_index(cfg, e, s)] = (c + kItem - 1) / kItem;
 }
 
-// item -> segment map: item_seg[item_off[seg] + k] = seg for k < items[seg]
+// item -> segment map: item_seg[item_off[q] + k] = q for k < items[q], q the
+// work-item order index of the segment (item_index)
 __global__ void item_map_kernel(const int32_t* __restrict__ items, const int64_t* __restrict__ item_off,
                                 int64_t nseg, int32_t* __restrict__ item_seg) {
     const int64_t seg = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -275,30 +298,24 @@ struct Unit {
     uint32_t t;
 };
 
-// largest i with row[i] < v <= row[i+1] (binarySearch of src/arsenal.cpp:644-678),
-// started from the guide table's bucket; falls back to the full range when
-// the bucket is unset or does not bracket v
-__device__ __forceinline__ int cell_search(const double* __restrict__ row, int64_t n,
-                                           const int32_t* __restrict__ g, int glen, double total,
-                                           double v) {
-    if (v > row[n]) return static_cast<int>(n - 1);
-    int64_t lo = 0, hi = n;
-    const double scale = total > 0.0 ? static_cast<double>(glen) / total : 0.0;
-    int64_t j = static_cast<int64_t>(floor(v * scale));
-    j = min(max(j, static_cast<int64_t>(0)), static_cast<int64_t>(glen - 1));
-    const int g0 = g[j], g1 = g[j + 1];
-    if (g0 >= 0 && g1 >= g0) {
-        const int64_t a = g0, b = static_cast<int64_t>(g1) + 1;
-        if (row[a] < v && v <= row[b]) {
-            lo = a;
-            hi = b;
-        }
+// Cell draw from 64 random bits r on the fixed-point CDF row C[0..n]
+// (cdf_quantize): v = floor(r * Q / 2^64), and the cell is the i with
+// C[i] <= v < C[i+1] -- the reference's binarySearch (src/arsenal.cpp:644-678)
+// on integer sums.  The guide bucket j = r >> (64 - g) brackets the cell by
+// guide[j] <= i <= guide[j+1]; when both agree no CDF entry is read.
+__device__ __forceinline__ int cell_search(const unsigned long long* __restrict__ row, int64_t n,
+                                           const int32_t* __restrict__ gd, int g,
+                                           unsigned long long Q, unsigned long long r) {
+    const unsigned long long v = __umul64hi(r, Q);
+    const unsigned j = static_cast<unsigned>(r >> (64 - g));
+    const int2 b = make_int2(__ldg(gd + j), __ldg(gd + j + 1));
+    const int last = static_cast<int>(n - 1);
+    int lo = min(max(b.x, 0), last), hi = min(max(b.y, lo), last);
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(row + mid) <= v) lo = mid; else hi = mid - 1;
     }
-    while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (row[mid] < v) lo = mid; else hi = mid;
-    }
-    return static_cast<int>(lo);
+    return lo;
 }
 
 // returns false when m/T - mu/T is outside the reference's momentum tables
@@ -567,22 +584,62 @@ __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& 
                  pos.x * sinhf(eta_s));
 }
 
+// Cell of every hadron's first draw (redraw 0), one warp per work item in
+// species-major order.  Each lane runs independent searches, so the latency
+// of the guide and CDF reads overlaps across many warps; the sampler then
+// starts each hadron from cell_of[slot] instead of a dependent search.
+constexpr int kAssignThreads = 256;
+
+__global__ void __launch_bounds__(kAssignThreads)
+cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
+                   const int32_t* __restrict__ guide, int guide_bits,
+                   const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
+                   const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
+                   int64_t k_begin, int64_t k_end, int32_t* __restrict__ cell_of) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t ncell = cfg.n_cells;
+    for (int64_t k = k_begin + warp; k < k_end; k += n_warps) {
+        const int q = item_seg[k];
+        const int64_t j = k - item_off[q];
+        int e, s;
+        item_decode(cfg, q, e, s);
+        const int64_t seg = static_cast<int64_t>(e) * cfg.n_species + s;
+        const int64_t base = offsets[seg];
+        const int64_t start = base + j * kItem;
+        const int64_t end = min(start + kItem, offsets[seg + 1]);
+        const unsigned long long* row = cdf + static_cast<int64_t>(s) * (ncell + 1);
+        const int32_t* gd = guide + static_cast<int64_t>(s) * ((int64_t(1) << guide_bits) + 1);
+        const unsigned long long Q = qtot[s];
+        const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
+        const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
+        for (int64_t h = start + lane; h < end; h += 32) {
+            const uint4 w = block(0u, static_cast<uint32_t>(h - base), eg, c3, cfg.key0, cfg.key1);
+            const unsigned long long r =
+                (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
+            cell_of[h] = cell_search(row, ncell, gd, guide_bits, Q, r);
+        }
+    }
+}
+
 constexpr int kSampleThreads = 256;
 
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
-               const int32_t* __restrict__ pids, const double* __restrict__ cdf,
-               const int32_t* __restrict__ guide, int guide_len,
-               const double* __restrict__ totals, const int64_t* __restrict__ offsets,
+               const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
+               const int32_t* __restrict__ guide, int guide_bits,
+               const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
-               int64_t n_items, HadronRec* __restrict__ out,
+               int64_t k_begin, int64_t k_end, const int32_t* __restrict__ cell_of,
+               HadronRec* __restrict__ out,
                unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t ncell = cfg.n_cells;
-    // the warp's current work item: units [next, end) of segment cur_seg
+    // the warp's current work item: units [next, end) of species cur_s in event cur_e
     int64_t next = 0, end = 0, seg_base = 0;
-    int cur_seg = 0;
+    int cur_s = 0, cur_e = 0;
     bool exhausted = false;
     bool active = false;
     Unit u;
@@ -598,26 +655,28 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
             if (need == 0 || exhausted) break;
             if (next >= end) {
                 long long k = 0;
-                if (lane == 0) k = static_cast<long long>(atomicAdd(work_counter, 1ull));
+                if (lane == 0) k = k_begin + static_cast<long long>(atomicAdd(work_counter, 1ull));
                 k = __shfl_sync(FULL, k, 0);
-                if (k >= n_items) {
+                if (k >= k_end) {
                     exhausted = true;
                     break;
                 }
-                cur_seg = item_seg[k];
-                const int64_t j = k - item_off[cur_seg];
-                seg_base = offsets[cur_seg];
+                const int q = item_seg[k];
+                const int64_t j = k - item_off[q];
+                item_decode(cfg, q, cur_e, cur_s);
+                const int64_t seg = static_cast<int64_t>(cur_e) * cfg.n_species + cur_s;
+                seg_base = offsets[seg];
                 next = seg_base + j * kItem;
-                end = min(next + kItem, offsets[cur_seg + 1]);
+                end = min(next + kItem, offsets[seg + 1]);
             }
             const int64_t avail = end - next;
             const int rank = __popc(need & ((1u << lane) - 1u));
             if (!active && rank < avail) {
                 const int64_t h = next + rank;
-                u.s = cur_seg % cfg.n_species;
+                u.s = cur_s;
                 u.slot = h;
                 u.i = static_cast<uint32_t>(h - seg_base);
-                u.eg = cfg.event_offset + static_cast<uint32_t>(cur_seg / cfg.n_species);
+                u.eg = cfg.event_offset + static_cast<uint32_t>(cur_e);
                 u.redraw = 0;
                 u.t = 0;
                 u.tries_cell = 0;
@@ -640,15 +699,20 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                     active = false;
                     continue;
                 }
-                const uint4 w = block(static_cast<uint32_t>(u.redraw), u.i, u.eg,
-                                      static_cast<uint32_t>(u.s) | (kTagCell << 16), cfg.key0,
-                                      cfg.key1);
-                const double* row = cdf + static_cast<int64_t>(u.s) * (ncell + 1);
-                const double tot = totals[u.s];
-                const double v = u53(w.x, w.y) * (tot - 1e-15);
-                int l = cell_search(row, ncell, guide + static_cast<int64_t>(u.s) * (guide_len + 1),
-                                    guide_len, tot, v);
-                l = max(0, min(l, static_cast<int>(ncell - 1)));
+                int l;
+                if (u.redraw == 0) {
+                    l = cell_of[u.slot];
+                } else {
+                    const uint4 w = block(static_cast<uint32_t>(u.redraw), u.i, u.eg,
+                                          static_cast<uint32_t>(u.s) | (kTagCell << 16), cfg.key0,
+                                          cfg.key1);
+                    const unsigned long long r = (static_cast<unsigned long long>(w.x) << 32) |
+                                                 static_cast<unsigned long long>(w.y);
+                    l = cell_search(
+                        cdf + static_cast<int64_t>(u.s) * (ncell + 1), ncell,
+                        guide + static_cast<int64_t>(u.s) * ((int64_t(1) << guide_bits) + 1),
+                        guide_bits, qtot[u.s], r);
+                }
                 u.cell = l;
                 u.tries_cell = 0;
                 if (!setup_prop(cfg, cells, species[u.s], l, p)) {
@@ -720,20 +784,30 @@ cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64
 }
 
 cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                           const int32_t* pids, const double* cdf, const int32_t* guide,
-                           int guide_len, const double* totals, const int64_t* offsets,
-                           const int64_t* item_off, const int32_t* item_seg, int64_t n_items,
-                           HadronRec* out, unsigned long long* work_counter,
-                           SampleCounters* counters, int num_sms, cudaStream_t stream) {
+                           const int32_t* pids, const unsigned long long* cdf,
+                           const int32_t* guide, int guide_bits, const unsigned long long* qtot,
+                           const int64_t* offsets,
+                           const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
+                           int64_t k_end, int32_t* cell_of, HadronRec* out,
+                           unsigned long long* work_counter, SampleCounters* counters, int num_sms,
+                           cudaStream_t stream) {
+    const int64_t n_items = k_end - k_begin;
     if (n_items <= 0) return cudaSuccess;
+    {
+        int64_t blocks = static_cast<int64_t>(num_sms) * 8;
+        const int64_t need = (n_items + (kAssignThreads / 32) - 1) / (kAssignThreads / 32);
+        if (blocks > need) blocks = need;
+        cell_assign_kernel<<<static_cast<unsigned>(blocks), kAssignThreads, 0, stream>>>(
+            cfg, cdf, guide, guide_bits, qtot, offsets, item_off, item_seg, k_begin, k_end, cell_of);
+    }
     const int per_sm = 3;
     int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
     sampler_kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
-        cfg, cells, sp, pids, cdf, guide, guide_len, totals, offsets, item_off, item_seg, n_items,
-        out, work_counter, counters);
+        cfg, cells, sp, pids, cdf, guide, guide_bits, qtot, offsets, item_off, item_seg, k_begin,
+        k_end, cell_of, out, work_counter, counters);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,8 @@ OUTPUT_OSCAR, OUTPUT_GZIP, OUTPUT_BINARY = 1, 2, 3
 EXPORTED = [
     "iss_gpu_create", "iss_gpu_destroy", "iss_gpu_set_param", "iss_gpu_get_param",
     "iss_gpu_parse_param_line", "iss_gpu_set_seed", "iss_gpu_set_seed_from_params",
-    "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_generate", "iss_gpu_shell",
+    "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_generate", "iss_gpu_generate_into",
+    "iss_gpu_shell",
     "iss_gpu_clear", "iss_gpu_num_events", "iss_gpu_num_particles", "iss_gpu_get_hadron",
     "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output", "iss_gpu_species",
     "iss_gpu_species_yields", "iss_gpu_num_cells", "iss_gpu_copy_lrf_cells",
@@ -78,6 +79,7 @@ def lib():
         L.iss_gpu_read_surface.argtypes = [h]
         L.iss_gpu_set_surface.argtypes = [h, v, C.c_int64]
         L.iss_gpu_generate.argtypes = [h]
+        L.iss_gpu_generate_into.argtypes = [h, v, C.c_int64, C.POINTER(C.c_int64)]
         L.iss_gpu_shell.argtypes = [h]
         L.iss_gpu_clear.argtypes = [h]
         L.iss_gpu_num_events.argtypes = [h, C.POINTER(C.c_int32)]
@@ -183,6 +185,17 @@ class iSS:
 
     def generate_samples(self):
         return self._check(self._L.iss_gpu_generate(self._h))
+
+    def generate_into(self, out):
+        """generate_samples with every event's hadrons copied into `out` (a
+        HADRON_DTYPE array, best in pinned memory) while later events are
+        still being sampled; returns (hadrons, event_offsets)."""
+        n = C.c_int64()
+        self._check(self._L.iss_gpu_generate_into(self._h, _ptr(out), out.size, C.byref(n)))
+        nev = self.get_number_of_sampled_events()
+        off = np.zeros(nev + 1, dtype=np.int64)
+        self._check(self._L.iss_gpu_copy_all(self._h, None, 0, _ptr(off), None))
+        return out[:n.value], off
 
     def shell(self):
         return self._check(self._L.iss_gpu_shell(self._h))

@@ -430,21 +430,62 @@ int orc_yields(const orc_cfg* c, const orc_species* sp, int32_t n_sp, const floa
     return status;
 }
 
-/* RandomVariable1DArray, src/RandomVariable1DArray.cpp:25-74: sequential
- * FP64 prefix sums of the (non-negative) per-cell yields, one row of n+1
- * entries per species, cdf[0] = 0. */
-void orc_cdf(const float* yields_f32, int32_t n_sp, int64_t n, double* cdf, double* totals) {
+/* Cell CDF of the GPU sampler: RandomVariable1DArray
+ * (src/RandomVariable1DArray.cpp:25-74) on fixed-point yields.  Each FP32 yield
+ * y of species k becomes q = floor(y * 2^E_k), where E_k = 188 - e_max - L:
+ *   - e_max is the biased exponent of the species' largest yield;
+ *   - L = ceil(log2 n).
+ * So every q < 2^(62-L) and the row sum Q_k < 2^62.  Row k holds the
+ * exclusive prefix sums C[0..n] (C[n] = Q_k).  qtot[k] = Q_k and
+ * totals[k] = Q_k * 2^-E_k.  Integer sums are exact, so the GPU's tiled scan
+ * gives the same bits. */
+static int orc_log2_cells(int64_t n) {
+    int L = 0;
+    while (L < 62 && ((int64_t)1 << L) < n) ++L;
+    return L;
+}
+
+static uint64_t orc_quantize(uint32_t b, int base) {
+    int e = (int)((b >> 23) & 0xFFu);
+    uint32_t m = b & 0x7FFFFFu;
+    if (e) m |= 0x800000u; else e = 1;
+    const int sh = e + base;
+    if (sh >= 0) return (uint64_t)m << sh;
+    if (sh <= -24) return 0;
+    return (uint64_t)(m >> (-sh));
+}
+
+void orc_cdf(const float* yields_f32, int32_t n_sp, int64_t n, uint64_t* cdf, uint64_t* qtot,
+             double* totals) {
+    const int L = orc_log2_cells(n);
     for (int32_t k = 0; k < n_sp; k++) {
-        double sum = 0.0;
-        double* row = cdf + (int64_t)k * (n + 1);
-        row[0] = 0.0;
+        const float* y = yields_f32 + (int64_t)k * n;
+        uint32_t ymax = 0;
         for (int64_t l = 0; l < n; l++) {
-            double v = yields_f32[(int64_t)k * n + l];
-            if (v < 0) v = 0;
-            sum += v;
-            row[l + 1] = sum;
+            float v = y[l];
+            if (!(v > 0.0f)) v = 0.0f;            /* negative, -0 and NaN -> +0 */
+            if (v > 3.40282347e38f) v = 3.40282347e38f;
+            uint32_t b;
+            memcpy(&b, &v, 4);
+            if (b > ymax) ymax = b;
         }
-        totals[k] = sum;
+        int ex = (int)((ymax >> 23) & 0xFFu);
+        if (ex == 0) ex = 1;
+        const int base = 38 - L - ex;
+        uint64_t* row = cdf + (int64_t)k * (n + 1);
+        uint64_t sum = 0;
+        for (int64_t l = 0; l < n; l++) {
+            float v = y[l];
+            if (!(v > 0.0f)) v = 0.0f;
+            if (v > 3.40282347e38f) v = 3.40282347e38f;
+            uint32_t b;
+            memcpy(&b, &v, 4);
+            row[l] = sum;
+            sum += orc_quantize(b, base);
+        }
+        row[n] = sum;
+        qtot[k] = sum;
+        totals[k] = sum ? ldexp((double)sum, -(150 + base)) : 0.0;
     }
 }
 

@@ -87,14 +87,15 @@ void orc_lrf_cells(const float* fo34, int64_t n, float* lrf28, int32_t* keep);
 void orc_cell_coeffs(const orc_cfg* c, const float* lrf28, int64_t n, double* coef4);
 int orc_yields(const orc_cfg* c, const orc_species* sp, int32_t n_sp,
                const float* lrf28, const int32_t* keep, int64_t n, double* yields);
-void orc_cdf(const float* yields_f32, int32_t n_sp, int64_t n, double* cdf, double* totals);
+void orc_cdf(const float* yields_f32, int32_t n_sp, int64_t n, uint64_t* cdf, uint64_t* qtot,
+             double* totals);
 
 /* Part 2 */
 int orc_counts(const orc_cfg* c, const orc_species* sp, int32_t n_sp, const double* totals,
                int32_t* counts);
 int64_t orc_sample_replay(const orc_cfg* c, const orc_species* sp, int32_t n_sp,
                           const float* lrf28, int64_t n_cells, const float* coef4,
-                          const double* cdf, const double* totals, const int32_t* counts,
+                          const uint64_t* cdf, const uint64_t* qtot, const int32_t* counts,
                           orc_hadron* out, int64_t capacity, orc_stats* stats);
 
 /* Part 3 */

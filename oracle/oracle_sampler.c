@@ -47,15 +47,16 @@ static void orc_load_cell(const float* lrf28, const float* coef4, int64_t l, orc
     c->vis2 = coef4[4 * l + 2]; c->kappa = coef4[4 * l + 3];
 }
 
-/* binarySearch semantics (src/arsenal.cpp:644-678) on cdf[0..n]: the largest
- * index i with cdf[i] < v <= cdf[i+1]. */
-static int64_t orc_search(const double* cdf, int64_t n, double v) {
-    if (v > cdf[n]) return n;
-    if (v < cdf[0]) return -1;
-    int64_t lo = 0, hi = n;
-    while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) / 2;
-        if (cdf[mid] < v) lo = mid; else hi = mid;
+/* Cell draw of the GPU sampler on the fixed-point CDF C[0..n] (orc_cdf):
+ * v = floor(r * Q / 2^64) for 64 random bits r, and the cell is the largest i
+ * with C[i] <= v, i.e. C[i] <= v < C[i+1] -- binarySearch
+ * (src/arsenal.cpp:644-678) on integer sums. */
+static int64_t orc_search(const uint64_t* cdf, int64_t n, uint64_t Q, uint64_t r) {
+    const uint64_t v = (uint64_t)(((unsigned __int128)r * Q) >> 64);
+    int64_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (cdf[mid] <= v) lo = mid; else hi = mid - 1;
     }
     return lo;
 }
@@ -300,7 +301,7 @@ static void orc_emit(const orc_cfg* cfg, const orc_cell* c, double m, int32_t pi
 
 int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_sp,
                           const float* lrf28, int64_t n_cells, const float* coef4,
-                          const double* cdf, const double* totals, const int32_t* counts,
+                          const uint64_t* cdf, const uint64_t* qtot, const int32_t* counts,
                           orc_hadron* out, int64_t capacity, orc_stats* stats) {
     memset(stats, 0, sizeof(*stats));
     int64_t w = 0;
@@ -309,7 +310,7 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
         for (int32_t k = 0; k < n_sp; k++) {
             const int32_t n_units = counts[e * n_sp + k];
             const orc_species* s = sp + k;
-            const double* row = cdf + (int64_t)k * (n_cells + 1);
+            const uint64_t* row = cdf + (int64_t)k * (n_cells + 1);
             for (int32_t i = 0; i < n_units; i++) {
                 if (w >= capacity) return -1;
                 orc_hstream hs;
@@ -324,10 +325,8 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
                 while (!done) {
                     uint32_t wc[4];
                     orc_hblock(&hs, (uint32_t)redraw, ORC_TAG_CELL, wc);
-                    const double v = orc_u53(wc[0], wc[1]) * (totals[k] - 1e-15);
-                    int64_t l = orc_search(row, n_cells, v);
-                    if (l < 0) l = 0;
-                    if (l >= n_cells) l = n_cells - 1;
+                    const uint64_t r = ((uint64_t)wc[0] << 32) | (uint64_t)wc[1];
+                    const int64_t l = orc_search(row, n_cells, qtot[k], r);
                     orc_cell c;
                     orc_load_cell(lrf28, coef4, l, &c);
                     orc_prop p;

@@ -82,7 +82,7 @@ def _setup(L):
     L.orc_cell_coeffs.argtypes = [C.POINTER(Cfg), v, C.c_int64, v]
     L.orc_yields.argtypes = [C.POINTER(Cfg), v, C.c_int32, v, v, C.c_int64, v]
     L.orc_yields.restype = C.c_int
-    L.orc_cdf.argtypes = [v, C.c_int32, C.c_int64, v, v]
+    L.orc_cdf.argtypes = [v, C.c_int32, C.c_int64, v, v, v]
     L.orc_counts.argtypes = [C.POINTER(Cfg), v, C.c_int32, v, v]
     L.orc_counts.restype = C.c_int
     L.orc_sample_replay.argtypes = [C.POINTER(Cfg), v, C.c_int32, v, C.c_int64, v, v, v, v,
@@ -265,11 +265,14 @@ def yields(oc: OracleConfig, sp, lrf, keep=None):
 
 
 def cdf(yields_f32):
+    """Fixed-point cell CDF of the GPU sampler: (rows, totals), rows uint64
+    (n_species, n_cells + 1) with rows[:, -1] the integer totals Q."""
     y = np.ascontiguousarray(yields_f32, dtype=np.float32)
     n_sp, n = y.shape
-    c = np.zeros((n_sp, n + 1))
+    c = np.zeros((n_sp, n + 1), dtype=np.uint64)
+    q = np.zeros(n_sp, dtype=np.uint64)
     tot = np.zeros(n_sp)
-    lib().orc_cdf(_p(y), n_sp, n, _p(c), _p(tot))
+    lib().orc_cdf(_p(y), n_sp, n, _p(c), _p(q), _p(tot))
     return c, tot
 
 
@@ -283,18 +286,18 @@ def counts(oc: OracleConfig, sp, totals):
     return out
 
 
-def sample_replay(oc: OracleConfig, sp, lrf, coef4, cdf_rows, totals, cnt):
+def sample_replay(oc: OracleConfig, sp, lrf, coef4, cdf_rows, cnt):
     arr = species_array(sp)
     lrf = np.ascontiguousarray(lrf, dtype=np.float32)
     coef = np.ascontiguousarray(coef4, dtype=np.float32)
-    cdf_rows = np.ascontiguousarray(cdf_rows, dtype=np.float64)
-    tot = np.ascontiguousarray(totals, dtype=np.float64)
+    cdf_rows = np.ascontiguousarray(cdf_rows, dtype=np.uint64)
+    qtot = np.ascontiguousarray(cdf_rows[:, -1])
     cnt = np.ascontiguousarray(cnt, dtype=np.int32)
     cap = int(cnt.sum())
     out = np.zeros(max(cap, 1), dtype=HADRON_DTYPE)
     st = Stats()
     n = lib().orc_sample_replay(C.byref(oc.cfg), C.cast(arr, C.c_void_p), len(sp), _p(lrf),
-                                lrf.shape[0], _p(coef), _p(cdf_rows), _p(tot), _p(cnt),
+                                lrf.shape[0], _p(coef), _p(cdf_rows), _p(qtot), _p(cnt),
                                 _p(out), cap, C.byref(st))
     if n < 0:
         raise RuntimeError(f"orc_sample_replay status {n}")

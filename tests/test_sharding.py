@@ -31,7 +31,7 @@ def _sample(event_offset, n_events):
                         event_offset=event_offset)
     cnt = O.counts(oc, g["species"], tot)
     coef = O.cell_coeffs(oc, lrf).astype(np.float32)
-    had, _ = O.sample_replay(oc, g["species"], lrf, coef, cdf, tot, cnt)
+    had, _ = O.sample_replay(oc, g["species"], lrf, coef, cdf, cnt)
     return had
 
 
