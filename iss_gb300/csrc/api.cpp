@@ -112,7 +112,7 @@ struct iss_handle {
     TableKey table_key;
     DevBuf<float4> d_sfK;
     DevBuf<float> d_sfE;
-    DevBuf<double> d_b14c0, d_b14c1, d_b14c2, d_ce, d_qmu;
+    DevBuf<double> d_b14c0, d_b14c1, d_b14c2, d_ce, d_qmu, d_logfact, d_pois;
     Bulk14Table b14;
 
     // last generate
@@ -134,7 +134,8 @@ struct iss_handle {
             d_cells.release();
             d_species.release();
             d_pids.release();
-            DevBuf<double>* db[] = {&d_totals, &d_b14c0, &d_b14c1, &d_b14c2, &d_ce, &d_qmu};
+            DevBuf<double>* db[] = {&d_totals, &d_b14c0, &d_b14c1, &d_b14c2, &d_ce, &d_qmu,
+                                    &d_logfact, &d_pois};
             for (auto* b : db) b->release();
             DevBuf<unsigned long long>* ub[] = {&d_cdf, &d_tile_sum, &d_tile_off, &d_qtot};
             for (auto* b : ub) b->release();
@@ -329,6 +330,15 @@ iss_status prepare(iss_handle* h) {
         }
         h->table_key = key;
     }
+    if (!h->d_logfact.ptr) {
+        // log(k!) for k < 256, from the C library's lgamma (Poisson draws)
+        std::vector<double> lf(kLogFactLen);
+        for (int i = 0; i < kLogFactLen; i++) lf[i] = std::lgamma(i + 1.0);
+        CUDA_TRY(h, h->d_logfact.reserve(kLogFactLen));
+        CUDA_TRY(h, cudaMemcpy(h->d_logfact.ptr, lf.data(), sizeof(double) * kLogFactLen,
+                               cudaMemcpyHostToDevice));
+    }
+    c.tab.logfact = h->d_logfact.ptr;
     c.tab.sfK = h->d_sfK.ptr;
     c.tab.sfE = h->d_sfE.ptr;
     c.tab.b14c0 = h->d_b14c0.ptr;
@@ -412,7 +422,7 @@ iss_status run_cells(iss_handle* h) {
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
     CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvPrologue], st));
-    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, h->d_ymax.ptr, st));
+    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
     CUDA_TRY(h, launch_cdf(h->d_yields.ptr, h->d_ymax.ptr, S, n, h->d_tile_sum.ptr,
                            h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
@@ -484,7 +494,12 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, h->d_work.reserve(static_cast<size_t>(n_chunks)));
     CUDA_TRY(h, h->d_counters.reserve(1));
     CUDA_TRY(h, cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
-    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_counts.ptr, h->d_items.ptr, h->d_error.ptr, s));
+    // per species: kPoissonConsts constants, then an inversion table of
+    // kInvTable + 1 doubles (the last holds the length)
+    CUDA_TRY(h, h->d_pois.reserve(static_cast<size_t>(std::max(S, 1)) *
+                                  (kPoissonConsts + kInvTable + 1)));
+    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr, h->d_items.ptr,
+                              h->d_error.ptr, s));
     CUDA_TRY(h, launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
     CUDA_TRY(h, launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
     int64_t sizes[2] = {0, 0};   // hadrons, work items
@@ -571,7 +586,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures);
-    t.kernel_launches = 13 + 2 * n_chunks;
+    t.kernel_launches = 15 + 2 * n_chunks;
     h->n_events = c.n_events;
     h->n_hadrons = n_units;
     h->samples_valid = true;

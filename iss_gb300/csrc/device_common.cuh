@@ -21,7 +21,12 @@ struct DevTables {
     double b14_T0, b14_mu0, b14_dT, b14_dmu;
     const double* ce;       // NEoS-BQS Chapman-Enskog, 200 * 200 rows of 5
     const double* qmu;      // RTA diffusion coefficient, 150 * 100
+    const double* logfact;  // [kLogFactLen] log(k!) from the C library's lgamma
 };
+
+constexpr int kLogFactLen = 256;
+constexpr int kPoissonConsts = 8;   // doubles per species, see poisson_consts
+constexpr int kInvTable = 127;      // inversion CDF entries per species (+ length: 128 doubles)
 
 struct DevConfig {
     int hydro_mode;
@@ -160,8 +165,10 @@ __device__ __forceinline__ float u01f_pos(uint32_t x) {
 }
 // [0, 1), 53 bits
 __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
-    return (static_cast<double>(a >> 5) * 67108864.0 + static_cast<double>(b >> 6)) *
-           (1.0 / 9007199254740992.0);
+    // (a >> 5) * 2^26 + (b >> 6) is an integer below 2^53: converted exactly
+    const unsigned long long m =
+        (static_cast<unsigned long long>(a >> 5) << 26) | static_cast<unsigned long long>(b >> 6);
+    return static_cast<double>(m) * (1.0 / 9007199254740992.0);
 }
 
 // ---------------------------------------------------------------------------

@@ -12,17 +12,21 @@ namespace iss {
 cudaError_t launch_cell_prologue(const DevConfig& cfg, const float* fo34, int64_t n,
                                  const CellArrays& cells, cudaStream_t stream);
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, uint32_t* ymax, cudaStream_t stream);
+                          float* yields, cudaStream_t stream);
 int cdf_num_tiles(int64_t n);
-// fixed-point cell CDF (cdf_quantize): row s holds n + 1 entries C[0..n],
+// fixed-point cell CDF (cdf_quantize), four launches (species maxima ymax,
+// tile sums, tile offsets, scan): row s holds n + 1 entries C[0..n],
 // the guide table 2^g + 1 entries per species, g = cdf_guide_bits(n)
-cudaError_t launch_cdf(const float* yields, const uint32_t* ymax, int n_species, int64_t n,
+cudaError_t launch_cdf(const float* yields, uint32_t* ymax, int n_species, int64_t n,
                        unsigned long long* tile_sum, unsigned long long* tile_off,
                        unsigned long long* qtot, double* totals, unsigned long long* cdf,
                        int32_t* guide, cudaStream_t stream);
 
 // kernels_sample.cu
-cudaError_t launch_counts(const DevConfig& cfg, const double* totals, int32_t* counts,
+// two launches: per-species Poisson constants and inversion tables (pois,
+// (kPoissonConsts + kInvTable + 1) doubles per species), then one count per
+// (event, species)
+cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* pois, int32_t* counts,
                           int32_t* items, int* error, cudaStream_t stream);
 int offsets_num_tiles(int64_t n);
 cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_sum,

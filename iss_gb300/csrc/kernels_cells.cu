@@ -91,12 +91,13 @@ __device__ __forceinline__ GridPos grid_pos(float xh, float xl) {
 
 // ------------------------------------------------------------------------
 constexpr int kYieldThreads = 128;
+constexpr int kYieldGroups = 4;   // species groups per cell (grid y)
 
-// Yields of every species in cell l (not dropped: u.dsigma >= 0).
+// Yields of species k0, k0 + kstep, ... in cell l (not dropped: u.dsigma >= 0).
 __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArrays& cells,
-                                            const SpeciesDev* s_sp, int nsp, int64_t n,
-                                            int64_t l, float4 da, float* __restrict__ yields,
-                                            uint32_t* s_max) {
+                                            const SpeciesDev* s_sp, int nsp, int k0, int kstep,
+                                            int64_t n, int64_t l, float4 da,
+                                            float* __restrict__ yields) {
     const float4 th = cells.th[l];
     const float4 th2 = cells.th2[l];
     const float4 cf = cells.coef[l];
@@ -124,7 +125,7 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
     const float unit_pref = (1.0f / (0.197327053f * 0.197327053f * 0.197327053f)) /
                             (2.0f * 9.8696044010893586f);
 
-    for (int k = 0; k < nsp; k++) {
+    for (int k = k0; k < nsp; k += kstep) {
         const SpeciesDev sp = s_sp[k];
         const float mass = sp.m_hi + sp.m_lo;
         const float mu = static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
@@ -236,39 +237,29 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
         const float yv = __uint_as_float(
             __float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
         yields[static_cast<int64_t>(k) * n + l] = yv;
-        const unsigned am = __activemask();
-        const uint32_t wm = __reduce_max_sync(am, __float_as_uint(yv));
-        if ((threadIdx.x & 31) == __ffs(am) - 1 && wm) atomicMax(s_max + k, wm);
     }
 }
 
 __global__ void __launch_bounds__(kYieldThreads)
 yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
-              float* __restrict__ yields, uint32_t* __restrict__ ymax) {
+              float* __restrict__ yields) {
     extern __shared__ SpeciesDev s_sp[];
     const int nsp = cfg.n_species;
-    // per-species maximum yield of this block, as float bits (yields are >= 0,
-    // so the unsigned order of the bits is the order of the values)
-    uint32_t* s_max = reinterpret_cast<uint32_t*>(s_sp + nsp);
-    for (int k = threadIdx.x; k < nsp; k += blockDim.x) {
-        s_sp[k] = species[k];
-        s_max[k] = 0u;
-    }
+    for (int k = threadIdx.x; k < nsp; k += blockDim.x) s_sp[k] = species[k];
     __syncthreads();
     const int64_t n = cfg.n_cells;
     const int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // blockIdx.y picks every gridDim.y-th species: the light species (ten
+    // series terms each) come first in mass order, so interleaving keeps the
+    // groups' work equal, and the grid has several waves of blocks
+    const int k0 = blockIdx.y, kstep = gridDim.y;
     if (l < n) {
         const float4 da = cells.da[l];
         if (da.x < 0.0f) {
-            for (int k = 0; k < nsp; k++) yields[static_cast<int64_t>(k) * n + l] = 0.0f;
+            for (int k = k0; k < nsp; k += kstep) yields[static_cast<int64_t>(k) * n + l] = 0.0f;
         } else {
-            cell_yields(cfg, cells, s_sp, nsp, n, l, da, yields, s_max);
+            cell_yields(cfg, cells, s_sp, nsp, k0, kstep, n, l, da, yields);
         }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nsp; k += blockDim.x) {
-        const uint32_t v = s_max[k];
-        if (v) atomicMax(ymax + k, v);
     }
 }
 
@@ -277,7 +268,7 @@ yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ sp
 // tile offsets and totals, tile scan with the guide-table scatter
 
 constexpr int kScanThreads = 256;
-constexpr int kScanPer = 16;
+constexpr int kScanPer = 8;
 constexpr int kScanTile = kScanThreads * kScanPer;
 
 __device__ __forceinline__ unsigned long long warp_incl_scan_u64(unsigned long long v) {
@@ -311,22 +302,53 @@ __device__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned
     return out;
 }
 
+// per-species maximum yield, as float bits (the yields are >= +0, so the
+// unsigned order of the bits is the order of the values); ymax starts at 0
+__global__ void __launch_bounds__(kScanThreads)
+cdf_tile_max_kernel(const float* __restrict__ yields, int64_t n, uint32_t* __restrict__ ymax) {
+    const int s = blockIdx.y;
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
+    uint32_t v[kScanPer];
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        const int64_t i = t0 + k * kScanThreads + threadIdx.x;
+        v[k] = i < n ? __ldg(row + i) : 0u;
+    }
+    uint32_t m = 0u;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) m = max(m, v[k]);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(ymax + s, m);
+}
+
 __global__ void __launch_bounds__(kScanThreads)
 cdf_tile_sum_kernel(const float* __restrict__ yields, const uint32_t* __restrict__ ymax, int64_t n,
                     int n_tiles, unsigned long long* __restrict__ tile_sum) {
-    __shared__ unsigned long long s_warp[33];
+    __shared__ unsigned long long s_warp[kScanThreads / 32];
     const int s = blockIdx.y;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
     const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
     const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
-    unsigned long long acc = 0;
+    uint32_t v[kScanPer];
+#pragma unroll
     for (int k = 0; k < kScanPer; k++) {
         const int64_t i = t0 + k * kScanThreads + threadIdx.x;
-        if (i < n) acc += cdf_quantize(row[i], base);
+        v[k] = i < n ? __ldg(row + i) : 0u;
     }
-    unsigned long long tot;
-    block_excl_scan_u64(acc, s_warp, &tot);
-    if (threadIdx.x == 0) tile_sum[static_cast<int64_t>(s) * n_tiles + blockIdx.x] = tot;
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) acc += cdf_quantize(v[k], base);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; w++) t += s_warp[w];
+        tile_sum[static_cast<int64_t>(s) * n_tiles + blockIdx.x] = t;
+    }
 }
 
 __global__ void __launch_bounds__(kScanThreads)
@@ -372,11 +394,11 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restric
                      int n_tiles, const unsigned long long* __restrict__ tile_off,
                      const unsigned long long* __restrict__ qtot, int guide_bits,
                      unsigned long long* __restrict__ cdf, int32_t* __restrict__ guide) {
-    // padded tile buffer: element e of the tile sits at (e / 16) * 17 + e % 16;
-    // it holds the FP32 yield bits on the way in and the CDF values on the way out
-    __shared__ unsigned long long s_buf[kScanThreads * (kScanPer + 1)];
+    // padded tile buffers: element e of the tile sits at (e / 8) * 9 + e % 8;
+    // s_in holds the FP32 yield bits, s_c the CDF values on the way out
+    __shared__ uint32_t s_in[kScanThreads * (kScanPer + 1)];
+    __shared__ unsigned long long s_c[kScanThreads * (kScanPer + 1)];
     __shared__ unsigned long long s_warp[33];
-    uint32_t* s_in = reinterpret_cast<uint32_t*>(s_buf);
     const int s = blockIdx.y;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
     const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
@@ -394,47 +416,55 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restric
     }
     __syncthreads();
     const uint32_t* mine = s_in + threadIdx.x * (kScanPer + 1);
-    unsigned long long q[kScanPer];
+    unsigned long long* mine_c = s_c + threadIdx.x * (kScanPer + 1);
     unsigned long long acc = 0;
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-        q[k] = cdf_quantize(mine[k], base);
-        acc += q[k];
+        const unsigned long long q = cdf_quantize(mine[k], base);
+        mine_c[k] = q;
+        acc += q;
     }
     unsigned long long tot;
-    // (its barriers also order the reads of s_in above before the writes below)
     const unsigned long long ex = block_excl_scan_u64(acc, s_warp, &tot);
     const unsigned long long start = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x] + ex;
     const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kScanPer;
+    // q -> exclusive prefix C, in place
     unsigned long long run = start;
-    unsigned long long* mine_out = s_buf + threadIdx.x * (kScanPer + 1);
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-        mine_out[k] = run;
-        run += q[k];
+        const unsigned long long q = mine_c[k];
+        mine_c[k] = run;
+        run += q;
     }
     __syncthreads();
-    // coalesced store of C[t0 .. t0 + 4096)
+    // coalesced store of C[t0 .. t0 + tile)
     for (int k = 0; k < kScanPer; k++) {
         const int e = k * kScanThreads + threadIdx.x;
         const int64_t i = t0 + e;
-        if (i < n) out[i] = s_buf[(e / kScanPer) * (kScanPer + 1) + e % kScanPer];
+        if (i < n) out[i] = s_c[(e / kScanPer) * (kScanPer + 1) + e % kScanPer];
     }
-    if (Q == 0 || e0 >= n || acc == 0) return;
-    // first bucket whose start lies at or after this thread's first cell:
-    // a float estimate of ceil(start * G / Q), then exact integer steps
+    if (Q == 0 || e0 >= n || run == start) return;
+    // Guide scatter.  Bucket j starts at f(j) = floor(j Q / G) = j qd + floor(j qr / G)
+    // with Q = qd G + qr; f is stepped exactly: f(j+1) = f(j) + qd + carry.
+    // First bucket at or after this thread's first cell: a float estimate of
+    // ceil(start G / Q), then exact steps.
     int64_t j = static_cast<int64_t>(static_cast<float>(start) *
                                      (static_cast<float>(G) / static_cast<float>(Q)));
     j = j < 0 ? 0 : (j > G ? G : j);
     while (j > 0 && bucket_start(static_cast<unsigned long long>(j - 1), g, Q) >= start) --j;
     while (j < G && bucket_start(static_cast<unsigned long long>(j), g, Q) < start) ++j;
-    unsigned long long hi = start;
+    const unsigned long long qd = Q >> g, qr = Q & static_cast<unsigned long long>(G - 1);
+    unsigned long long rem = (static_cast<unsigned long long>(j) * qr) & static_cast<unsigned long long>(G - 1);
+    unsigned long long f = j < G ? bucket_start(static_cast<unsigned long long>(j), g, Q) : Q;
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-        hi += q[k];
-        while (j < G && bucket_start(static_cast<unsigned long long>(j), g, Q) < hi) {
+        const unsigned long long hi = (k + 1 < kScanPer) ? mine_c[k + 1] : run;
+        while (j < G && f < hi) {
             gd[j] = static_cast<int32_t>(e0 + k);
             ++j;
+            rem += qr;
+            f += qd + (rem >> g);
+            rem &= static_cast<unsigned long long>(G - 1);
         }
     }
 }
@@ -445,27 +475,24 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restric
 // launch wrappers
 
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, uint32_t* ymax, cudaStream_t stream) {
-    if (cfg.n_species > 0) {
-        cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * cfg.n_species, stream);
-        if (e != cudaSuccess) return e;
-    }
+                          float* yields, cudaStream_t stream) {
     if (cfg.n_cells <= 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>((cfg.n_cells + kYieldThreads - 1) / kYieldThreads);
-    const size_t smem = (sizeof(SpeciesDev) + sizeof(uint32_t)) * static_cast<size_t>(cfg.n_species);
+    const size_t smem = sizeof(SpeciesDev) * static_cast<size_t>(cfg.n_species);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(yields_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    yields_kernel<<<blocks, kYieldThreads, smem, stream>>>(cfg, cells, sp, yields, ymax);
+    const unsigned groups = static_cast<unsigned>(cfg.n_species < kYieldGroups ? 1 : kYieldGroups);
+    yields_kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
     return cudaGetLastError();
 }
 
 int cdf_num_tiles(int64_t n) { return static_cast<int>((n + kScanTile - 1) / kScanTile); }
 
-cudaError_t launch_cdf(const float* yields, const uint32_t* ymax, int n_species, int64_t n,
+cudaError_t launch_cdf(const float* yields, uint32_t* ymax, int n_species, int64_t n,
                        unsigned long long* tile_sum, unsigned long long* tile_off,
                        unsigned long long* qtot, double* totals, unsigned long long* cdf,
                        int32_t* guide, cudaStream_t stream) {
@@ -473,6 +500,9 @@ cudaError_t launch_cdf(const float* yields, const uint32_t* ymax, int n_species,
     if (nt == 0 || n_species == 0) return cudaSuccess;
     const int g = cdf_guide_bits(n);
     dim3 grid(static_cast<unsigned>(nt), static_cast<unsigned>(n_species));
+    cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * n_species, stream);
+    if (e != cudaSuccess) return e;
+    cdf_tile_max_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, ymax);
     cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, ymax, n, nt, tile_sum);
     cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, ymax, nt, n, g, tile_off,
                                                                    qtot, totals, cdf, guide);

@@ -46,37 +46,113 @@ __device__ __forceinline__ uint4 block(uint32_t c0, uint32_t c1, uint32_t c2, ui
 // ------------------------------------------------------------------------
 // counts
 
+// Poisson draws: inversion for mu < 12, PTRS (Hoermann 1993) above.  The
+// FP64 expressions use explicitly rounded operations (__dmul_rn, __dadd_rn),
+// so no multiply-add is contracted and the CPU replay gets the same bits.
+struct PoissonC {
+    double mu, emu;                 // mu, exp(-mu)          (inversion)
+    double b, a, inv_alpha, vr;     // PTRS constants
+    double log_mu, log_ia;          // log(mu), log(inv_alpha)
+};
+static_assert(sizeof(PoissonC) == kPoissonConsts * sizeof(double), "PoissonC layout");
+
+// Inversion CDF of one species, cdf[0..len) as the inversion loop forms it,
+// stopped where adding the next term no longer changes it (then every later
+// term is smaller still); len = 0 when kInvTable entries do not reach that.
+struct PoissonInv {
+    double cdf[kInvTable];
+    int len;
+};
+static_assert(sizeof(PoissonInv) == (kInvTable + 1) * sizeof(double), "PoissonInv layout");
+
+__device__ PoissonC poisson_consts(double mu) {
+    PoissonC c{};
+    c.mu = mu;
+    if (mu < 12.0) {
+        c.emu = exp(-mu);
+        return c;
+    }
+    const double smu = sqrt(mu);
+    c.b = __dadd_rn(0.931, __dmul_rn(2.53, smu));
+    c.a = __dadd_rn(-0.059, __dmul_rn(0.02483, c.b));
+    c.inv_alpha = __dadd_rn(1.1239, 1.1328 / __dadd_rn(c.b, -3.4));
+    c.vr = __dadd_rn(0.9277, -(3.6224 / __dadd_rn(c.b, -2.0)));
+    c.log_mu = log(mu);
+    c.log_ia = log(c.inv_alpha);
+    return c;
+}
+
+// log(k!): the table for k < kLogFactLen, else the Stirling series of
+// lgamma(n), n = k + 1, to the n^-5 term (truncation below 1e-20 relative)
+__device__ __forceinline__ double log_factorial(const double* __restrict__ table, double kd) {
+    if (kd < static_cast<double>(kLogFactLen)) return table[static_cast<int>(kd)];
+    const double n = __dadd_rn(kd, 1.0);
+    const double r = 1.0 / n, r2 = __dmul_rn(r, r);
+    const double t = __dadd_rn(1.0 / 12.0,
+                               -__dmul_rn(r2, __dadd_rn(1.0 / 360.0, -__dmul_rn(r2, 1.0 / 1260.0))));
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(n, -0.5), log(n)), -n),
+                               0.91893853320467274178),
+                     __dmul_rn(r, t));
+}
+
+__device__ void poisson_inv_table(const PoissonC& c, PoissonInv& t) {
+    t.len = 0;
+    if (!(c.mu < 12.0)) return;
+    double p = c.emu, cdf = p;
+    t.cdf[0] = cdf;
+    for (int k = 1; k < kInvTable; k++) {
+        p = __dmul_rn(p, c.mu / static_cast<double>(k));
+        const double next = __dadd_rn(cdf, p);
+        if (next == cdf && static_cast<double>(k) > c.mu) {
+            t.len = k;
+            return;
+        }
+        cdf = next;
+        t.cdf[k] = cdf;
+    }
+}
+
 __device__ int64_t poisson_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t iter0,
-                                double mu) {
+                                const PoissonC& c, const double* __restrict__ logfact,
+                                const PoissonInv* __restrict__ inv = nullptr) {
+    const double mu = c.mu;
     if (mu < 12.0) {
         const uint4 w = block(iter0, 0u, c2, c3, k0, k1);
         const double u = u53(w.x, w.y);
-        double p = exp(-mu);
+        if (inv && inv->len > 0) {
+            // first k with u <= cdf[k]; past the saturated end the loop below
+            // would run to its cap
+            int lo = 0, hi = inv->len;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (u > inv->cdf[mid]) lo = mid + 1; else hi = mid;
+            }
+            return lo < inv->len ? lo : 1000;
+        }
+        double p = c.emu;
         double cdf = p;
         int64_t k = 0;
         while (u > cdf && k < 1000) {
             k++;
-            p *= mu / static_cast<double>(k);
-            cdf += p;
+            p = __dmul_rn(p, mu / static_cast<double>(k));
+            cdf = __dadd_rn(cdf, p);
         }
         return k;
     }
-    const double smu = sqrt(mu);
-    const double b = 0.931 + 2.53 * smu;
-    const double a = -0.059 + 0.02483 * b;
-    const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
-    const double vr = 0.9277 - 3.6224 / (b - 2.0);
-    const double log_mu = log(mu);
     for (uint32_t it = 0; it < 10000u; it++) {
         const uint4 w = block(iter0 + it, 0u, c2, c3, k0, k1);
-        const double U = u53(w.x, w.y) - 0.5;
+        const double U = __dadd_rn(u53(w.x, w.y), -0.5);
         const double V = u53(w.z, w.w);
-        const double us = 0.5 - fabs(U);
-        const double kd = floor((2.0 * a / us + b) * U + mu + 0.43);
-        if (us >= 0.07 && V <= vr) return static_cast<int64_t>(kd);
+        const double us = __dadd_rn(0.5, -fabs(U));
+        const double kd = floor(__dadd_rn(
+            __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(2.0, c.a) / us, c.b), U), mu), 0.43));
+        if (us >= 0.07 && V <= c.vr) return static_cast<int64_t>(kd);
         if (kd < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -mu + kd * log_mu - lgamma(kd + 1.0))
-            return static_cast<int64_t>(kd);
+        const double lhs =
+            __dadd_rn(__dadd_rn(log(V), c.log_ia), -log(__dadd_rn(c.a / __dmul_rn(us, us), c.b)));
+        const double rhs =
+            __dadd_rn(__dadd_rn(-mu, __dmul_rn(kd, c.log_mu)), -log_factorial(logfact, kd));
+        if (lhs <= rhs) return static_cast<int64_t>(kd);
     }
     return -1;
 }
@@ -130,9 +206,21 @@ __device__ __forceinline__ void item_decode(const DevConfig& cfg, int q, int& e,
     e = e0 + (r - s * ne);
 }
 
+// per-species Poisson constants of the model-30 draws (same mu in every event)
+__global__ void count_consts_kernel(DevConfig cfg, const double* __restrict__ totals,
+                                    PoissonC* __restrict__ pois, PoissonInv* __restrict__ inv) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cfg.n_species) return;
+    const double dN = __dmul_rn(totals[s], cfg.ymult);
+    const PoissonC c = poisson_consts(dN);
+    pois[s] = c;
+    poisson_inv_table(c, inv[s]);
+}
+
 __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
-                              int32_t* __restrict__ counts, int32_t* __restrict__ items,
-                              int* __restrict__ error) {
+                              const PoissonC* __restrict__ pois,
+                              const PoissonInv* __restrict__ inv, int32_t* __restrict__ counts,
+                              int32_t* __restrict__ items, int* __restrict__ error) {
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (idx >= total) return;
@@ -140,9 +228,9 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
     const int s = static_cast<int>(idx % cfg.n_species);
     const uint32_t c2 = cfg.event_offset + static_cast<uint32_t>(e);
     const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCount << 16);
-    const double dN = totals[s] * cfg.ymult;
+    const double dN = __dmul_rn(totals[s], cfg.ymult);
     const int64_t dN_int = static_cast<int64_t>(dN);
-    const double frac = dN - static_cast<double>(dN_int);
+    const double frac = __dadd_rn(dN, -static_cast<double>(dN_int));
     const double para1 = cfg.sampling_para1;
     int64_t nsamp = 0;
     if (dN < 0) {
@@ -151,18 +239,21 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
         const uint4 w = block(0u, 0u, c2, c3, cfg.key0, cfg.key1);
         nsamp = dN_int + (u53(w.x, w.y) < frac ? 1 : 0);
     } else if (cfg.sampling_model == 10 || cfg.sampling_model == 20) {
-        const double kk = (cfg.sampling_model == 10) ? para1 * frac : para1 * dN;
-        const double p = 1.0 / (1.0 + para1);
+        const double kk = (cfg.sampling_model == 10) ? __dmul_rn(para1, frac) : __dmul_rn(para1, dN);
+        const double p = 1.0 / __dadd_rn(1.0, para1);
         if (kk < 1e-15) {
             nsamp = dN_int;
         } else {
             const double g = gamma_draw(c2, c3, cfg.key0, cfg.key1, 0u, kk);
-            const int64_t nb = poisson_draw(c2, c3, cfg.key0, cfg.key1, 1u << 20, g * (1.0 - p) / p);
+            const PoissonC pc = poisson_consts(__dmul_rn(g, __dadd_rn(1.0, -p)) / p);
+            const int64_t nb = poisson_draw(c2, c3, cfg.key0, cfg.key1, 1u << 20, pc, cfg.tab.logfact);
             nsamp = (cfg.sampling_model == 10) ? dN_int + nb : nb;
             if (g < 0.0 || nb < 0) atomicCAS(error, 0, 3);
         }
     } else {
-        nsamp = (dN < 1e-15) ? 0 : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, dN);
+        nsamp = (dN < 1e-15) ? 0
+                             : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, pois[s], cfg.tab.logfact,
+                                            inv + s);
         if (nsamp < 0) atomicCAS(error, 0, 3);
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
@@ -295,7 +386,7 @@ struct Unit {
     int cell;
     int redraw;
     int tries_cell;
-    uint32_t t;
+    uint32_t t;                // tries made so far (proposal counter)
 };
 
 // Cell draw from 64 random bits r on the fixed-point CDF row C[0..n]
@@ -462,8 +553,8 @@ __device__ float compat_ratio(const Prop& p, float Et) {
 // One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
 // the uniform used for the rapidity of boost-invariant surfaces.
 __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, const Unit& u,
-                                         int s, float4& pl, float& u_rap, unsigned& violations) {
-    const uint32_t c3 = static_cast<uint32_t>(s) | (kTagTry << 16);
+                                         float4& pl, float& u_rap, unsigned& violations) {
+    const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagTry << 16);
     const uint4 A = block(2u * u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
     const float sel = u01f(A.x) * p.W;
     float prod = u01f_pos(A.y);
@@ -726,7 +817,7 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
             }
             float4 pl;
             float u_rap;
-            const bool ok = try_once(cfg, p, u, u.s, pl, u_rap, n_viol);
+            const bool ok = try_once(cfg, p, u, pl, u_rap, n_viol);
             u.t++;
             u.tries_cell++;
             n_tries++;
@@ -754,12 +845,15 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
 
 }  // namespace
 
-cudaError_t launch_counts(const DevConfig& cfg, const double* totals, int32_t* counts,
+cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* pois, int32_t* counts,
                           int32_t* items, int* error, cudaStream_t stream) {
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (total <= 0) return cudaSuccess;
+    PoissonC* pc = reinterpret_cast<PoissonC*>(pois);
+    PoissonInv* inv = reinterpret_cast<PoissonInv*>(pc + cfg.n_species);
+    count_consts_kernel<<<(cfg.n_species + 127) / 128, 128, 0, stream>>>(cfg, totals, pc, inv);
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
-    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, counts, items, error);
+    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, pc, inv, counts, items, error);
     return cudaGetLastError();
 }
 

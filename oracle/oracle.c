@@ -504,6 +504,22 @@ static void orc_block(orc_block_stream* s, uint32_t iter, uint32_t w[4]) {
     orc_philox4x32_10(ctr, s->key, w);
 }
 
+/* log(k!): lgamma(k + 1) for k < 256, else the Stirling series of
+ * lgamma(n), n = k + 1, to the n^-5 term (truncation below 1e-20 relative). */
+static double orc_logfact(double kd) {
+    static double table[256];
+    static int ready = 0;
+    if (!ready) {
+        for (int i = 0; i < 256; i++) table[i] = lgamma(i + 1.0);
+        ready = 1;
+    }
+    if (kd < 256.0) return table[(int)kd];
+    const double n = kd + 1.0;
+    const double r = 1.0 / n, r2 = r * r;
+    return (n - 0.5) * log(n) - n + 0.91893853320467274178 +
+           r * (1.0 / 12.0 - r2 * (1.0 / 360.0 - r2 * (1.0 / 1260.0)));
+}
+
 static int64_t orc_poisson(orc_block_stream* s, uint32_t iter0, double mu) {
     uint32_t w[4];
     if (mu < 12.0) {
@@ -533,7 +549,7 @@ static int64_t orc_poisson(orc_block_stream* s, uint32_t iter0, double mu) {
         const double kd = floor((2.0 * a / us + b) * U + mu + 0.43);
         if (us >= 0.07 && V <= vr) return (int64_t)kd;
         if (kd < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -mu + kd * log_mu - lgamma(kd + 1.0))
+        if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -mu + kd * log_mu - orc_logfact(kd))
             return (int64_t)kd;
     }
     return -1;
