@@ -271,9 +271,9 @@ def run_gpu(args, ws, rank, local):
     e2e = None
     if not args.no_e2e:
         n_h = max(hadrons)
-        out = torch.empty((int(n_h * 1.2) + 1024) * 40, dtype=torch.uint8).pin_memory().numpy()
+        out_t = torch.empty((int(n_h * 1.2) + 1024) * 40, dtype=torch.uint8).pin_memory()
         from iss_gb300 import HADRON_DTYPE
-        out = out.view(HADRON_DTYPE)
+        out = out_t.numpy().view(HADRON_DTYPE)
         e_had, e_bytes_in, e_bytes_out = 0, 0, 0
         parts = [0.0, 0.0]   # set_surface, generate_into (host clock)
         torch.cuda.synchronize()
@@ -293,8 +293,20 @@ def run_gpu(args, ws, rank, local):
         torch.cuda.synchronize()
         barrier()
         e_sec = time.perf_counter() - t0
+        # the device->host link alone: one step's record bytes in one copy
+        nbytes = e_bytes_out // args.steps
+        dev_buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        link = []
+        for _ in range(3):
+            ev0.record()
+            out_t[:nbytes].copy_(dev_buf, non_blocking=True)
+            ev1.record()
+            ev1.synchronize()
+            link.append(nbytes / (ev0.elapsed_time(ev1) * 1e-3) / 1e9)
+        del dev_buf
         e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps,
-               [1e3 * x / args.steps for x in parts]]
+               [1e3 * x / args.steps for x in parts], max(link)]
 
     sec = sum(dev_ms) / 1e3
     local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
@@ -352,7 +364,8 @@ def run_gpu(args, ws, rank, local):
                 "e2e": ({"value": e2e_h / e2e_sec, "unit": UNIT,
                          "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3],
                          "host_ms_per_step": {"set_surface": e2e[4][0],
-                                              "generate_into": e2e[4][1]}}
+                                              "generate_into": e2e[4][1]},
+                         "d2h_link_gbs": e2e[5]}
                         if e2e else None),
                 "gpu_launches": launches, "clocks": clk,
                 "hadrons_per_step": nh / args.steps,
