@@ -50,6 +50,36 @@ PARAMS = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1, include_
               bulk_deltaf_kind=11, turn_on_bulk=1, quantum_statistics=1,
               dN_dy_sampling_model=30, number_of_repeated_sampling=N_EVENTS)
 ALG_BYTES_PER_HADRON = 40 + 96 + 4     # record write + LRF cell gather + slot/index
+
+# the other configurations of the benchmark set, for --workload (the default
+# line is always the viscous one above)
+WORKLOADS = {
+    "viscous": dict(cells=N_CELLS, events=N_EVENTS, species=319, params=PARAMS,
+                    data="synthetic (iss_gb300.surfaces.viscous_3d, seed 2)"),
+    # ideal fluid, boost-invariant, r < 10 fm on a 0.5 fm grid, T = 0.150 GeV
+    "ideal": dict(cells=1245, events=100, species=319,
+                  params=dict(hydro_mode=1, afterburner_type=0, include_deltaf_shear=0,
+                              include_deltaf_bulk=0, quantum_statistics=1,
+                              dN_dy_sampling_model=30),
+                  data="synthetic (iss_gb300.surfaces.ideal_boost_invariant)"),
+    # finite baryon density with diffusion, SMASH species, 1M cells
+    "finite_density": dict(cells=1_000_000, events=2000, species=400,
+                           params=dict(hydro_mode=2, afterburner_type=2, include_deltaf_shear=1,
+                                       include_deltaf_bulk=1, bulk_deltaf_kind=11,
+                                       turn_on_bulk=1, include_deltaf_diffusion=1, turn_on_rhob=1,
+                                       turn_on_diff=1, quantum_statistics=1,
+                                       dN_dy_sampling_model=30),
+                           data="synthetic (iss_gb300.surfaces.finite_density_3d, seed 3)"),
+}
+
+
+def make_surface(workload: str, cells: int):
+    from iss_gb300 import surfaces as S
+    if workload == "ideal":
+        return S.ideal_boost_invariant()
+    if workload == "finite_density":
+        return S.finite_density_3d(cells, seed=3)
+    return S.viscous_3d(cells, seed=SEED_SURFACE)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -218,10 +248,11 @@ def run_gpu(args, ws, rank, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from iss_gb300 import iSS, surfaces as S
 
-    surf = S.viscous_3d(args.cells, seed=SEED_SURFACE)
+    wl = WORKLOADS[args.workload]
+    surf = make_surface(args.workload, args.cells)
     fo = surf.fo_surf()
     n_events = args.events
-    params = dict(S.DEFAULT_PARAMETERS, **PARAMS)
+    params = dict(S.DEFAULT_PARAMETERS, **wl["params"])
     params["number_of_repeated_sampling"] = n_events
     params["gpu_event_offset"] = rank * n_events
     s = iSS(".", inputfile="")
@@ -342,7 +373,7 @@ def run_gpu(args, ws, rank, local):
                     "kernel_ms_per_launch": 1e3 * samp_sec / args.steps,
                     "yields_kernel_ms_per_launch": 1e3 * local_stats[3] / args.steps}
         cpu = None
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and args.workload == "viscous":
             h_cpu, t_cpu = cpu_baseline(1, args.cpu_cells, N_EVENTS, seed=7)
             cpu = {"value": h_cpu / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
                    "sample": f"viscous 3+1D surface, every {N_CELLS // args.cpu_cells}th cell "
@@ -352,11 +383,16 @@ def run_gpu(args, ws, rank, local):
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * max_sec / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (iss_gb300.surfaces.viscous_3d, seed 2)",
-                "config": {"workload": f"viscous_3d_{args.cells // 1000}k_cells_s95p_"
-                                       f"{n_events}_events",
-                           "cells": args.cells, "events_per_gpu": n_events, "species": 319,
-                           "bulk_deltaf_kind": 11, "sampler": "plain",
+                "data": wl["data"],
+                "config": {"workload": (f"viscous_3d_{args.cells // 1000}k_cells_s95p_"
+                                        f"{n_events}_events" if args.workload == "viscous" else
+                                        f"{args.workload}_{surf.records.shape[0]}_cells_"
+                                        f"{n_events}_events"),
+                           "cells": int(surf.records.shape[0]), "events_per_gpu": n_events,
+                           "species": wl["species"],
+                           "delta_f": {k: v for k, v in wl["params"].items()
+                                       if k.startswith("include_") or k == "bulk_deltaf_kind"},
+                           "sampler": "plain",
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
                            "wall_s_timed": wall},
@@ -383,13 +419,19 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--events", type=int, default=N_EVENTS)
-    ap.add_argument("--cells", type=int, default=N_CELLS,
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="viscous")
+    ap.add_argument("--events", type=int, default=None)
+    ap.add_argument("--cells", type=int, default=None,
                     help="surface size (profiling runs use a smaller surface)")
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.cells is None:
+        args.cells = wl["cells"]
+    if args.events is None:
+        args.events = wl["events"]
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
