@@ -62,6 +62,10 @@ WORKLOADS = {
                               include_deltaf_bulk=0, quantum_statistics=1,
                               dN_dy_sampling_model=30),
                   data="synthetic (iss_gb300.surfaces.ideal_boost_invariant)"),
+    # 256 independent viscous surfaces sampled by one generate: cells
+    # log-uniform in [5k, 400k], events log-uniform in [10, 2000] (seeds 100..)
+    "batched": dict(cells=None, events=None, species=319, params=PARAMS,
+                    data="synthetic (iss_gb300.surfaces.viscous_3d, seeds 100.., sizes from seed 0)"),
     # finite baryon density with diffusion, SMASH species, 1M cells
     "finite_density": dict(cells=1_000_000, events=2000, species=400,
                            params=dict(hydro_mode=2, afterburner_type=2, include_deltaf_shear=1,
@@ -71,6 +75,13 @@ WORKLOADS = {
                                        dN_dy_sampling_model=30),
                            data="synthetic (iss_gb300.surfaces.finite_density_3d, seed 3)"),
 }
+
+
+def batch_sizes(n_surfaces: int):
+    rng = np.random.default_rng(0)
+    cells = np.exp(rng.uniform(np.log(5e3), np.log(4e5), n_surfaces)).astype(np.int64)
+    events = np.exp(rng.uniform(np.log(10), np.log(2000), n_surfaces)).astype(np.int32)
+    return cells, events
 
 
 def make_surface(workload: str, cells: int):
@@ -249,17 +260,30 @@ def run_gpu(args, ws, rank, local):
     from iss_gb300 import iSS, surfaces as S
 
     wl = WORKLOADS[args.workload]
-    surf = make_surface(args.workload, args.cells)
-    fo = surf.fo_surf()
-    n_events = args.events
+    batch = None
+    if args.workload == "batched":
+        b_cells, b_events = batch_sizes(args.surfaces)
+        batch = [S.viscous_3d(int(c), seed=100 + i).fo_surf() for i, c in enumerate(b_cells)]
+        total_cells = int(b_cells.sum())
+        fo = None
+        n_events = int(b_events.sum())
+        args.no_e2e = True      # the records of a batch (~1e2 GB) stay on the device
+    else:
+        surf = make_surface(args.workload, args.cells)
+        fo = surf.fo_surf()
+        total_cells = int(fo.shape[0])
+        n_events = args.events
     params = dict(S.DEFAULT_PARAMETERS, **wl["params"])
     params["number_of_repeated_sampling"] = n_events
     params["gpu_event_offset"] = rank * n_events
     s = iSS(".", inputfile="")
     s.set_params(**params)
-    # pinned host buffers for the end-to-end leg
-    fo_pinned = torch.from_numpy(fo).pin_memory().numpy()
-    s.set_surface(fo_pinned)
+    if batch is not None:
+        s.set_surface_batch(batch, b_events)
+    else:
+        # pinned host buffers for the end-to-end leg
+        fo_pinned = torch.from_numpy(fo).pin_memory().numpy()
+        s.set_surface(fo_pinned)
     s.set_random_seed(20261203)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -386,9 +410,10 @@ def run_gpu(args, ws, rank, local):
                 "data": wl["data"],
                 "config": {"workload": (f"viscous_3d_{args.cells // 1000}k_cells_s95p_"
                                         f"{n_events}_events" if args.workload == "viscous" else
-                                        f"{args.workload}_{surf.records.shape[0]}_cells_"
-                                        f"{n_events}_events"),
-                           "cells": int(surf.records.shape[0]), "events_per_gpu": n_events,
+                                        f"{args.workload}_{total_cells}_cells_"
+                                        f"{n_events}_events" + (f"_{args.surfaces}_surfaces"
+                                                                if batch is not None else "")),
+                           "cells": total_cells, "events_per_gpu": n_events,
                            "species": wl["species"],
                            "delta_f": {k: v for k, v in wl["params"].items()
                                        if k.startswith("include_") or k == "bulk_deltaf_kind"},
@@ -423,15 +448,16 @@ def main():
     ap.add_argument("--events", type=int, default=None)
     ap.add_argument("--cells", type=int, default=None,
                     help="surface size (profiling runs use a smaller surface)")
+    ap.add_argument("--surfaces", type=int, default=256, help="surfaces of --workload batched")
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.cells is None:
-        args.cells = wl["cells"]
+        args.cells = wl["cells"] or 0
     if args.events is None:
-        args.events = wl["events"]
+        args.events = wl["events"] or 0
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -126,6 +126,27 @@ iss_status iss_gpu_read_surface(iss_handle* h);
 iss_status iss_gpu_set_surface(iss_handle* h, const float* fo_surf_records,
                                int64_t n_cells);
 
+/* A batch of independent surfaces sampled by one iss_gpu_generate (no
+ * counterpart in the reference, which holds one surface per iSS object).
+ *   - Surface b has the FO_surf records
+ *     [cell_offsets[b], cell_offsets[b+1]) of `fo_surf_records`.
+ *   - cell_offsets[0] = 0, n_surfaces + 1 entries.
+ *   - Surface b gets events[b] events, which replaces
+ *     number_of_repeated_sampling.
+ *   - Events are numbered across the batch: surface 0's events come first,
+ *     then surface 1's, and so on. iss_gpu_num_events returns the sum.
+ *   - Every kernel runs once over the whole batch.
+ *   - Surface b's events are bit-identical to a single-surface run of b with
+ *     the same seed and gpu_event_offset raised by the events of surfaces
+ *     0 .. b-1.
+ *   - iss_gpu_species_yields then returns n_surfaces * n_species values,
+ *     row b * n_species + k.
+ *   - Fewer than 2^31 cells and events in total.
+ *   - iss_gpu_set_surface or iss_gpu_read_surface ends batch mode. */
+iss_status iss_gpu_set_surface_batch(iss_handle* h, const float* fo_surf_records,
+                                     const int64_t* cell_offsets, const int32_t* events,
+                                     int32_t n_surfaces);
+
 /* iSS::generate_samples (src/iSS.cpp:130-165) for MC_sampling = 4, i.e.
  * FSSW::shell (src/FSSW.cpp:344-361) without the optional decays and
  * spectators: yields, counts, momenta and the hadron lists, all on the GPU. */

@@ -75,6 +75,12 @@ struct iss_handle {
     // surface (host)
     std::vector<float> fo34;
     int64_t n_cells = 0;
+    // a batch of surfaces (iss_gpu_set_surface_batch); empty for one surface
+    std::vector<int64_t> batch_cells;     // cell offsets, n_surfaces + 1
+    std::vector<int32_t> batch_events;    // events per surface
+    std::vector<SurfSeg> segs;            // per-surface layout of the CDF rows
+    std::vector<int32_t> ev_surf;         // surface of every event (host copy of d_ev_surf)
+    int64_t cdf_len = 0, guide_len = 0, n_tiles = 0;
     int hydro_mode = 2;
     int iEOS = 2;
     int afterburner = 0;
@@ -102,7 +108,8 @@ struct iss_handle {
     DevBuf<unsigned long long> d_cdf, d_tile_sum, d_tile_off, d_qtot;
     DevBuf<double> d_totals;
     DevBuf<uint32_t> d_ymax;
-    DevBuf<int32_t> d_counts, d_items, d_item_seg, d_guide, d_cell_of;
+    DevBuf<int32_t> d_counts, d_items, d_item_seg, d_guide, d_cell_of, d_ev_surf;
+    DevBuf<SurfSeg> d_surf;
     DevBuf<int64_t> d_offsets, d_off_tiles, d_item_off;
     DevBuf<HadronRec> d_hadrons;
     DevBuf<unsigned long long> d_work;
@@ -145,6 +152,8 @@ struct iss_handle {
             d_item_seg.release();
             d_guide.release();
             d_cell_of.release();
+            d_ev_surf.release();
+            d_surf.release();
             d_offsets.release();
             d_off_tiles.release();
             d_item_off.release();
@@ -278,6 +287,49 @@ iss_status prepare(iss_handle* h) {
     c.key1 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed) >> 32);
     c.n_species = static_cast<int>(h->species.size());
     c.n_cells = h->n_cells;
+    // surfaces of the batch and the layout of their CDF rows
+    {
+        std::vector<int64_t> cells = h->batch_cells;
+        std::vector<int32_t> events = h->batch_events;
+        if (cells.empty()) {
+            cells = {0, h->n_cells};
+            events = {c.n_events};
+        } else if (h->params.get_or("sample_upto_desired_particle_number", 0) == 1) {
+            return fail(h, ISS_ERR_UNSUPPORTED,
+                        "sample_upto_desired_particle_number with a batch of surfaces");
+        }
+        const int B = static_cast<int>(events.size());
+        const int S = c.n_species;
+        h->segs.assign(static_cast<size_t>(B), SurfSeg{});
+        int64_t cdf = 0, guide = 0, tiles = 0;
+        int e0 = 0;
+        for (int b = 0; b < B; b++) {
+            SurfSeg& g = h->segs[b];
+            g.c0 = cells[b];
+            g.n = cells[b + 1] - cells[b];
+            g.L = cdf_log2_cells(g.n);
+            g.g = cdf_guide_bits(g.n);
+            g.nt = cdf_num_tiles(g.n);
+            g.cdf_base = cdf;
+            g.guide_base = guide;
+            g.tile_base = tiles;
+            g.e0 = e0;
+            g.ne = events[b];
+            cdf += static_cast<int64_t>(S) * (g.n + 1);
+            guide += static_cast<int64_t>(S) * ((int64_t(1) << g.g) + 1);
+            tiles += static_cast<int64_t>(S) * g.nt;
+            e0 += events[b];
+        }
+        h->cdf_len = cdf;
+        h->guide_len = guide;
+        h->n_tiles = tiles;
+        c.n_surfaces = B;
+        c.n_events = e0;
+        CUDA_TRY(h, h->d_surf.reserve(static_cast<size_t>(B)));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_surf.ptr, h->segs.data(), sizeof(SurfSeg) * B,
+                                    cudaMemcpyHostToDevice, h->stream));
+        c.surf = h->d_surf.ptr;
+    }
     const int fix_c0 = static_cast<int>(h->params.get_or("gpu_fix_14mom_c0", 0)) != 0;
 
     // tables
@@ -410,23 +462,23 @@ iss_status run_cells(iss_handle* h) {
     }
     CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 8));
     CUDA_TRY(h, h->d_yields.reserve(static_cast<size_t>(n) * S));
-    CUDA_TRY(h, h->d_cdf.reserve(static_cast<size_t>(n + 1) * S));
-    const int nt = cdf_num_tiles(n);
-    CUDA_TRY(h, h->d_tile_sum.reserve(static_cast<size_t>(nt) * S));
-    CUDA_TRY(h, h->d_tile_off.reserve(static_cast<size_t>(nt) * S));
-    CUDA_TRY(h, h->d_totals.reserve(static_cast<size_t>(S)));
-    CUDA_TRY(h, h->d_qtot.reserve(static_cast<size_t>(S)));
-    CUDA_TRY(h, h->d_ymax.reserve(static_cast<size_t>(S)));
-    CUDA_TRY(h, h->d_guide.reserve(((size_t(1) << cdf_guide_bits(n)) + 1) * S));
+    const size_t rows = static_cast<size_t>(c.n_surfaces) * S;
+    CUDA_TRY(h, h->d_cdf.reserve(static_cast<size_t>(std::max<int64_t>(h->cdf_len, 1))));
+    CUDA_TRY(h, h->d_tile_sum.reserve(static_cast<size_t>(std::max<int64_t>(h->n_tiles, 1))));
+    CUDA_TRY(h, h->d_tile_off.reserve(static_cast<size_t>(std::max<int64_t>(h->n_tiles, 1))));
+    CUDA_TRY(h, h->d_totals.reserve(rows));
+    CUDA_TRY(h, h->d_qtot.reserve(rows));
+    CUDA_TRY(h, h->d_ymax.reserve(rows));
+    CUDA_TRY(h, h->d_guide.reserve(static_cast<size_t>(std::max<int64_t>(h->guide_len, 1))));
     const CellArrays cells = cell_arrays(h);
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
     CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvPrologue], st));
     CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
-    CUDA_TRY(h, launch_cdf(h->d_yields.ptr, h->d_ymax.ptr, S, n, h->d_tile_sum.ptr,
-                           h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
-                           h->d_guide.ptr, st));
+    CUDA_TRY(h, launch_cdf(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S,
+                           h->d_ymax.ptr, h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr,
+                           h->d_totals.ptr, h->d_cdf.ptr, h->d_guide.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCdf], st));
     h->yields_valid = true;
     return ISS_OK;
@@ -477,6 +529,18 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
         if (c.hydro_mode == 2) nev *= 10;
         nev = std::max(1, std::min(static_cast<int>(max_ev), nev));
         c.n_events = nev;
+        h->segs[0].ne = nev;
+    }
+    // surface of every event
+    {
+        std::vector<int32_t>& ev_surf = h->ev_surf;
+        ev_surf.assign(static_cast<size_t>(std::max(c.n_events, 1)), 0);
+        for (int b = 0; b < c.n_surfaces; b++)
+            for (int e = 0; e < h->segs[b].ne; e++) ev_surf[h->segs[b].e0 + e] = b;
+        CUDA_TRY(h, h->d_ev_surf.reserve(ev_surf.size()));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_ev_surf.ptr, ev_surf.data(), 4 * ev_surf.size(),
+                                    cudaMemcpyHostToDevice, s));
+        c.ev_surf = h->d_ev_surf.ptr;
     }
 
     const int64_t nseg = static_cast<int64_t>(c.n_events) * S;
@@ -496,7 +560,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
     // per species: kPoissonConsts constants, then an inversion table of
     // kInvTable + 1 doubles (the last holds the length)
-    CUDA_TRY(h, h->d_pois.reserve(static_cast<size_t>(std::max(S, 1)) *
+    CUDA_TRY(h, h->d_pois.reserve(static_cast<size_t>(std::max(S * c.n_surfaces, 1)) *
                                   (kPoissonConsts + kInvTable + 1)));
     CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr, h->d_items.ptr,
                               h->d_error.ptr, s));
@@ -548,7 +612,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
     for (int ch = 0; ch < n_chunks; ch++) {
         CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
-                                   h->d_guide.ptr, cdf_guide_bits(h->n_cells), h->d_qtot.ptr,
+                                   h->d_guide.ptr, h->d_qtot.ptr,
                                    h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr,
                                    chunk_item[ch], chunk_item[ch + 1], h->d_cell_of.ptr,
                                    h->d_hadrons.ptr, h->d_work.ptr + ch, h->d_counters.ptr,
@@ -704,6 +768,8 @@ iss_status iss_gpu_set_seed_from_params(iss_handle* h) {
 
 iss_status iss_gpu_read_surface(iss_handle* h) {
     if (!h) return ISS_ERR_INVALID_ARG;
+    h->batch_cells.clear();
+    h->batch_events.clear();
     double mode, qs;
     if (!need(h, "hydro_mode", &mode) || !need(h, "quantum_statistics", &qs))
         return ISS_ERR_PARAM_MISSING;
@@ -750,6 +816,8 @@ iss_status iss_gpu_set_surface(iss_handle* h, const float* records, int64_t n_ce
         if (st != ISS_OK) return st;
     }
     if (n_cells == 0) return fail(h, ISS_ERR_NO_SURFACE, "no freeze-out fluid cell");
+    h->batch_cells.clear();
+    h->batch_events.clear();
     // With a device, the records go straight from the caller's buffer (pinned
     // or pageable) to HBM; without one a host copy is kept for inspection.
     if (ensure_cuda(h) == ISS_OK) {
@@ -770,6 +838,30 @@ iss_status iss_gpu_set_surface(iss_handle* h, const float* records, int64_t n_ce
     h->last_error.clear();
     h->fo34.assign(records, records + static_cast<size_t>(n_cells) * kFoSurfFloats);
     return finish_surface(h);
+}
+
+iss_status iss_gpu_set_surface_batch(iss_handle* h, const float* records,
+                                     const int64_t* cell_offsets, const int32_t* events,
+                                     int32_t n_surfaces) {
+    if (!h || !records || !cell_offsets || !events || n_surfaces <= 0)
+        return ISS_ERR_INVALID_ARG;
+    if (cell_offsets[0] != 0) return fail(h, ISS_ERR_INVALID_ARG, "cell_offsets[0] must be 0");
+    int64_t total_events = 0;
+    for (int32_t b = 0; b < n_surfaces; b++) {
+        if (cell_offsets[b + 1] <= cell_offsets[b])
+            return fail(h, ISS_ERR_NO_SURFACE, "surface %d of the batch has no cell", b);
+        if (events[b] < 0) return fail(h, ISS_ERR_INVALID_ARG, "surface %d: negative events", b);
+        total_events += events[b];
+    }
+    if (cell_offsets[n_surfaces] >= (int64_t(1) << 31))
+        return fail(h, ISS_ERR_INVALID_ARG, "a batch holds fewer than 2^31 cells");
+    if (total_events >= (int64_t(1) << 31))
+        return fail(h, ISS_ERR_INVALID_ARG, "a batch holds fewer than 2^31 events");
+    iss_status st = iss_gpu_set_surface(h, records, cell_offsets[n_surfaces]);
+    if (st != ISS_OK) return st;
+    h->batch_cells.assign(cell_offsets, cell_offsets + n_surfaces + 1);
+    h->batch_events.assign(events, events + n_surfaces);
+    return ISS_OK;
 }
 
 iss_status iss_gpu_generate(iss_handle* h) {
@@ -930,8 +1022,8 @@ iss_status iss_gpu_species(iss_handle* h, int32_t* n_species, int32_t* pids, int
 iss_status iss_gpu_species_yields(iss_handle* h, double* dn_dy, int32_t capacity) {
     if (!h || !dn_dy) return ISS_ERR_INVALID_ARG;
     if (!h->yields_valid) return fail(h, ISS_ERR_NO_SAMPLES, "no yields: call iss_gpu_generate first");
-    const int32_t n = static_cast<int32_t>(h->species.size());
-    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "%d species", n);
+    const int32_t n = static_cast<int32_t>(h->species.size()) * h->cfg.n_surfaces;
+    if (capacity < n) return fail(h, ISS_ERR_CAPACITY, "%d (surface, species) rows", n);
     CUDA_TRY(h, cudaMemcpy(dn_dy, h->d_totals.ptr, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
     return ISS_OK;
 }

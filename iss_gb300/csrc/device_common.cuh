@@ -28,6 +28,18 @@ constexpr int kLogFactLen = 256;
 constexpr int kPoissonConsts = 8;   // doubles per species, see poisson_consts
 constexpr int kInvTable = 127;      // inversion CDF entries per species (+ length: 128 doubles)
 
+// One surface of a batch.  The cells of all surfaces are concatenated; the
+// per-(surface, species) rows of the cell CDF and of the guide tables are
+// laid out surface by surface, species by species.
+struct SurfSeg {
+    int64_t c0, n;            // first cell, number of cells
+    int64_t cdf_base;         // row (b, k) of the CDF starts at cdf_base + k (n + 1)
+    int64_t guide_base;       // row (b, k) of the guide starts at guide_base + k (2^g + 1)
+    int64_t tile_base;        // first flattened scan tile of the surface (S nt tiles)
+    int nt, L, g;             // tiles per row, ceil(log2 n), guide bits
+    int e0, ne;               // first event (batch numbering) and number of events
+};
+
 struct DevConfig {
     int hydro_mode;
     int include_shear, include_bulk, include_diff;
@@ -44,6 +56,9 @@ struct DevConfig {
     uint32_t event_offset;
     int max_tries, max_redraws;
     int chunk_events;        // events per sampling chunk (work-item order, see item_index)
+    int n_surfaces;          // surfaces in the batch (1 for a single surface)
+    const SurfSeg* surf;     // [n_surfaces]
+    const int32_t* ev_surf;  // [n_events] surface of each event
     DevTables tab;
 };
 
@@ -112,10 +127,11 @@ ISS_HD inline int cdf_log2_cells(int64_t n) {
     return L;
 }
 
-// 2^g guide buckets per species, g = clamp(ceil(log2 n), 1, 24)
+// 2^g guide buckets per row, g = clamp(ceil(log2 n) - 1, 1, 24): between n/2
+// and n buckets, so a bucket spans one or two cells on average
 ISS_HD inline int cdf_guide_bits(int64_t n) {
-    const int L = cdf_log2_cells(n);
-    return L < 1 ? 1 : (L > 24 ? 24 : L);
+    const int g = cdf_log2_cells(n) - 1;
+    return g < 1 ? 1 : (g > 24 ? 24 : g);
 }
 
 // q(y) = mantissa(y) * 2^(exponent(y) + base) with base = 38 - L - e_max,

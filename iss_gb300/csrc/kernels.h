@@ -14,18 +14,21 @@ cudaError_t launch_cell_prologue(const DevConfig& cfg, const float* fo34, int64_
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
                           float* yields, cudaStream_t stream);
 int cdf_num_tiles(int64_t n);
-// fixed-point cell CDF (cdf_quantize), four launches (species maxima ymax,
-// tile sums, tile offsets, scan): row s holds n + 1 entries C[0..n],
-// the guide table 2^g + 1 entries per species, g = cdf_guide_bits(n)
-cudaError_t launch_cdf(const float* yields, uint32_t* ymax, int n_species, int64_t n,
-                       unsigned long long* tile_sum, unsigned long long* tile_off,
-                       unsigned long long* qtot, double* totals, unsigned long long* cdf,
-                       int32_t* guide, cudaStream_t stream);
+// Fixed-point cell CDF (cdf_quantize) of every (surface, species) row of a
+// batch; four launches over n_tiles = sum over surfaces of S * nt tiles
+// (row maxima, tile sums, tile offsets, scan).  Row (b, k) of the CDF holds
+// n_b + 1 entries C[0..n_b] at surf[b].cdf_base + k (n_b + 1); its guide
+// table 2^g_b + 1 entries at surf[b].guide_base + k (2^g_b + 1).  ymax,
+// qtot and totals hold n_surf * S rows.  surf is a device array.
+cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                       int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
+                       unsigned long long* tile_off, unsigned long long* qtot, double* totals,
+                       unsigned long long* cdf, int32_t* guide, cudaStream_t stream);
 
 // kernels_sample.cu
-// two launches: per-species Poisson constants and inversion tables (pois,
-// (kPoissonConsts + kInvTable + 1) doubles per species), then one count per
-// (event, species)
+// two launches: Poisson constants and inversion tables of every (surface,
+// species) row (pois, (kPoissonConsts + kInvTable + 1) doubles per row), then
+// one count per (event, species); totals has n_surfaces * S rows
 cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* pois, int32_t* counts,
                           int32_t* items, int* error, cudaStream_t stream);
 int offsets_num_tiles(int64_t n);
@@ -38,7 +41,7 @@ cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64
 // be zero
 cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
                            const int32_t* pids, const unsigned long long* cdf,
-                           const int32_t* guide, int guide_bits, const unsigned long long* qtot,
+                           const int32_t* guide, const unsigned long long* qtot,
                            const int64_t* offsets,
                            const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
                            int64_t k_end, int32_t* cell_of, HadronRec* out,

@@ -302,13 +302,42 @@ __device__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned
     return out;
 }
 
-// per-species maximum yield, as float bits (the yields are >= +0, so the
+// Scan tiles are numbered over all rows (b, k) of the batch: surface b owns
+// tiles [tile_base, tile_base + S nt) -- species k's row is its k-th run of
+// nt tiles.  A block finds its surface by binary search over tile_base.
+struct TileRef {
+    const SurfSeg* sg;
+    int b, k;
+    int64_t tile;             // tile index inside the row
+};
+
+__device__ __forceinline__ TileRef tile_ref(const SurfSeg* __restrict__ surf, int n_surf, int S,
+                                            int64_t t) {
+    int lo = 0, hi = n_surf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (surf[mid].tile_base <= t) lo = mid; else hi = mid - 1;
+    }
+    TileRef r;
+    r.sg = surf + lo;
+    r.b = lo;
+    const int64_t local = t - r.sg->tile_base;
+    r.k = static_cast<int>(local / r.sg->nt);
+    r.tile = local - static_cast<int64_t>(r.k) * r.sg->nt;
+    if (r.k >= S) r.k = S - 1;   // not reached: the grid has exactly the batch's tiles
+    return r;
+}
+
+// maximum yield of every row, as float bits (the yields are >= +0, so the
 // unsigned order of the bits is the order of the values); ymax starts at 0
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_max_kernel(const float* __restrict__ yields, int64_t n, uint32_t* __restrict__ ymax) {
-    const int s = blockIdx.y;
-    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
+cdf_tile_max_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg* __restrict__ surf,
+                    int n_surf, int S, uint32_t* __restrict__ ymax) {
+    const TileRef tr = tile_ref(surf, n_surf, S, blockIdx.x);
+    const int64_t n = tr.sg->n;
+    const int64_t t0 = tr.tile * kScanTile;
+    const uint32_t* row =
+        reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(tr.k) * N + tr.sg->c0);
     uint32_t v[kScanPer];
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
@@ -319,17 +348,20 @@ cdf_tile_max_kernel(const float* __restrict__ yields, int64_t n, uint32_t* __res
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) m = max(m, v[k]);
     m = __reduce_max_sync(0xffffffffu, m);
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(ymax + s, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(ymax + tr.b * S + tr.k, m);
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_sum_kernel(const float* __restrict__ yields, const uint32_t* __restrict__ ymax, int64_t n,
-                    int n_tiles, unsigned long long* __restrict__ tile_sum) {
+cdf_tile_sum_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg* __restrict__ surf,
+                    int n_surf, int S, const uint32_t* __restrict__ ymax,
+                    unsigned long long* __restrict__ tile_sum) {
     __shared__ unsigned long long s_warp[kScanThreads / 32];
-    const int s = blockIdx.y;
-    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
-    const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
+    const TileRef tr = tile_ref(surf, n_surf, S, blockIdx.x);
+    const int64_t n = tr.sg->n;
+    const int64_t t0 = tr.tile * kScanTile;
+    const uint32_t* row =
+        reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(tr.k) * N + tr.sg->c0);
+    const int base = cdf_quant_base(ymax[tr.b * S + tr.k], tr.sg->L);
     uint32_t v[kScanPer];
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
@@ -347,34 +379,39 @@ cdf_tile_sum_kernel(const float* __restrict__ yields, const uint32_t* __restrict
         unsigned long long t = 0;
 #pragma unroll
         for (int w = 0; w < kScanThreads / 32; w++) t += s_warp[w];
-        tile_sum[static_cast<int64_t>(s) * n_tiles + blockIdx.x] = t;
+        tile_sum[blockIdx.x] = t;
     }
 }
 
+// one block per row (b, k): exclusive scan of the row's tile sums, the row
+// total Q, the FP64 yield Q 2^-E, C[n] = Q and the guide sentinel
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_offset_kernel(const unsigned long long* __restrict__ tile_sum,
-                       const uint32_t* __restrict__ ymax, int n_tiles, int64_t n, int guide_bits,
-                       unsigned long long* __restrict__ tile_off, unsigned long long* __restrict__ qtot,
-                       double* __restrict__ totals, unsigned long long* __restrict__ cdf,
-                       int32_t* __restrict__ guide) {
+cdf_tile_offset_kernel(const SurfSeg* __restrict__ surf, int S,
+                       const unsigned long long* __restrict__ tile_sum,
+                       const uint32_t* __restrict__ ymax, unsigned long long* __restrict__ tile_off,
+                       unsigned long long* __restrict__ qtot, double* __restrict__ totals,
+                       unsigned long long* __restrict__ cdf, int32_t* __restrict__ guide) {
     __shared__ unsigned long long s_warp[33];
-    const int s = blockIdx.x;
+    const int r = blockIdx.x;
+    const int b = r / S, k = r - b * S;
+    const SurfSeg sg = surf[b];
+    const int64_t first = sg.tile_base + static_cast<int64_t>(k) * sg.nt;
     unsigned long long carry = 0;
-    for (int b = 0; b < n_tiles; b += kScanThreads) {
-        const int i = b + threadIdx.x;
-        const unsigned long long v = i < n_tiles ? tile_sum[static_cast<int64_t>(s) * n_tiles + i] : 0ull;
+    for (int i0 = 0; i0 < sg.nt; i0 += kScanThreads) {
+        const int i = i0 + threadIdx.x;
+        const unsigned long long v = i < sg.nt ? tile_sum[first + i] : 0ull;
         unsigned long long tot;
         const unsigned long long ex = block_excl_scan_u64(v, s_warp, &tot);
-        if (i < n_tiles) tile_off[static_cast<int64_t>(s) * n_tiles + i] = carry + ex;
+        if (i < sg.nt) tile_off[first + i] = carry + ex;
         carry += tot;
     }
     if (threadIdx.x == 0) {
-        const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
-        qtot[s] = carry;
-        totals[s] = carry ? ldexp(static_cast<double>(carry), -(150 + base)) : 0.0;
-        cdf[static_cast<int64_t>(s) * (n + 1) + n] = carry;
-        guide[(static_cast<int64_t>(s) << guide_bits) + s + (int64_t(1) << guide_bits)] =
-            static_cast<int32_t>(n - 1);
+        const int base = cdf_quant_base(ymax[r], sg.L);
+        qtot[r] = carry;
+        totals[r] = carry ? ldexp(static_cast<double>(carry), -(150 + base)) : 0.0;
+        cdf[sg.cdf_base + static_cast<int64_t>(k) * (sg.n + 1) + sg.n] = carry;
+        const int64_t G = int64_t(1) << sg.g;
+        guide[sg.guide_base + static_cast<int64_t>(k) * (G + 1) + G] = static_cast<int32_t>(sg.n - 1);
     }
 }
 
@@ -384,30 +421,34 @@ __device__ __forceinline__ unsigned long long bucket_start(unsigned long long j,
     return __umul64hi(j << (64 - g), Q);
 }
 
-// Writes row s of the cell CDF, C[i] = sum of q over cells < i, and scatters
-// the guide table (indexed search, Chen & Asau 1974): guide[j] is the cell
-// whose interval [C[i], C[i+1]) holds f(j).  The intervals partition [0, Q),
-// so every bucket j < 2^g gets exactly one writer; the cell of any v drawn
-// in bucket j lies in [guide[j], guide[j+1]].
+// Writes row (b, k) of the cell CDF, C[i] = sum of q over cells < i, and
+// scatters the guide table (indexed search, Chen & Asau 1974): guide[j] is
+// the cell whose interval [C[i], C[i+1]) holds f(j).  The intervals partition
+// [0, Q), so every bucket j < 2^g gets exactly one writer; the cell of any v
+// drawn in bucket j lies in [guide[j], guide[j+1]].
 __global__ void __launch_bounds__(kScanThreads)
-cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restrict__ ymax, int64_t n,
-                     int n_tiles, const unsigned long long* __restrict__ tile_off,
-                     const unsigned long long* __restrict__ qtot, int guide_bits,
+cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg* __restrict__ surf,
+                     int n_surf, int S, const uint32_t* __restrict__ ymax,
+                     const unsigned long long* __restrict__ tile_off,
+                     const unsigned long long* __restrict__ qtot,
                      unsigned long long* __restrict__ cdf, int32_t* __restrict__ guide) {
     // padded tile buffers: element e of the tile sits at (e / 8) * 9 + e % 8;
     // s_in holds the FP32 yield bits, s_c the CDF values on the way out
     __shared__ uint32_t s_in[kScanThreads * (kScanPer + 1)];
     __shared__ unsigned long long s_c[kScanThreads * (kScanPer + 1)];
     __shared__ unsigned long long s_warp[33];
-    const int s = blockIdx.y;
-    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(s) * n);
-    unsigned long long* out = cdf + static_cast<int64_t>(s) * (n + 1);
-    const int g = guide_bits;
+    const TileRef tr = tile_ref(surf, n_surf, S, blockIdx.x);
+    const int64_t n = tr.sg->n;
+    const int r = tr.b * S + tr.k;
+    const int64_t t0 = tr.tile * kScanTile;
+    const uint32_t* row =
+        reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(tr.k) * N + tr.sg->c0);
+    unsigned long long* out = cdf + tr.sg->cdf_base + static_cast<int64_t>(tr.k) * (n + 1);
+    const int g = tr.sg->g;
     const int64_t G = int64_t(1) << g;
-    int32_t* gd = guide + s * (G + 1);
-    const int base = cdf_quant_base(ymax[s], cdf_log2_cells(n));
-    const unsigned long long Q = qtot[s];
+    int32_t* gd = guide + tr.sg->guide_base + static_cast<int64_t>(tr.k) * (G + 1);
+    const int base = cdf_quant_base(ymax[r], tr.sg->L);
+    const unsigned long long Q = qtot[r];
     // coalesced load
     for (int k = 0; k < kScanPer; k++) {
         const int e = k * kScanThreads + threadIdx.x;
@@ -426,7 +467,7 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, const uint32_t* __restric
     }
     unsigned long long tot;
     const unsigned long long ex = block_excl_scan_u64(acc, s_warp, &tot);
-    const unsigned long long start = tile_off[static_cast<int64_t>(s) * n_tiles + blockIdx.x] + ex;
+    const unsigned long long start = tile_off[blockIdx.x] + ex;
     const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kScanPer;
     // q -> exclusive prefix C, in place
     unsigned long long run = start;
@@ -492,22 +533,22 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
 
 int cdf_num_tiles(int64_t n) { return static_cast<int>((n + kScanTile - 1) / kScanTile); }
 
-cudaError_t launch_cdf(const float* yields, uint32_t* ymax, int n_species, int64_t n,
-                       unsigned long long* tile_sum, unsigned long long* tile_off,
-                       unsigned long long* qtot, double* totals, unsigned long long* cdf,
-                       int32_t* guide, cudaStream_t stream) {
-    const int nt = cdf_num_tiles(n);
-    if (nt == 0 || n_species == 0) return cudaSuccess;
-    const int g = cdf_guide_bits(n);
-    dim3 grid(static_cast<unsigned>(nt), static_cast<unsigned>(n_species));
-    cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * n_species, stream);
+cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                       int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
+                       unsigned long long* tile_off, unsigned long long* qtot, double* totals,
+                       unsigned long long* cdf, int32_t* guide, cudaStream_t stream) {
+    if (n_tiles <= 0 || S <= 0 || n_surf <= 0) return cudaSuccess;
+    const int rows = n_surf * S;
+    cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * rows, stream);
     if (e != cudaSuccess) return e;
-    cdf_tile_max_kernel<<<grid, kScanThreads, 0, stream>>>(yields, n, ymax);
-    cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, ymax, n, nt, tile_sum);
-    cdf_tile_offset_kernel<<<n_species, kScanThreads, 0, stream>>>(tile_sum, ymax, nt, n, g, tile_off,
-                                                                   qtot, totals, cdf, guide);
-    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, ymax, n, nt, tile_off, qtot, g,
-                                                           cdf, guide);
+    const unsigned grid = static_cast<unsigned>(n_tiles);
+    cdf_tile_max_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax);
+    cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax,
+                                                          tile_sum);
+    cdf_tile_offset_kernel<<<rows, kScanThreads, 0, stream>>>(surf, S, tile_sum, ymax, tile_off,
+                                                             qtot, totals, cdf, guide);
+    cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax,
+                                                           tile_off, qtot, cdf, guide);
     return cudaGetLastError();
 }
 

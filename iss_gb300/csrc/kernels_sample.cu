@@ -209,8 +209,9 @@ __device__ __forceinline__ void item_decode(const DevConfig& cfg, int q, int& e,
 // per-species Poisson constants of the model-30 draws (same mu in every event)
 __global__ void count_consts_kernel(DevConfig cfg, const double* __restrict__ totals,
                                     PoissonC* __restrict__ pois, PoissonInv* __restrict__ inv) {
+    // one thread per (surface, species) row
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= cfg.n_species) return;
+    if (s >= cfg.n_surfaces * cfg.n_species) return;
     const double dN = __dmul_rn(totals[s], cfg.ymult);
     const PoissonC c = poisson_consts(dN);
     pois[s] = c;
@@ -228,7 +229,8 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
     const int s = static_cast<int>(idx % cfg.n_species);
     const uint32_t c2 = cfg.event_offset + static_cast<uint32_t>(e);
     const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCount << 16);
-    const double dN = __dmul_rn(totals[s], cfg.ymult);
+    const int row = cfg.ev_surf[e] * cfg.n_species + s;    // (surface, species)
+    const double dN = __dmul_rn(totals[row], cfg.ymult);
     const int64_t dN_int = static_cast<int64_t>(dN);
     const double frac = __dadd_rn(dN, -static_cast<double>(dN_int));
     const double para1 = cfg.sampling_para1;
@@ -252,8 +254,8 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
         }
     } else {
         nsamp = (dN < 1e-15) ? 0
-                             : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, pois[s], cfg.tab.logfact,
-                                            inv + s);
+                             : poisson_draw(c2, c3, cfg.key0, cfg.key1, 0u, pois[row],
+                                            cfg.tab.logfact, inv + row);
         if (nsamp < 0) atomicCAS(error, 0, 3);
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
@@ -683,14 +685,13 @@ constexpr int kAssignThreads = 256;
 
 __global__ void __launch_bounds__(kAssignThreads)
 cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
-                   const int32_t* __restrict__ guide, int guide_bits,
+                   const int32_t* __restrict__ guide,
                    const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                    const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
                    int64_t k_begin, int64_t k_end, int32_t* __restrict__ cell_of) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    const int64_t ncell = cfg.n_cells;
     for (int64_t k = k_begin + warp; k < k_end; k += n_warps) {
         const int q = item_seg[k];
         const int64_t j = k - item_off[q];
@@ -700,16 +701,18 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         const int64_t base = offsets[seg];
         const int64_t start = base + j * kItem;
         const int64_t end = min(start + kItem, offsets[seg + 1]);
-        const unsigned long long* row = cdf + static_cast<int64_t>(s) * (ncell + 1);
-        const int32_t* gd = guide + static_cast<int64_t>(s) * ((int64_t(1) << guide_bits) + 1);
-        const unsigned long long Q = qtot[s];
+        const int b = cfg.ev_surf[e];
+        const SurfSeg sg = cfg.surf[b];
+        const unsigned long long* row = cdf + sg.cdf_base + static_cast<int64_t>(s) * (sg.n + 1);
+        const int32_t* gd = guide + sg.guide_base + static_cast<int64_t>(s) * ((int64_t(1) << sg.g) + 1);
+        const unsigned long long Q = qtot[b * cfg.n_species + s];
         const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
         const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
         for (int64_t h = start + lane; h < end; h += 32) {
             const uint4 w = block(0u, static_cast<uint32_t>(h - base), eg, c3, cfg.key0, cfg.key1);
             const unsigned long long r =
                 (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
-            cell_of[h] = cell_search(row, ncell, gd, guide_bits, Q, r);
+            cell_of[h] = static_cast<int32_t>(sg.c0) + cell_search(row, sg.n, gd, sg.g, Q, r);
         }
     }
 }
@@ -719,7 +722,7 @@ constexpr int kSampleThreads = 256;
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
-               const int32_t* __restrict__ guide, int guide_bits,
+               const int32_t* __restrict__ guide,
                const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
                int64_t k_begin, int64_t k_end, const int32_t* __restrict__ cell_of,
@@ -727,7 +730,6 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int64_t ncell = cfg.n_cells;
     // the warp's current work item: units [next, end) of species cur_s in event cur_e
     int64_t next = 0, end = 0, seg_base = 0;
     int cur_s = 0, cur_e = 0;
@@ -799,10 +801,13 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                                           cfg.key1);
                     const unsigned long long r = (static_cast<unsigned long long>(w.x) << 32) |
                                                  static_cast<unsigned long long>(w.y);
-                    l = cell_search(
-                        cdf + static_cast<int64_t>(u.s) * (ncell + 1), ncell,
-                        guide + static_cast<int64_t>(u.s) * ((int64_t(1) << guide_bits) + 1),
-                        guide_bits, qtot[u.s], r);
+                    const int b = cfg.ev_surf[u.eg - cfg.event_offset];
+                    const SurfSeg sg = cfg.surf[b];
+                    l = static_cast<int>(sg.c0) +
+                        cell_search(cdf + sg.cdf_base + static_cast<int64_t>(u.s) * (sg.n + 1), sg.n,
+                                    guide + sg.guide_base +
+                                        static_cast<int64_t>(u.s) * ((int64_t(1) << sg.g) + 1),
+                                    sg.g, qtot[b * cfg.n_species + u.s], r);
                 }
                 u.cell = l;
                 u.tries_cell = 0;
@@ -849,9 +854,10 @@ cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* po
                           int32_t* items, int* error, cudaStream_t stream) {
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (total <= 0) return cudaSuccess;
+    const int rows = cfg.n_surfaces * cfg.n_species;
     PoissonC* pc = reinterpret_cast<PoissonC*>(pois);
-    PoissonInv* inv = reinterpret_cast<PoissonInv*>(pc + cfg.n_species);
-    count_consts_kernel<<<(cfg.n_species + 127) / 128, 128, 0, stream>>>(cfg, totals, pc, inv);
+    PoissonInv* inv = reinterpret_cast<PoissonInv*>(pc + rows);
+    count_consts_kernel<<<(rows + 127) / 128, 128, 0, stream>>>(cfg, totals, pc, inv);
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
     counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, pc, inv, counts, items, error);
     return cudaGetLastError();
@@ -879,7 +885,7 @@ cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64
 
 cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
                            const int32_t* pids, const unsigned long long* cdf,
-                           const int32_t* guide, int guide_bits, const unsigned long long* qtot,
+                           const int32_t* guide, const unsigned long long* qtot,
                            const int64_t* offsets,
                            const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
                            int64_t k_end, int32_t* cell_of, HadronRec* out,
@@ -892,7 +898,7 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
         const int64_t need = (n_items + (kAssignThreads / 32) - 1) / (kAssignThreads / 32);
         if (blocks > need) blocks = need;
         cell_assign_kernel<<<static_cast<unsigned>(blocks), kAssignThreads, 0, stream>>>(
-            cfg, cdf, guide, guide_bits, qtot, offsets, item_off, item_seg, k_begin, k_end, cell_of);
+            cfg, cdf, guide, qtot, offsets, item_off, item_seg, k_begin, k_end, cell_of);
     }
     const int per_sm = 3;
     int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
@@ -900,7 +906,7 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
     sampler_kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
-        cfg, cells, sp, pids, cdf, guide, guide_bits, qtot, offsets, item_off, item_seg, k_begin,
+        cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters);
     return cudaGetLastError();
 }

@@ -29,7 +29,8 @@ OUTPUT_OSCAR, OUTPUT_GZIP, OUTPUT_BINARY = 1, 2, 3
 EXPORTED = [
     "iss_gpu_create", "iss_gpu_destroy", "iss_gpu_set_param", "iss_gpu_get_param",
     "iss_gpu_parse_param_line", "iss_gpu_set_seed", "iss_gpu_set_seed_from_params",
-    "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_generate", "iss_gpu_generate_into",
+    "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_set_surface_batch",
+    "iss_gpu_generate", "iss_gpu_generate_into",
     "iss_gpu_shell",
     "iss_gpu_clear", "iss_gpu_num_events", "iss_gpu_num_particles", "iss_gpu_get_hadron",
     "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output", "iss_gpu_species",
@@ -78,6 +79,7 @@ def lib():
         L.iss_gpu_set_seed_from_params.argtypes = [h]
         L.iss_gpu_read_surface.argtypes = [h]
         L.iss_gpu_set_surface.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_set_surface_batch.argtypes = [h, v, v, v, C.c_int32]
         L.iss_gpu_generate.argtypes = [h]
         L.iss_gpu_generate_into.argtypes = [h, v, C.c_int64, C.POINTER(C.c_int64)]
         L.iss_gpu_shell.argtypes = [h]
@@ -182,6 +184,18 @@ class iSS:
         a = np.ascontiguousarray(fo_surf_records, dtype=np.float32)
         assert a.ndim == 2 and a.shape[1] == 34
         self._check(self._L.iss_gpu_set_surface(self._h, _ptr(a), a.shape[0]))
+
+    def set_surface_batch(self, surfaces, events):
+        """Several FO_surf record arrays, sampled together by one
+        generate_samples; events[b] events for surface b, numbered across the
+        batch in surface order."""
+        recs = np.ascontiguousarray(np.concatenate([np.asarray(r, dtype=np.float32)
+                                                    for r in surfaces]), dtype=np.float32)
+        off = np.zeros(len(surfaces) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(r) for r in surfaces])
+        ev = np.ascontiguousarray(events, dtype=np.int32)
+        return self._check(self._L.iss_gpu_set_surface_batch(self._h, _ptr(recs), _ptr(off),
+                                                             _ptr(ev), len(surfaces)))
 
     def generate_samples(self):
         return self._check(self._L.iss_gpu_generate(self._h))

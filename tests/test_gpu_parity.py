@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
-from iss_gb300 import iSS, surfaces as S
+from iss_gb300 import iSS, native, surfaces as S
 
 pytestmark = pytest.mark.gpu
 
@@ -168,3 +168,38 @@ def test_generate_into_matches_generate_and_copy_all():
         b.generate_into(small)
     hc, _ = b.all_hadrons()
     assert hc.tobytes() == ha.tobytes()
+
+
+def test_surface_batch_matches_single_surface_runs():
+    """iss_gpu_set_surface_batch: one generate over three surfaces of
+    different sizes gives, for each surface, the hadrons of a single-surface
+    run with the event offset of its place in the batch (bit for bit), and
+    the same per-species yields."""
+    surfs = [S.viscous_3d(n, seed=sd) for n, sd in ((3000, 21), (517, 22), (6001, 23))]
+    events = [5, 12, 3]
+    params = dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=0,
+                  include_deltaf_shear=1, include_deltaf_bulk=1, bulk_deltaf_kind=11,
+                  turn_on_bulk=1)
+    s = iSS(".", inputfile="")
+    s.set_params(**params)
+    s.set_surface_batch([x.fo_surf() for x in surfs], events)
+    s.set_random_seed(31)
+    s.generate_samples()
+    had, off = s.all_hadrons()
+    assert s.get_number_of_sampled_events() == sum(events)
+    nsp = len(s.species())
+    rows = np.zeros(3 * nsp)
+    native.lib().iss_gpu_species_yields(s._h, native._ptr(rows), rows.size)
+    e0 = 0
+    for b, (surf, ne) in enumerate(zip(surfs, events)):
+        t = iSS(".", inputfile="")
+        t.set_params(**dict(params, number_of_repeated_sampling=ne, gpu_event_offset=e0))
+        t.set_surface(surf.fo_surf())
+        t.set_random_seed(31)
+        t.generate_samples()
+        hb, offb = t.all_hadrons()
+        mine = had[off[e0]:off[e0 + ne]]
+        assert mine.tobytes() == hb.tobytes(), f"surface {b} differs"
+        assert np.array_equal(off[e0:e0 + ne + 1] - off[e0], offb)
+        assert np.array_equal(rows[b * nsp:(b + 1) * nsp], t.species_yields())
+        e0 += ne
