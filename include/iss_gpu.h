@@ -230,8 +230,10 @@ iss_status iss_gpu_copy_lrf_cells(iss_handle* h, float* out, int64_t capacity_ce
 iss_status iss_gpu_copy_cell_yields(iss_handle* h, int32_t species_index,
                                     float* out, int64_t capacity_cells);
 
-/* Hadron counts per (event, species), event-major, of the last generate
- * (src/FSSW.cpp:970-977). */
+/* Hadron records per (event, species), event-major, of the last generate
+ * (src/FSSW.cpp:970-977).  Under local_charge_conservation, a positively
+ * charged species counts two records per draw (hadron and partner), and a
+ * negatively charged one counts 0. */
 iss_status iss_gpu_copy_counts(iss_handle* h, int32_t* out, int64_t capacity);
 
 /* Timings and loop counters of the last iss_gpu_generate. */

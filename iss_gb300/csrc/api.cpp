@@ -262,8 +262,7 @@ iss_status prepare(iss_handle* h) {
     c.bulk_kind = static_cast<int>(vals[3]);
     c.include_diff = static_cast<int>(vals[4]) == 1;
     c.neos_kind = (c.bulk_kind == 21) ? 1 : (c.bulk_kind == 20 ? 0 : -1);
-    if (static_cast<int>(vals[5]) != 0)
-        return fail(h, ISS_ERR_UNSUPPORTED, "local_charge_conservation = 1 is not supported");
+    c.lcc = static_cast<int>(vals[5]) == 1;
     c.n_events = static_cast<int>(vals[6]);
     c.sampling_model = static_cast<int>(vals[7]);
     c.sampling_para1 = vals[8];
@@ -562,8 +561,8 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     // kInvTable + 1 doubles (the last holds the length)
     CUDA_TRY(h, h->d_pois.reserve(static_cast<size_t>(std::max(S * c.n_surfaces, 1)) *
                                   (kPoissonConsts + kInvTable + 1)));
-    CUDA_TRY(h, launch_counts(c, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr, h->d_items.ptr,
-                              h->d_error.ptr, s));
+    CUDA_TRY(h, launch_counts(c, h->d_species.ptr, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr,
+                              h->d_items.ptr, h->d_error.ptr, s));
     CUDA_TRY(h, launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
     CUDA_TRY(h, launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
     int64_t sizes[2] = {0, 0};   // hadrons, work items

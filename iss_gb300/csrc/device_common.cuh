@@ -45,6 +45,7 @@ struct DevConfig {
     int include_shear, include_bulk, include_diff;
     int bulk_kind, neos_kind;
     int compat_fermion;
+    int lcc;                 // local_charge_conservation (src/FSSW.cpp:931-938, 1035-1048)
     int sampling_model;
     double sampling_para1;
     float y_lb, y_rb;

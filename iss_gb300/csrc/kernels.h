@@ -29,8 +29,9 @@ cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int 
 // two launches: Poisson constants and inversion tables of every (surface,
 // species) row (pois, (kPoissonConsts + kInvTable + 1) doubles per row), then
 // one count per (event, species); totals has n_surfaces * S rows
-cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* pois, int32_t* counts,
-                          int32_t* items, int* error, cudaStream_t stream);
+cudaError_t launch_counts(const DevConfig& cfg, const SpeciesDev* species, const double* totals,
+                          double* pois, int32_t* counts, int32_t* items, int* error,
+                          cudaStream_t stream);
 int offsets_num_tiles(int64_t n);
 cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_sum,
                                 int64_t* offsets, cudaStream_t stream);

@@ -196,6 +196,15 @@ __device__ __forceinline__ int64_t item_index(const DevConfig& cfg, int e, int s
     return static_cast<int64_t>(e0) * cfg.n_species + static_cast<int64_t>(s) * ne + (e - e0);
 }
 
+// local_charge_conservation: every hadron of a positively charged species is
+// followed in its event by a partner of the same mass and opposite quantum
+// numbers sampled in the same cell; negatively charged species are not
+// sampled on their own (src/FSSW.cpp:931-938, 1035-1048).  A segment of a
+// positive species then holds two records per draw.
+__device__ __forceinline__ int records_per_draw(const DevConfig& cfg, const SpeciesDev& sp) {
+    return (cfg.lcc && sp.charge > 0) ? 2 : 1;
+}
+
 __device__ __forceinline__ void item_decode(const DevConfig& cfg, int q, int& e, int& s) {
     const int per = cfg.chunk_events * cfg.n_species;
     const int c = q / per;
@@ -218,7 +227,8 @@ __global__ void count_consts_kernel(DevConfig cfg, const double* __restrict__ to
     poisson_inv_table(c, inv[s]);
 }
 
-__global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
+__global__ void counts_kernel(DevConfig cfg, const SpeciesDev* __restrict__ species,
+                              const double* __restrict__ totals,
                               const PoissonC* __restrict__ pois,
                               const PoissonInv* __restrict__ inv, int32_t* __restrict__ counts,
                               int32_t* __restrict__ items, int* __restrict__ error) {
@@ -235,7 +245,10 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
     const double frac = __dadd_rn(dN, -static_cast<double>(dN_int));
     const double para1 = cfg.sampling_para1;
     int64_t nsamp = 0;
-    if (dN < 0) {
+    const SpeciesDev sp = species[s];
+    if (cfg.lcc && sp.charge < 0) {
+        nsamp = 0;   // sampled as partners of the positive species
+    } else if (dN < 0) {
         atomicCAS(error, 0, 2);
     } else if (cfg.sampling_model == 1) {
         const uint4 w = block(0u, 0u, c2, c3, cfg.key0, cfg.key1);
@@ -259,7 +272,7 @@ __global__ void counts_kernel(DevConfig cfg, const double* __restrict__ totals,
         if (nsamp < 0) atomicCAS(error, 0, 3);
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
-    counts[idx] = c;
+    counts[idx] = c * records_per_draw(cfg, sp);       // records of the segment
     items[item_index(cfg, e, s)] = (c + kItem - 1) / kItem;
 }
 
@@ -389,6 +402,8 @@ struct Unit {
     int redraw;
     int tries_cell;
     uint32_t t;                // tries made so far (proposal counter)
+    int mult;                  // records per draw (2: local charge conservation pair)
+    int phase;                 // 1: sampling the partner of a pair
 };
 
 // Cell draw from 64 random bits r on the fixed-point CDF row C[0..n]
@@ -688,7 +703,8 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
                    const int32_t* __restrict__ guide,
                    const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                    const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
-                   int64_t k_begin, int64_t k_end, int32_t* __restrict__ cell_of) {
+                   int64_t k_begin, int64_t k_end, const SpeciesDev* __restrict__ species,
+                   int32_t* __restrict__ cell_of) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -699,8 +715,10 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         item_decode(cfg, q, e, s);
         const int64_t seg = static_cast<int64_t>(e) * cfg.n_species + s;
         const int64_t base = offsets[seg];
-        const int64_t start = base + j * kItem;
-        const int64_t end = min(start + kItem, offsets[seg + 1]);
+        const int mult = records_per_draw(cfg, species[s]);
+        const int64_t draws = (offsets[seg + 1] - base) / mult;
+        const int64_t d_begin = j * kItem;
+        const int64_t d_end = min(d_begin + kItem, draws);
         const int b = cfg.ev_surf[e];
         const SurfSeg sg = cfg.surf[b];
         const unsigned long long* row = cdf + sg.cdf_base + static_cast<int64_t>(s) * (sg.n + 1);
@@ -708,17 +726,20 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         const unsigned long long Q = qtot[b * cfg.n_species + s];
         const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
         const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
-        for (int64_t h = start + lane; h < end; h += 32) {
-            const uint4 w = block(0u, static_cast<uint32_t>(h - base), eg, c3, cfg.key0, cfg.key1);
+        for (int64_t d = d_begin + lane; d < d_end; d += 32) {
+            const uint4 w = block(0u, static_cast<uint32_t>(d), eg, c3, cfg.key0, cfg.key1);
             const unsigned long long r =
                 (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
-            cell_of[h] = static_cast<int32_t>(sg.c0) + cell_search(row, sg.n, gd, sg.g, Q, r);
+            cell_of[base + d * mult] = static_cast<int32_t>(sg.c0) + cell_search(row, sg.n, gd, sg.g, Q, r);
         }
     }
 }
 
 constexpr int kSampleThreads = 256;
 
+// kLcc: local_charge_conservation pairs (a separate instantiation, so the
+// common case carries none of the pair state)
+template <bool kLcc>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
@@ -731,8 +752,8 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // the warp's current work item: units [next, end) of species cur_s in event cur_e
-    int64_t next = 0, end = 0, seg_base = 0;
-    int cur_s = 0, cur_e = 0;
+    int64_t next = 0, end = 0, seg_base = 0;     // draws [next, end); records from seg_base
+    int cur_s = 0, cur_e = 0, cur_mult = 1;
     bool exhausted = false;
     bool active = false;
     Unit u;
@@ -759,16 +780,19 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                 item_decode(cfg, q, cur_e, cur_s);
                 const int64_t seg = static_cast<int64_t>(cur_e) * cfg.n_species + cur_s;
                 seg_base = offsets[seg];
-                next = seg_base + j * kItem;
-                end = min(next + kItem, offsets[seg + 1]);
+                cur_mult = kLcc ? records_per_draw(cfg, species[cur_s]) : 1;
+                next = j * kItem;
+                end = min(next + kItem, (offsets[seg + 1] - seg_base) / cur_mult);
             }
             const int64_t avail = end - next;
             const int rank = __popc(need & ((1u << lane) - 1u));
             if (!active && rank < avail) {
-                const int64_t h = next + rank;
+                const int64_t d = next + rank;
                 u.s = cur_s;
-                u.slot = h;
-                u.i = static_cast<uint32_t>(h - seg_base);
+                u.slot = seg_base + d * cur_mult;
+                u.i = static_cast<uint32_t>(d);
+                u.mult = cur_mult;
+                u.phase = 0;
                 u.eg = cfg.event_offset + static_cast<uint32_t>(cur_e);
                 u.redraw = 0;
                 u.t = 0;
@@ -781,14 +805,26 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
         }
         if (__ballot_sync(FULL, active) == 0) break;
         if (active) {
-            if (u.cell < 0 || u.tries_cell >= cfg.max_tries) {
+            if (kLcc && u.phase == 1 && u.tries_cell >= cfg.max_tries) {
+                // the partner stays in its pair's cell (the reference retries there)
+                u.redraw++;
+                n_redraws++;
+                u.tries_cell = 0;
+                if (u.redraw > cfg.max_redraws) {
+                    write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                    n_fail++;
+                    active = false;
+                    continue;
+                }
+            } else if (u.cell < 0 || u.tries_cell >= cfg.max_tries) {
                 if (u.cell >= 0) {
                     u.redraw++;
                     n_redraws++;
                 }
                 if (u.redraw > cfg.max_redraws) {
-                    write_hadron(out, u.slot, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-                    n_fail++;
+                    for (int q = 0; q < (kLcc ? u.mult : 1); q++)
+                        write_hadron(out, u.slot + q, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                    n_fail += kLcc ? u.mult : 1;
                     active = false;
                     continue;
                 }
@@ -814,8 +850,9 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                 if (!setup_prop(cfg, cells, species[u.s], l, p)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
-                    write_hadron(out, u.slot, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-                    n_fail++;
+                    for (int q = 0; q < (kLcc ? u.mult : 1); q++)
+                        write_hadron(out, u.slot + q, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                    n_fail += kLcc ? u.mult : 1;
                     active = false;
                     continue;
                 }
@@ -827,8 +864,28 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
             u.tries_cell++;
             n_tries++;
             if (ok) {
-                emit(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
-                active = false;
+                if (kLcc)
+                    emit(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out, u.slot + u.phase);
+                else
+                    emit(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
+                if (kLcc && u.mult == 2 && u.phase == 0) {
+                    // the partner: same cell and mass, opposite B, S, Q
+                    SpeciesDev sp2 = species[u.s];
+                    sp2.baryon = -sp2.baryon;
+                    sp2.strange = -sp2.strange;
+                    sp2.charge = -sp2.charge;
+                    u.phase = 1;
+                    u.tries_cell = 0;
+                    if (!setup_prop(cfg, cells, sp2, u.cell, p)) {
+                        atomicCAS(&ctrs->error_code, 0, 1);
+                        ctrs->error_species = u.s;
+                        write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+                        n_fail++;
+                        active = false;
+                    }
+                } else {
+                    active = false;
+                }
             }
         }
     }
@@ -850,8 +907,9 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
 
 }  // namespace
 
-cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* pois, int32_t* counts,
-                          int32_t* items, int* error, cudaStream_t stream) {
+cudaError_t launch_counts(const DevConfig& cfg, const SpeciesDev* species, const double* totals,
+                          double* pois, int32_t* counts, int32_t* items, int* error,
+                          cudaStream_t stream) {
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (total <= 0) return cudaSuccess;
     const int rows = cfg.n_surfaces * cfg.n_species;
@@ -859,7 +917,7 @@ cudaError_t launch_counts(const DevConfig& cfg, const double* totals, double* po
     PoissonInv* inv = reinterpret_cast<PoissonInv*>(pc + rows);
     count_consts_kernel<<<(rows + 127) / 128, 128, 0, stream>>>(cfg, totals, pc, inv);
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
-    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, totals, pc, inv, counts, items, error);
+    counts_kernel<<<blocks, 256, 0, stream>>>(cfg, species, totals, pc, inv, counts, items, error);
     return cudaGetLastError();
 }
 
@@ -898,14 +956,15 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
         const int64_t need = (n_items + (kAssignThreads / 32) - 1) / (kAssignThreads / 32);
         if (blocks > need) blocks = need;
         cell_assign_kernel<<<static_cast<unsigned>(blocks), kAssignThreads, 0, stream>>>(
-            cfg, cdf, guide, qtot, offsets, item_off, item_seg, k_begin, k_end, cell_of);
+            cfg, cdf, guide, qtot, offsets, item_off, item_seg, k_begin, k_end, sp, cell_of);
     }
     const int per_sm = 3;
     int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    sampler_kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
+    auto kernel = cfg.lcc ? sampler_kernel<true> : sampler_kernel<false>;
+    kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters);
     return cudaGetLastError();

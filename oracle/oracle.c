@@ -597,7 +597,13 @@ int orc_counts(const orc_cfg* c, const orc_species* sp, int32_t n_sp, const doub
             s.ctr[3] = (uint32_t)k | ((uint32_t)ORC_TAG_COUNT << 16);
             const double dN = totals[k] * ymult;
             int64_t n = 0;
-            (void)sp;
+            /* local_charge_conservation: negative species are not drawn; a
+             * positive species' segment holds two records per draw */
+            if (c->lcc && sp[k].charge < 0) {
+                counts[e * n_sp + k] = 0;
+                continue;
+            }
+            const int mult = (c->lcc && sp[k].charge > 0) ? 2 : 1;
             if (dN < 0) return -2;
             const int64_t dN_int = (int64_t)dN;
             const double frac = dN - (double)dN_int;
@@ -638,7 +644,7 @@ int orc_counts(const orc_cfg* c, const orc_species* sp, int32_t n_sp, const doub
                     return -3;
             }
             if (n < 0) return -4;
-            counts[e * n_sp + k] = (int32_t)n;
+            counts[e * n_sp + k] = (int32_t)(n * mult);
         }
     }
     return 0;

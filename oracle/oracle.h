@@ -54,6 +54,7 @@ typedef struct orc_cfg {
     int32_t compat_fermion;     /* 1: reproduce the reference's fermion CDF_2 term */
     int32_t max_tries;          /* proposals per cell before the cell is redrawn */
     int32_t max_redraws;
+    int32_t lcc;                /* local_charge_conservation */
     /* special-function tables, ORC_SF_LEN rows */
     const double* sf_K;         /* [row][3] = K1, K2, K3 */
     const double* sf_E;         /* [row][9] = E_2, E_4, ..., E_18 */

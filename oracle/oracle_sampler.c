@@ -308,11 +308,15 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
     for (int64_t e = 0; e < cfg->n_events; e++) {
         const uint32_t eg = (uint32_t)(cfg->event_offset + e);
         for (int32_t k = 0; k < n_sp; k++) {
-            const int32_t n_units = counts[e * n_sp + k];
             const orc_species* s = sp + k;
+            /* local_charge_conservation: two records per draw of a positive
+             * species, the second a partner with opposite B, S, Q sampled in
+             * the same cell (src/FSSW.cpp:1035-1048) */
+            const int paired = cfg->lcc && s->charge > 0;
+            const int32_t n_draws = counts[e * n_sp + k] / (paired ? 2 : 1);
             const uint64_t* row = cdf + (int64_t)k * (n_cells + 1);
-            for (int32_t i = 0; i < n_units; i++) {
-                if (w >= capacity) return -1;
+            for (int32_t i = 0; i < n_draws; i++) {
+                if (w + (paired ? 2 : 1) > capacity) return -1;
                 orc_hstream hs;
                 hs.key[0] = (uint32_t)cfg->seed;
                 hs.key[1] = (uint32_t)(cfg->seed >> 32);
@@ -322,12 +326,12 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
                 uint32_t t = 0;
                 int32_t redraw = 0;
                 int done = 0;
+                orc_cell c;
                 while (!done) {
                     uint32_t wc[4];
                     orc_hblock(&hs, (uint32_t)redraw, ORC_TAG_CELL, wc);
                     const uint64_t r = ((uint64_t)wc[0] << 32) | (uint64_t)wc[1];
                     const int64_t l = orc_search(row, n_cells, qtot[k], r);
-                    orc_cell c;
                     orc_load_cell(lrf28, coef4, l, &c);
                     orc_prop p;
                     const double mu = s->baryon * c.muB + s->strange * c.muS + s->charge * c.muQ;
@@ -350,11 +354,47 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
                         redraw++;
                         stats->n_redraws++;
                         if (redraw > cfg->max_redraws) {
-                            /* abandoned: the GPU writes an empty record */
+                            /* abandoned: the GPU writes empty records */
+                            for (int q = 0; q < (paired ? 2 : 1); q++) {
+                                memset(out + w, 0, sizeof(orc_hadron));
+                                w++;
+                                stats->n_failures++;
+                            }
+                            done = 2;
+                        }
+                    }
+                }
+                if (!paired || done == 2) continue;
+                /* the partner: same cell and mass, opposite quantum numbers; the
+                 * proposal counter t continues and the cell is never redrawn */
+                orc_prop p2;
+                const double mu2 =
+                    (-s->baryon) * c.muB + (-s->strange) * c.muS + (-s->charge) * c.muQ;
+                orc_setup(cfg, s->mass, s->sign, mu2, c.T, &p2);
+                if (p2.status) return -2;
+                int pdone = 0;
+                while (!pdone) {
+                    for (int32_t tr = 0; tr < cfg->max_tries; tr++) {
+                        double pl[4], u_rap = 0.0;
+                        const int ok = orc_try(cfg, &c, &p2, s->sign, -s->baryon, &hs, t, pl,
+                                               &u_rap, &stats->n_bound_violations);
+                        t++;
+                        stats->n_tries++;
+                        if (ok) {
+                            orc_emit(cfg, &c, s->mass, -s->pid, pl, u_rap, out + w);
+                            w++;
+                            pdone = 1;
+                            break;
+                        }
+                    }
+                    if (!pdone) {
+                        redraw++;
+                        stats->n_redraws++;
+                        if (redraw > cfg->max_redraws) {
                             memset(out + w, 0, sizeof(orc_hadron));
                             w++;
                             stats->n_failures++;
-                            done = 1;
+                            pdone = 1;
                         }
                     }
                 }

@@ -159,12 +159,29 @@ def sample_case(name, surface, params, work_root):
     print(f"{name}: {len(events)} events, {tot} hadrons")
 
 
+def lcc_case(visc_params, work_root):
+    """local_charge_conservation = 1: positive hadrons with partners."""
+    sample_case("viscous_lcc", S.viscous_3d(256, seed=2),
+                dict(visc_params, local_charge_conservation=1, number_of_repeated_sampling=30000,
+                     randomSeed=14), work_root)
+
+
 def main():
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=None, help="make only this fixture (e.g. samples_viscous_lcc)")
+    only = ap.parse_args().only
     build_reference()
     work_root = tempfile.mkdtemp(prefix="iss_golden_")
+    visc_params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
+                       include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1)
+    if only == "samples_viscous_lcc":
+        try:
+            lcc_case(visc_params, work_root)
+        finally:
+            shutil.rmtree(work_root, ignore_errors=True)
+        return
     try:
-        visc_params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
-                           include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1)
         # per-cell yields
         yield_case("ideal_boost_invariant", S.ideal_boost_invariant(),
                    dict(hydro_mode=1, afterburner_type=0, include_deltaf_shear=1),
@@ -194,6 +211,7 @@ def main():
         sample_case("ideal_boost_invariant", S.ideal_boost_invariant(),
                     dict(hydro_mode=1, afterburner_type=0, include_deltaf_shear=1,
                          number_of_repeated_sampling=1000, randomSeed=13), work_root)
+        lcc_case(visc_params, work_root)
     finally:
         shutil.rmtree(work_root, ignore_errors=True)
 

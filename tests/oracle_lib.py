@@ -50,7 +50,7 @@ class Cfg(C.Structure):
                 ("sampling_model", C.c_int32), ("sampling_para1", C.c_double),
                 ("n_events", C.c_int64), ("event_offset", C.c_int64), ("seed", C.c_uint64),
                 ("compat_fermion", C.c_int32), ("max_tries", C.c_int32),
-                ("max_redraws", C.c_int32),
+                ("max_redraws", C.c_int32), ("lcc", C.c_int32),
                 ("sf_K", C.c_void_p), ("sf_E", C.c_void_p),
                 ("b14_nT", C.c_int32), ("b14_nmu", C.c_int32),
                 ("b14_T0", C.c_double), ("b14_mu0", C.c_double), ("b14_dT", C.c_double),
@@ -207,6 +207,7 @@ class OracleConfig:
         c.compat_fermion = int(compat_fermion)
         c.max_tries = max_tries
         c.max_redraws = max_redraws
+        c.lcc = int(int(p.get("local_charge_conservation", 0)) == 1)
         L = lib()
         self.sf_K = np.zeros(SF_LEN * 3)
         self.sf_E = np.zeros(SF_LEN * 9)

@@ -78,12 +78,14 @@ def test_yields_match_reference(name):
     assert trel.max() < TOTAL_RTOL, f"per-species yields differ by {trel.max():.2e}"
 
 
-@pytest.mark.parametrize("name", ["viscous_14moment", "ideal_boost_invariant", "diffusion_smash",
-                                  "viscous_ce_smash"])
-def test_counts_and_hadrons_match_oracle_replay(name):
+@pytest.mark.parametrize("name,extra", [("viscous_14moment", None), ("ideal_boost_invariant", None),
+                                        ("diffusion_smash", None), ("viscous_ce_smash", None),
+                                        ("viscous_14moment", {"local_charge_conservation": 1}),
+                                        ("diffusion_smash", {"local_charge_conservation": 1})])
+def test_counts_and_hadrons_match_oracle_replay(name, extra):
     g = O.load_golden(f"yields_{name}.npz")
     n_events = 200 if name != "ideal_boost_invariant" else 20
-    s, params = run_golden_case(g, n_events=n_events, seed=2024)
+    s, params = run_golden_case(g, n_events=n_events, seed=2024, extra=extra)
     lrf = s.lrf_cells()
     tot = s.species_yields()
     cnt = s.counts()

@@ -146,6 +146,42 @@ def test_fixed_point_cdf_properties():
         assert C[i] <= v < C[i + 1] and q[i] > 0
 
 
+def test_local_charge_conservation_pairs():
+    """local_charge_conservation = 1 (src/FSSW.cpp:931-938, 1035-1048):
+    negatively charged species are not drawn, every hadron of a positive
+    species is followed by its partner (-pid, same mass, same cell)."""
+    g = O.load_golden("yields_viscous_14moment.npz")
+    p = dict(g["params"], number_of_repeated_sampling=4, local_charge_conservation=1)
+    oc = O.OracleConfig(p, S.TABLE_DIR, n_events=4, seed=9)
+    lrf = g["lrf"]
+    y = g["yields"].astype(np.float32)
+    cdf, tot = O.cdf(y)
+    sp_ = g["species"]
+    cnt = O.counts(oc, sp_, tot)
+    assert np.all(cnt[:, sp_["charge"] < 0] == 0)
+    assert np.all(cnt[:, sp_["charge"] > 0] % 2 == 0)
+    assert cnt[:, sp_["charge"] > 0].sum() > 0
+    coef = O.cell_coeffs(oc, lrf).astype(np.float32)
+    had, st = O.sample_replay(oc, sp_, lrf, coef, cdf, cnt)
+    assert len(had) == cnt.sum() and st.n_failures == 0
+    pos = np.isin(had["pid"], sp_["pid"][sp_["charge"] > 0])
+    first = np.flatnonzero(pos)
+    # records of positive species come in (hadron, partner) pairs
+    seg_start = np.concatenate([[0], np.cumsum(cnt.ravel())])[:-1]
+    pairs = []
+    for e in range(cnt.shape[0]):
+        for k in np.flatnonzero(sp_["charge"] > 0):
+            b = seg_start[e * len(sp_) + k]
+            for i in range(cnt[e, k] // 2):
+                pairs.append((b + 2 * i, b + 2 * i + 1))
+    a, b = np.array(pairs).T
+    assert np.array_equal(had["pid"][b], -had["pid"][a])
+    assert np.array_equal(had["mass"][b], had["mass"][a])
+    for f in ("x", "y", "t", "z"):
+        assert np.array_equal(had[f][b], had[f][a])
+    assert len(first) >= len(pairs)
+
+
 def test_oracle_replay_respects_counts_and_order():
     g = O.load_golden("yields_viscous_14moment.npz")
     p = dict(g["params"], number_of_repeated_sampling=3)
