@@ -678,6 +678,101 @@ iss_status ensure_host_copy(iss_handle* h) {
     return ISS_OK;
 }
 
+// OSCAR output with the text made on the GPU: the header file is copied,
+// then chunks of whole events are formatted on the device, copied to
+// page-locked host memory and written, two chunks in flight.
+iss_status write_oscar_gpu(iss_handle* h, const char* filename) {
+    const std::string header_file = h->table_path + "/OSCAR_header.txt";
+    std::ifstream header(header_file);
+    if (!header) return fail(h, ISS_ERR_IO, "OSCAR header file %s not found", header_file.c_str());
+    std::remove(filename);
+    std::FILE* f = std::fopen(filename, "w");
+    if (!f) return fail(h, ISS_ERR_IO, "can not open %s", filename);
+    std::string line;
+    while (std::getline(header, line)) std::fprintf(f, "%s\n", line.c_str());
+    const int E = h->n_events;
+    const std::vector<int64_t>& off = h->event_offsets;
+    std::vector<int64_t> ev_byte(static_cast<size_t>(E) + 1, 0);
+    for (int e = 0; e < E; e++) {
+        const int64_t n = off[e + 1] - off[e];
+        ev_byte[e + 1] = ev_byte[e] + (n > 0 ? kOscarSubHeader + n * kOscarLine : 0);
+    }
+    const int64_t kChunk = int64_t(256) << 20;
+    DevBuf<int64_t> d_off, d_byte;
+    DevBuf<char> d_text[2];
+    char* host[2] = {nullptr, nullptr};
+    cudaStream_t s = h->stream;
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    iss_status st = ISS_OK;
+    auto cleanup = [&]() {
+        for (int k = 0; k < 2; k++) {
+            if (done[k]) cudaEventDestroy(done[k]);
+            if (host[k]) cudaFreeHost(host[k]);
+            d_text[k].release();
+        }
+        d_off.release();
+        d_byte.release();
+        std::fclose(f);
+    };
+#define OSCAR_TRY(x)                                                                   \
+    do {                                                                               \
+        const cudaError_t e_ = (x);                                                    \
+        if (e_ != cudaSuccess) {                                                       \
+            cleanup();                                                                 \
+            return fail(h, ISS_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));        \
+        }                                                                              \
+    } while (0)
+    // chunks: runs of whole events of at most kChunk bytes (an event larger
+    // than that is a chunk by itself)
+    std::vector<std::pair<int, int>> chunks;
+    int64_t max_bytes = 0;
+    for (int e = 0; e < E;) {
+        int e1 = e + 1;
+        while (e1 < E && ev_byte[e1 + 1] - ev_byte[e] <= kChunk) e1++;
+        chunks.push_back({e, e1});
+        max_bytes = std::max(max_bytes, ev_byte[e1] - ev_byte[e]);
+        e = e1;
+    }
+    OSCAR_TRY(d_off.reserve(off.size()));
+    OSCAR_TRY(d_byte.reserve(ev_byte.size()));
+    OSCAR_TRY(cudaMemcpyAsync(d_off.ptr, off.data(), 8 * off.size(), cudaMemcpyHostToDevice, s));
+    OSCAR_TRY(cudaMemcpyAsync(d_byte.ptr, ev_byte.data(), 8 * ev_byte.size(), cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < 2 && k < static_cast<int>(chunks.size()); k++) {
+        OSCAR_TRY(d_text[k].reserve(static_cast<size_t>(std::max<int64_t>(max_bytes, 1))));
+        OSCAR_TRY(cudaHostAlloc(reinterpret_cast<void**>(&host[k]),
+                                static_cast<size_t>(std::max<int64_t>(max_bytes, 1)), cudaHostAllocDefault));
+        OSCAR_TRY(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+    }
+    auto enqueue = [&](size_t c) -> cudaError_t {
+        const int k = static_cast<int>(c & 1);
+        const int ea = chunks[c].first, eb = chunks[c].second;
+        const int64_t bytes = ev_byte[eb] - ev_byte[ea];
+        cudaError_t e = launch_oscar_lines(h->d_hadrons.ptr, off[ea], off[eb], d_off.ptr, d_byte.ptr,
+                                           ea, eb, ev_byte[ea], d_text[k].ptr, h->num_sms, s);
+        if (e != cudaSuccess) return e;
+        if (bytes > 0) e = cudaMemcpyAsync(host[k], d_text[k].ptr, static_cast<size_t>(bytes),
+                                           cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+        return cudaEventRecord(done[k], s);
+    };
+    if (!chunks.empty()) OSCAR_TRY(enqueue(0));
+    for (size_t c = 0; c < chunks.size(); c++) {
+        // chunk c + 1 is formatted while chunk c is written; chunk c + 1 uses
+        // the other buffer, which chunk c - 1 released when it was written
+        if (c + 1 < chunks.size()) OSCAR_TRY(enqueue(c + 1));
+        const int k = static_cast<int>(c & 1);
+        OSCAR_TRY(cudaEventSynchronize(done[k]));
+        const int64_t bytes = ev_byte[chunks[c].second] - ev_byte[chunks[c].first];
+        if (bytes > 0 && std::fwrite(host[k], 1, static_cast<size_t>(bytes), f) != static_cast<size_t>(bytes)) {
+            cleanup();
+            return fail(h, ISS_ERR_IO, "write error on %s", filename);
+        }
+    }
+#undef OSCAR_TRY
+    cleanup();
+    return st;
+}
+
 }  // namespace
 
 static_assert(sizeof(iss_hadron_t) == 40, "iss_hadron_t must be 40 bytes");
@@ -988,6 +1083,9 @@ iss_status iss_gpu_copy_all(iss_handle* h, iss_hadron_t* out, int64_t capacity,
 
 iss_status iss_gpu_write_output(iss_handle* h, int format, const char* filename) {
     if (!h) return ISS_ERR_INVALID_ARG;
+    if (format == ISS_OUTPUT_OSCAR && h->samples_valid && h->cuda_ready &&
+        h->params.get_or("gpu_oscar_on_host", 0) == 0)
+        return write_oscar_gpu(h, filename ? filename : "OSCAR.DAT");
     iss_status st = ensure_host_copy(h);
     if (st != ISS_OK) return st;
     std::string err;

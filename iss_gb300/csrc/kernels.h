@@ -49,4 +49,15 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                            unsigned long long* work_counter, SampleCounters* counters, int num_sms,
                            cudaStream_t stream);
 
+// kernels_output.cu: OSCAR text (FSSW::combine_samples_to_OSCAR) of hadrons
+// [h0, h1), which are the whole events [e_lo, e_hi).  ev_off: the events'
+// first hadrons (n_events + 1 entries); ev_byte: the byte offset of each
+// event's block in the file body (sub-header, then its lines).  Writes to
+// out + ev_byte[e] - byte0.
+constexpr int kOscarSubHeader = 43;   // setw(10) iev, setw(10) n, two setw(8) zeros
+constexpr int kOscarLine = 257;       // setw(10) ipart, setw(10) pid, nine %24.16e
+cudaError_t launch_oscar_lines(const HadronRec* had, int64_t h0, int64_t h1, const int64_t* ev_off,
+                               const int64_t* ev_byte, int e_lo, int e_hi, int64_t byte0,
+                               char* out, int num_sms, cudaStream_t stream);
+
 }  // namespace iss

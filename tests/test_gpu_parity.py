@@ -205,3 +205,26 @@ def test_surface_batch_matches_single_surface_runs():
         assert np.array_equal(off[e0:e0 + ne + 1] - off[e0], offb)
         assert np.array_equal(rows[b * nsp:(b + 1) * nsp], t.species_yields())
         e0 += ne
+
+
+@pytest.mark.parametrize("cells,events", [(4, 60), (256, 200)])
+def test_oscar_text_from_gpu_equals_host_printf(tmp_path, cells, events):
+    """iss_gpu_write_output(OSCAR) formats the records on the GPU; the file is
+    byte-identical to the host writer's printf("%24.16e") output, empty
+    events included (a 4-cell surface leaves many events without hadrons)."""
+    surf = S.viscous_3d(cells, seed=41)
+    params = dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=0,
+                  include_deltaf_shear=1, include_deltaf_bulk=1, bulk_deltaf_kind=11,
+                  turn_on_bulk=1, number_of_repeated_sampling=events)
+    s = iSS(".", inputfile="")
+    s.set_params(**params)
+    s.set_surface(surf.fo_surf())
+    s.set_random_seed(77)
+    s.generate_samples()
+    a, b = tmp_path / "gpu.dat", tmp_path / "host.dat"
+    s.write_output(native.OUTPUT_OSCAR, str(a))
+    s.setVal("gpu_oscar_on_host", 1)
+    s.write_output(native.OUTPUT_OSCAR, str(b))
+    ta, tb = a.read_bytes(), b.read_bytes()
+    assert len(ta) > 1000
+    assert ta == tb
