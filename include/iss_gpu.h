@@ -72,7 +72,8 @@ typedef struct iss_timings {
     int64_t n_tries;      /* proposals made by the sampler                            */
     int64_t n_cell_redraws;  /* cells redrawn after the try cap (src/FSSW.cpp:1017-1021) */
     int64_t n_failures;   /* hadrons abandoned after the redraw cap (never expected)  */
-    int32_t kernel_launches; /* kernels launched by the last iss_gpu_generate          */
+    int32_t kernel_launches; /* kernels launched by the last iss_gpu_generate (without decays) */
+    double ms_decays;     /* resonance decays (perform_decays = 1), not in ms_total   */
 } iss_timings_t;
 
 /* ---- construction, parameters ------------------------------------------ */

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INCLUDES = [f"-I{CSRC}", f"-I{os.path.join(REPO, 'include')}", f"-I{CUDA_HOME}/include"]
 
 CU_SOURCES = ["kernels_prologue.cu", "kernels_cells.cu", "kernels_sample.cu", "kernels_output.cu",
-              "noalloc_scan.cu"]
+              "kernels_decay.cu", "noalloc_scan.cu"]
 # the prologue reproduces the reference's float/double rounding points exactly,
 # so mul+add must not be contracted into FMAs there
 CU_EXTRA = {"kernels_prologue.cu": ["--fmad=false"],

@@ -80,6 +80,14 @@ struct iss_handle {
     std::vector<int32_t> batch_events;    // events per surface
     std::vector<SurfSeg> segs;            // per-surface layout of the CDF rows
     std::vector<int32_t> ev_surf;         // surface of every event (host copy of d_ev_surf)
+    // resonance decays (perform_decays = 1, not for the SMASH afterburner)
+    bool decays = false;
+    int decay_table_afterburner = -1;
+    DevBuf<DecayParticle> d_dparticles;
+    DevBuf<DecayChannel> d_dchannels;
+    DevBuf<int32_t> d_dsorted;            // sorted pids, then their indices
+    int n_decay_particles = 0;
+    cudaEvent_t ev_decay[2] = {nullptr, nullptr};
     int64_t cdf_len = 0, guide_len = 0, n_tiles = 0;
     int hydro_mode = 2;
     int iEOS = 2;
@@ -166,6 +174,11 @@ struct iss_handle {
                 if (e) cudaEventDestroy(e);
             for (auto& e : chunk_ev)
                 if (e) cudaEventDestroy(e);
+            for (auto& e : ev_decay)
+                if (e) cudaEventDestroy(e);
+            d_dparticles.release();
+            d_dchannels.release();
+            d_dsorted.release();
             if (copy_stream) cudaStreamDestroy(copy_stream);
             if (stream) cudaStreamDestroy(stream);
         }
@@ -273,8 +286,8 @@ iss_status prepare(iss_handle* h) {
     c.y_lb = static_cast<float>(vals[10]);
     c.y_rb = static_cast<float>(vals[11]);
     c.ymult = (c.hydro_mode != 2) ? (vals[11] - vals[10]) : 1.0;
-    if (h->params.get_or("perform_decays", 0) == 1 && h->afterburner != 2)
-        return fail(h, ISS_ERR_UNSUPPORTED, "perform_decays = 1 is not supported");
+    // the reference decays unless SMASH is the afterburner (src/FSSW.cpp:346-348)
+    h->decays = h->params.get_or("perform_decays", 0) == 1 && h->afterburner != 2;
     if (h->params.get_or("include_spectators", 0) != 0)
         return fail(h, ISS_ERR_UNSUPPORTED, "include_spectators is not supported");
     if (c.n_events < 0) return fail(h, ISS_ERR_INVALID_ARG, "negative number of events");
@@ -489,6 +502,179 @@ float elapsed(iss_handle* h, int a, int b) {
     return ms;
 }
 
+// Resonance decays of the sampled records, generation by generation over
+// all events (kernels_decay.cu); replaces d_hadrons and the event offsets
+// with the final-state lists.
+constexpr int kMaxDecayGenerations = 64;
+
+iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
+    DevConfig& c = h->cfg;
+    cudaStream_t s = h->stream;
+    const int E = c.n_events;
+    if (h->decay_table_afterburner != h->afterburner) {
+        DecayTable tab;
+        std::string err;
+        if (!load_decay_table(h->particle_table_path, h->afterburner, &tab, &err))
+            return fail(h, ISS_ERR_IO, "%s", err.c_str());
+        const int n = static_cast<int>(tab.particles.size());
+        std::vector<std::pair<int32_t, int32_t>> by_pid;
+        for (int i = 0; i < n; i++) by_pid.push_back({tab.particles[i].pid, i});
+        // first entry of a repeated pid wins, as in the reference's lookups
+        std::stable_sort(by_pid.begin(), by_pid.end(),
+                         [](const std::pair<int32_t, int32_t>& a, const std::pair<int32_t, int32_t>& b) {
+                             return a.first < b.first;
+                         });
+        by_pid.erase(std::unique(by_pid.begin(), by_pid.end(),
+                                 [](const std::pair<int32_t, int32_t>& a,
+                                    const std::pair<int32_t, int32_t>& b) { return a.first == b.first; }),
+                     by_pid.end());
+        std::vector<int32_t> sorted(2 * by_pid.size());
+        for (size_t i = 0; i < by_pid.size(); i++) {
+            sorted[i] = by_pid[i].first;
+            sorted[by_pid.size() + i] = by_pid[i].second;
+        }
+        CUDA_TRY(h, h->d_dparticles.reserve(tab.particles.size()));
+        CUDA_TRY(h, h->d_dchannels.reserve(std::max<size_t>(tab.channels.size(), 1)));
+        CUDA_TRY(h, h->d_dsorted.reserve(sorted.size()));
+        CUDA_TRY(h, cudaMemcpy(h->d_dparticles.ptr, tab.particles.data(),
+                               sizeof(DecayParticle) * tab.particles.size(), cudaMemcpyHostToDevice));
+        if (!tab.channels.empty())
+            CUDA_TRY(h, cudaMemcpy(h->d_dchannels.ptr, tab.channels.data(),
+                                   sizeof(DecayChannel) * tab.channels.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(h, cudaMemcpy(h->d_dsorted.ptr, sorted.data(), 4 * sorted.size(),
+                               cudaMemcpyHostToDevice));
+        h->n_decay_particles = static_cast<int>(by_pid.size());
+        h->decay_table_afterburner = h->afterburner;
+    }
+    DecayTablesDev t;
+    t.particles = h->d_dparticles.ptr;
+    t.channels = h->d_dchannels.ptr;
+    t.sorted_pid = h->d_dsorted.ptr;
+    t.sorted_idx = h->d_dsorted.ptr + h->n_decay_particles;
+    t.n_particles = h->n_decay_particles;
+
+    // every buffer of this function is released on every return
+    std::vector<DevBuf<HadronRec>> out_s;     // stable products of each generation
+    std::vector<DevBuf<int32_t>> out_ev;
+    std::vector<int64_t> out_n;
+    DevBuf<HadronRec> cur, nxt;
+    DevBuf<int32_t> cur_ev, nxt_ev, ns, nu;
+    DevBuf<int64_t> first, last, s_off, u_off, tiles, evoff, base;
+    DevBuf<unsigned long long> fails;
+    DevBuf<HadronRec> final_buf;
+    auto release = [&]() {
+        for (auto& b : out_s) b.release();
+        for (auto& b : out_ev) b.release();
+        cur.release(); nxt.release(); cur_ev.release(); nxt_ev.release(); ns.release(); nu.release();
+        first.release(); last.release(); s_off.release(); u_off.release(); tiles.release();
+        evoff.release(); base.release(); fails.release(); final_buf.release();
+    };
+#define DECAY_TRY(x)                                                                   \
+    do {                                                                               \
+        const cudaError_t e_ = (x);                                                    \
+        if (e_ != cudaSuccess) {                                                       \
+            release();                                                                 \
+            return fail(h, ISS_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));        \
+        }                                                                              \
+    } while (0)
+    int64_t n = h->n_hadrons;
+    DECAY_TRY(evoff.reserve(static_cast<size_t>(E) + 1));
+    DECAY_TRY(cudaMemcpyAsync(evoff.ptr, h->event_offsets.data(), 8 * (static_cast<size_t>(E) + 1),
+                              cudaMemcpyHostToDevice, s));
+    DECAY_TRY(first.reserve(std::max(E, 1)));
+    DECAY_TRY(last.reserve(std::max(E, 1)));
+    DECAY_TRY(fails.reserve(1));
+    DECAY_TRY(cudaMemsetAsync(fails.ptr, 0, sizeof(unsigned long long), s));
+    // generation 0: the sampled records (moved out of d_hadrons)
+    std::swap(cur.ptr, h->d_hadrons.ptr);
+    std::swap(cur.cap, h->d_hadrons.cap);
+    DECAY_TRY(cur_ev.reserve(static_cast<size_t>(std::max<int64_t>(n, 1))));
+    DECAY_TRY(launch_event_ids(evoff.ptr, E, cur_ev.ptr, s));
+    int gen = 0;
+    for (; n > 0 && gen < kMaxDecayGenerations; gen++) {
+        DECAY_TRY(launch_event_bounds(cur_ev.ptr, n, E, first.ptr, last.ptr, s));
+        DECAY_TRY(ns.reserve(static_cast<size_t>(n)));
+        DECAY_TRY(nu.reserve(static_cast<size_t>(n)));
+        DECAY_TRY(launch_decay_count(c, t, static_cast<uint32_t>(gen), cur.ptr, cur_ev.ptr, first.ptr,
+                                     n, ns.ptr, nu.ptr, s));
+        DECAY_TRY(s_off.reserve(static_cast<size_t>(n) + 1));
+        DECAY_TRY(u_off.reserve(static_cast<size_t>(n) + 1));
+        DECAY_TRY(tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(n), 1))));
+        DECAY_TRY(launch_offsets_scan(ns.ptr, n, tiles.ptr, s_off.ptr, s));
+        DECAY_TRY(launch_offsets_scan(nu.ptr, n, tiles.ptr, u_off.ptr, s));
+        int64_t tot[2] = {0, 0};
+        DECAY_TRY(cudaMemcpyAsync(&tot[0], s_off.ptr + n, 8, cudaMemcpyDeviceToHost, s));
+        DECAY_TRY(cudaMemcpyAsync(&tot[1], u_off.ptr + n, 8, cudaMemcpyDeviceToHost, s));
+        DECAY_TRY(cudaStreamSynchronize(s));
+        out_s.emplace_back();
+        out_ev.emplace_back();
+        out_n.push_back(tot[0]);
+        DECAY_TRY(out_s.back().reserve(static_cast<size_t>(std::max<int64_t>(tot[0], 1))));
+        DECAY_TRY(out_ev.back().reserve(static_cast<size_t>(std::max<int64_t>(tot[0], 1))));
+        DECAY_TRY(nxt.reserve(static_cast<size_t>(std::max<int64_t>(tot[1], 1))));
+        DECAY_TRY(nxt_ev.reserve(static_cast<size_t>(std::max<int64_t>(tot[1], 1))));
+        DECAY_TRY(launch_decay_write(c, t, static_cast<uint32_t>(gen), cur.ptr, cur_ev.ptr, first.ptr,
+                                     n, s_off.ptr, u_off.ptr, out_s.back().ptr, out_ev.back().ptr,
+                                     nxt.ptr, nxt_ev.ptr, fails.ptr, s));
+        std::swap(cur, nxt);
+        std::swap(cur_ev, nxt_ev);
+        n = tot[1];
+    }
+    if (n > 0) {
+        release();
+        return fail(h, ISS_ERR_SAMPLING, "decay chains longer than %d generations",
+                    kMaxDecayGenerations);
+    }
+    // final lists: event e = its generation-0 products, then generation 1, ...
+    const int G = static_cast<int>(out_n.size());
+    std::vector<int64_t> cnt(static_cast<size_t>(G) * E, 0);
+    std::vector<int64_t> firsts(static_cast<size_t>(G) * E, 0);
+    std::vector<int64_t> fb(static_cast<size_t>(E)), lb(static_cast<size_t>(E));
+    for (int g = 0; g < G; g++) {
+        DECAY_TRY(launch_event_bounds(out_ev[g].ptr, out_n[g], E, first.ptr, last.ptr, s));
+        DECAY_TRY(cudaMemcpyAsync(fb.data(), first.ptr, 8 * static_cast<size_t>(E), cudaMemcpyDeviceToHost, s));
+        DECAY_TRY(cudaMemcpyAsync(lb.data(), last.ptr, 8 * static_cast<size_t>(E), cudaMemcpyDeviceToHost, s));
+        DECAY_TRY(cudaStreamSynchronize(s));
+        for (int e = 0; e < E; e++) {
+            cnt[static_cast<size_t>(g) * E + e] = fb[e] >= 0 ? lb[e] - fb[e] : 0;
+            firsts[static_cast<size_t>(g) * E + e] = fb[e];
+        }
+    }
+    std::vector<int64_t> off(static_cast<size_t>(E) + 1, 0);
+    for (int e = 0; e < E; e++) {
+        int64_t k = 0;
+        for (int g = 0; g < G; g++) k += cnt[static_cast<size_t>(g) * E + e];
+        off[e + 1] = off[e] + k;
+    }
+    const int64_t total = off[E];
+    DECAY_TRY(final_buf.reserve(static_cast<size_t>(std::max<int64_t>(total, 1))));
+    DECAY_TRY(base.reserve(static_cast<size_t>(std::max(E, 1))));
+    std::vector<int64_t> bg(static_cast<size_t>(E));
+    std::vector<int64_t> acc(off.begin(), off.end() - 1);
+    for (int g = 0; g < G; g++) {
+        for (int e = 0; e < E; e++) {
+            bg[e] = acc[e];
+            acc[e] += cnt[static_cast<size_t>(g) * E + e];
+            fb[e] = firsts[static_cast<size_t>(g) * E + e];
+        }
+        DECAY_TRY(cudaMemcpyAsync(base.ptr, bg.data(), 8 * static_cast<size_t>(E), cudaMemcpyHostToDevice, s));
+        DECAY_TRY(cudaMemcpyAsync(first.ptr, fb.data(), 8 * static_cast<size_t>(E), cudaMemcpyHostToDevice, s));
+        DECAY_TRY(launch_gather(out_s[g].ptr, out_ev[g].ptr, first.ptr, base.ptr, out_n[g],
+                                final_buf.ptr, s));
+        DECAY_TRY(cudaStreamSynchronize(s));   // bg and fb are reused
+    }
+    unsigned long long nf = 0;
+    DECAY_TRY(cudaMemcpy(&nf, fails.ptr, sizeof(nf), cudaMemcpyDeviceToHost));
+    *failures_out = nf;
+    std::swap(final_buf.ptr, h->d_hadrons.ptr);
+    std::swap(final_buf.cap, h->d_hadrons.cap);
+    h->event_offsets = off;
+    h->n_hadrons = total;
+#undef DECAY_TRY
+    release();
+    return ISS_OK;
+}
+
 // host_out != nullptr: iss_gpu_generate_into -- the sampler runs in chunks of
 // consecutive events and each chunk's records are copied to host_out on a
 // second stream while the next chunk is sampled.
@@ -550,7 +736,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, h->d_off_tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(nseg), 1))));
     // sampling chunks: one without a host destination, else up to kMaxChunks
     const int E = c.n_events;
-    int n_chunks = host_out ? std::min(kMaxChunks, std::max(E, 1)) : 1;
+    int n_chunks = (host_out && !h->decays) ? std::min(kMaxChunks, std::max(E, 1)) : 1;
     c.chunk_events = std::max(1, (E + n_chunks - 1) / n_chunks);
     n_chunks = std::max(1, (E + c.chunk_events - 1) / c.chunk_events);
     CUDA_TRY(h, h->d_error.reserve(1));
@@ -594,7 +780,8 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
 
-    const bool to_host = host_out != nullptr && n_units <= capacity && n_units > 0;
+    // with decays the records change after sampling: no copies during it
+    const bool to_host = host_out != nullptr && n_units <= capacity && n_units > 0 && !h->decays;
     if (to_host) {
         if (!h->copy_stream)
             CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
@@ -638,20 +825,40 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     }
     CUDA_TRY(h, cudaGetLastError());
 
+    h->n_events = c.n_events;
+    h->n_hadrons = n_units;
+    unsigned long long decay_failures = 0;
+    float ms_decays = 0.f;
+    if (h->decays) {
+        for (auto& e : h->ev_decay)
+            if (!e) CUDA_TRY(h, cudaEventCreate(&e));
+        CUDA_TRY(h, cudaEventRecord(h->ev_decay[0], s));
+        const iss_status dst = run_decays(h, &decay_failures);
+        if (dst != ISS_OK) return dst;
+        CUDA_TRY(h, cudaEventRecord(h->ev_decay[1], s));
+        CUDA_TRY(h, cudaEventSynchronize(h->ev_decay[1]));
+        cudaEventElapsedTime(&ms_decays, h->ev_decay[0], h->ev_decay[1]);
+        if (host_out && h->n_hadrons <= capacity && h->n_hadrons > 0) {
+            CUDA_TRY(h, cudaMemcpy(host_out, h->d_hadrons.ptr,
+                                   sizeof(iss_hadron_t) * static_cast<size_t>(h->n_hadrons),
+                                   cudaMemcpyDeviceToHost));
+            if (copied) *copied = true;
+        }
+    }
+
     iss_timings_t& t = h->timings;
+    t.ms_decays = ms_decays;
     t.ms_prologue = elapsed(h, kEvStart, kEvPrologue);
     t.ms_yields = elapsed(h, kEvPrologue, kEvYields);
     t.ms_cdf = elapsed(h, kEvYields, kEvCdf);
     t.ms_counts = elapsed(h, kEvCdf, kEvCounts);
     t.ms_sample = elapsed(h, kEvSampleStart, kEvSample);
     t.ms_total = elapsed(h, kEvStart, kEvSample);
-    t.n_hadrons = n_units;
+    t.n_hadrons = h->n_hadrons;
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
-    t.n_failures = static_cast<int64_t>(ctr.failures);
+    t.n_failures = static_cast<int64_t>(ctr.failures + decay_failures);
     t.kernel_launches = 15 + 2 * n_chunks;
-    h->n_events = c.n_events;
-    h->n_hadrons = n_units;
     h->samples_valid = true;
     if (ctr.error_code == 1) {
         const int k = ctr.error_species;

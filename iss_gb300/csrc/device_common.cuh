@@ -83,6 +83,27 @@ struct CellArrays {
     float4* coef;   // per-cell delta-f coefficients vis0, vis1, vis2, kappa_B
 };
 
+// Resonance decay table (particle_decay::read_resonances_list): particles
+// in pdg-file order with their channels; daughters are particle indices.
+struct DecayParticle {
+    int32_t pid;
+    float mass, width;
+    int32_t stable;
+    int32_t first_channel, n_channels;
+};
+struct DecayChannel {
+    int32_t n_daughters;
+    double branching_ratio;
+    int32_t daughter[5];
+};
+struct DecayTablesDev {
+    const DecayParticle* particles;
+    const DecayChannel* channels;
+    const int32_t* sorted_pid;   // pids in increasing order ...
+    const int32_t* sorted_idx;   // ... and their particle indices
+    int n_particles;
+};
+
 // Counters written by the sampler.
 struct SampleCounters {
     unsigned long long tries;

@@ -63,6 +63,95 @@ bool load_resonances(const std::string& particle_table_path, int afterburner,
     return true;
 }
 
+bool load_decay_table(const std::string& particle_table_path, int afterburner, DecayTable* out,
+                      std::string* err) {
+    const std::string fn = particle_table_path + "/" + pdg_file(afterburner);
+    std::ifstream f(fn);
+    if (!f) {
+        *err = "can not find pdg file " + fn;
+        return false;
+    }
+    struct Raw {
+        int32_t pid, baryon, strange, charge;
+        double mass, width;
+        std::vector<DecayChannel> ch;
+    };
+    std::vector<Raw> raw;
+    auto find = [&](int32_t pid) -> int {
+        for (size_t i = 0; i < raw.size(); i++)
+            if (raw[i].pid == pid) return static_cast<int>(i);
+        return -1;
+    };
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream ss(line);
+        Raw r;
+        std::string name;
+        int gspin, charm, bottom, giso, ndecays;
+        if (!(ss >> r.pid >> name >> r.mass >> r.width >> gspin >> r.baryon >> r.strange >> charm >>
+              bottom >> giso >> r.charge >> ndecays)) {
+            continue;
+        }
+        for (int j = 0; j < ndecays && std::getline(f, line); j++) {
+            std::istringstream cs(line);
+            int dummy;
+            DecayChannel c{};
+            if (!(cs >> dummy >> c.n_daughters >> c.branching_ratio >> c.daughter[0] >> c.daughter[1] >>
+                  c.daughter[2] >> c.daughter[3] >> c.daughter[4])) {
+                *err = "bad decay channel line in " + fn;
+                return false;
+            }
+            r.ch.push_back(c);
+        }
+        raw.push_back(r);
+        if (r.baryon == 1) {
+            Raw a = r;
+            a.pid = -r.pid;
+            a.baryon = -r.baryon;
+            a.strange = -r.strange;
+            a.charge = -r.charge;
+            for (DecayChannel& c : a.ch) {
+                for (int k = 0; k < 5; k++) {
+                    const int32_t d = c.daughter[k];
+                    if (d == 0) continue;
+                    const int idx = find(d);
+                    // neutral, non-strange mesons are their own antiparticles
+                    // (src/particle_decay.cpp:139-147); unknown daughters keep
+                    // their sign
+                    if (idx >= 0 && raw[idx].baryon == 0 && raw[idx].charge == 0 &&
+                        raw[idx].strange == 0)
+                        c.daughter[k] = d;
+                    else
+                        c.daughter[k] = -d;
+                }
+            }
+            raw.push_back(a);
+        }
+    }
+    out->particles.clear();
+    out->channels.clear();
+    for (const Raw& r : raw) {
+        DecayParticle p{};
+        p.pid = r.pid;
+        p.mass = static_cast<float>(r.mass);
+        p.width = static_cast<float>(r.width);
+        p.stable = (!r.ch.empty() && r.ch[0].n_daughters == 1) ? 1 : 0;
+        p.first_channel = static_cast<int32_t>(out->channels.size());
+        p.n_channels = static_cast<int32_t>(r.ch.size());
+        out->particles.push_back(p);
+        for (DecayChannel c : r.ch) out->channels.push_back(c);
+    }
+    // daughters as indices (the first entry with that pid, as
+    // particle_decay::get_particle_mass looks it up)
+    for (DecayChannel& c : out->channels) {
+        for (int k = 0; k < 5; k++) {
+            const int32_t d = c.daughter[k];
+            c.daughter[k] = (k < c.n_daughters && d != 0) ? find(d) : -1;
+        }
+    }
+    return true;
+}
+
 bool load_chosen_species(const std::string& particle_table_path, int afterburner,
                          bool quantum_statistics, std::vector<Species>* out,
                          std::vector<int32_t>* unidentified, std::string* err) {

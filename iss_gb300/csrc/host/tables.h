@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include "device_common.cuh"
+
 namespace iss {
 
 struct Species {
@@ -24,6 +26,19 @@ struct Species {
 bool load_chosen_species(const std::string& particle_table_path, int afterburner,
                          bool quantum_statistics, std::vector<Species>* out,
                          std::vector<int32_t>* unidentified, std::string* err);
+
+// Resonance decay table of particle_decay::read_resonances_list
+// (src/particle_decay.cpp:33-170): every entry of the pdg file, each baryon
+// followed by its anti-baryon, whose channels negate every daughter that is
+// not a neutral, non-strange meson (looked up among the entries read so far).
+// stable = the first channel has one daughter.  Daughters are indices into
+// `particles` (-1 when the pid is not in the table).
+struct DecayTable {
+    std::vector<DecayParticle> particles;
+    std::vector<DecayChannel> channels;
+};
+bool load_decay_table(const std::string& particle_table_path, int afterburner, DecayTable* out,
+                      std::string* err);
 
 // Full resonance list (for quantum-number lookups).
 bool load_resonances(const std::string& particle_table_path, int afterburner,

@@ -49,6 +49,24 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                            unsigned long long* work_counter, SampleCounters* counters, int num_sms,
                            cudaStream_t stream);
 
+// kernels_decay.cu: one generation of resonance decays over all events
+// (event-sorted input with event ids; first[e] = index of event e's first
+// element), event ids from event offsets, event bounds of an event-sorted
+// array, and the final gather out[base[e] + i - first[e]] = in[i].
+cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cudaStream_t s);
+cudaError_t launch_event_bounds(const int32_t* ev, int64_t n, int n_events, int64_t* first,
+                                int64_t* last, cudaStream_t s);
+cudaError_t launch_decay_count(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                               const HadronRec* in, const int32_t* ev, const int64_t* first,
+                               int64_t n, int32_t* n_stable, int32_t* n_unstable, cudaStream_t s);
+cudaError_t launch_decay_write(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                               const HadronRec* in, const int32_t* ev, const int64_t* first,
+                               int64_t n, const int64_t* s_off, const int64_t* u_off,
+                               HadronRec* out_s, int32_t* ev_s, HadronRec* out_u, int32_t* ev_u,
+                               unsigned long long* failures, cudaStream_t s);
+cudaError_t launch_gather(const HadronRec* in, const int32_t* ev, const int64_t* first,
+                          const int64_t* base, int64_t n, HadronRec* out, cudaStream_t s);
+
 // kernels_output.cu: OSCAR text (FSSW::combine_samples_to_OSCAR) of hadrons
 // [h0, h1), which are the whole events [e_lo, e_hi).  ev_off: the events'
 // first hadrons (n_events + 1 entries); ev_byte: the byte offset of each

@@ -166,6 +166,13 @@ def lcc_case(visc_params, work_root):
                      randomSeed=14), work_root)
 
 
+def decays_case(visc_params, work_root):
+    """perform_decays = 1: final-state hadrons after the resonance decays."""
+    sample_case("viscous_decays", S.viscous_3d(256, seed=2),
+                dict(visc_params, perform_decays=1, number_of_repeated_sampling=20000,
+                     randomSeed=15), work_root)
+
+
 def main():
     import argparse
     ap = argparse.ArgumentParser()
@@ -175,9 +182,9 @@ def main():
     work_root = tempfile.mkdtemp(prefix="iss_golden_")
     visc_params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
                        include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1)
-    if only == "samples_viscous_lcc":
+    if only in ("samples_viscous_lcc", "samples_viscous_decays"):
         try:
-            lcc_case(visc_params, work_root)
+            (lcc_case if only == "samples_viscous_lcc" else decays_case)(visc_params, work_root)
         finally:
             shutil.rmtree(work_root, ignore_errors=True)
         return
@@ -212,6 +219,7 @@ def main():
                     dict(hydro_mode=1, afterburner_type=0, include_deltaf_shear=1,
                          number_of_repeated_sampling=1000, randomSeed=13), work_root)
         lcc_case(visc_params, work_root)
+        decays_case(visc_params, work_root)
     finally:
         shutil.rmtree(work_root, ignore_errors=True)
 

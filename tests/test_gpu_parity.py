@@ -228,3 +228,46 @@ def test_oscar_text_from_gpu_equals_host_printf(tmp_path, cells, events):
     ta, tb = a.read_bytes(), b.read_bytes()
     assert len(ta) > 1000
     assert ta == tb
+
+
+def _stable_pids(table):
+    """pids whose first decay channel has one daughter (the reference's
+    'stable'), anti-baryons included."""
+    out = set()
+    lines = open(os.path.join(S.TABLE_DIR, table)).read().split("\n")
+    i = 0
+    while i < len(lines):
+        f = lines[i].split()
+        i += 1
+        if len(f) < 12:
+            continue
+        pid, baryon, ndec = int(f[0]), int(f[5]), int(f[11])
+        chans = [lines[i + j].split() for j in range(ndec)]
+        i += ndec
+        if chans and int(chans[0][1]) == 1:
+            out.add(pid)
+            if baryon == 1:
+                out.add(-pid)
+    return out
+
+
+def test_resonance_decays_final_state():
+    """perform_decays = 1: every final hadron is stable; the same seed gives
+    the same primaries, whose energy the decays conserve (pole masses) except
+    where a 4- or 5-body channel leaves no product, as in the reference."""
+    g = O.load_golden("yields_viscous_14moment.npz")
+    a, _ = run_golden_case(g, n_events=300, seed=64)
+    b, _ = run_golden_case(g, n_events=300, seed=64, extra={"perform_decays": 1})
+    ha, oa = a.all_hadrons()
+    hb, ob = b.all_hadrons()
+    assert b.get_number_of_sampled_events() == 300
+    assert len(hb) > len(ha)
+    stable = _stable_pids("pdg-s95pv1.dat")
+    assert set(np.unique(hb["pid"]).tolist()) <= stable
+    ea = np.add.reduceat(ha["E"].astype(np.float64), oa[:-1]) if len(ha) else np.zeros(0)
+    eb = np.add.reduceat(hb["E"].astype(np.float64), ob[:-1]) if len(hb) else np.zeros(0)
+    rel = (eb - ea) / ea
+    assert np.all(rel < 2e-5), rel.max()
+    assert np.median(np.abs(rel)) < 2e-6
+    t = b.timings()
+    assert t["ms_decays"] > 0 and t["n_failures"] == 0

@@ -68,7 +68,8 @@ def observables(h):
 
 
 @pytest.mark.parametrize("name,events", [("static_viscous", 40000), ("viscous_14moment", 100000),
-                                         ("ideal_boost_invariant", 1000), ("viscous_lcc", 30000)])
+                                         ("ideal_boost_invariant", 1000), ("viscous_lcc", 30000),
+                                         ("viscous_decays", 20000)])
 def test_spectra_match_reference_samples(name, events):
     g, s = sample_case(name, events, seed=4242)
     had, off = s.all_hadrons()
