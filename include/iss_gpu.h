@@ -155,7 +155,7 @@ iss_status iss_gpu_generate(iss_handle* h);
 
 /* iSS::generate_samples followed by reading every event's hadron list
  * (get_hadron_list_iev for iev = 0 .. n_events-1, src/iSS.h:85-91) in one call.
- *   - The sampler runs in up to 8 chunks of consecutive events.
+ *   - The sampler runs in up to 16 chunks of consecutive events.
  *   - Each chunk's records are copied into out[0 .. n_total) while the next
  *     chunk is sampled.
  *   - `out` should be page-locked (cudaHostAlloc or cudaHostRegister). Then

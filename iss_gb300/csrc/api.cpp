@@ -678,7 +678,7 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
 // host_out != nullptr: iss_gpu_generate_into -- the sampler runs in chunks of
 // consecutive events and each chunk's records are copied to host_out on a
 // second stream while the next chunk is sampled.
-constexpr int kMaxChunks = 8;
+constexpr int kMaxChunks = 16;
 
 iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
                         bool* copied = nullptr) {
