@@ -276,6 +276,8 @@ def run_gpu(args, ws, rank, local):
     params = dict(S.DEFAULT_PARAMETERS, **wl["params"])
     params["number_of_repeated_sampling"] = n_events
     params["gpu_event_offset"] = rank * n_events
+    if args.decays:
+        params["perform_decays"] = 1
     s = iSS(".", inputfile="")
     s.set_params(**params)
     if batch is not None:
@@ -309,7 +311,8 @@ def run_gpu(args, ws, rank, local):
         torch.cuda.synchronize()
         s.generate_samples()
         t = s.timings()
-        dev_ms.append(t["ms_total"])
+        # with --decays a step also includes the decays (and counts final hadrons)
+        dev_ms.append(t["ms_total"] + (t["ms_decays"] if args.decays else 0.0))
         hadrons.append(t["n_hadrons"])
         t_sample.append(t["ms_sample"])
         t_yields.append(t["ms_yields"])
@@ -321,6 +324,21 @@ def run_gpu(args, ws, rank, local):
     clk = clocks.stop()
     timings = s.timings()
     launches = args.steps * int(timings["kernel_launches"])
+    oscar = None
+    if args.oscar and rank == 0:
+        # OSCAR text of the last step (formatted on the GPU), written to a
+        # temporary file and removed
+        from iss_gb300 import native
+        d = tempfile.mkdtemp()
+        fn = os.path.join(d, "OSCAR.DAT")
+        t0 = time.perf_counter()
+        s.write_output(native.OUTPUT_OSCAR, fn)
+        dt = time.perf_counter() - t0
+        size = os.path.getsize(fn)
+        os.remove(fn)
+        os.rmdir(d)
+        oscar = {"seconds": dt, "bytes": size, "hadrons": timings["n_hadrons"],
+                 "hadrons_per_s": timings["n_hadrons"] / dt}
 
     # end-to-end steps through the C ABI with host buffers
     e2e = None
@@ -389,7 +407,8 @@ def run_gpu(args, ws, rank, local):
         achieved = nh * ALG_BYTES_PER_HADRON / samp_sec / 1e9
         traffic_per_h = profiled_traffic()
         per_launch_h = nh / args.steps
-        roofline = {"bound": "hbm", "kernel": "sampler_kernel", "achieved": achieved,
+        roofline = {"bound": "hbm", "kernel": "sample phase (cell_assign_kernel + sampler_kernel)",
+                    "achieved": achieved,
                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "peak_source": peak_kind,
                     "traffic": (traffic_per_h * per_launch_h) if traffic_per_h else None,
@@ -417,7 +436,7 @@ def run_gpu(args, ws, rank, local):
                            "species": wl["species"],
                            "delta_f": {k: v for k, v in wl["params"].items()
                                        if k.startswith("include_") or k == "bulk_deltaf_kind"},
-                           "sampler": "plain",
+                           "sampler": "plain", "decays": bool(args.decays),
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
                            "wall_s_timed": wall},
@@ -432,6 +451,11 @@ def run_gpu(args, ws, rank, local):
                 "hadrons_per_step": nh / args.steps,
                 "phase_ms_per_step": phases,
                 "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
+        if args.decays:
+            line["decays"] = {"ms_per_step": timings["ms_decays"],
+                              "final_hadrons_per_step": timings["n_hadrons"]}
+        if oscar:
+            line["oscar_writer"] = oscar
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -452,6 +476,10 @@ def main():
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--decays", action="store_true",
+                    help="perform_decays = 1 (resonance decays after sampling, timed apart)")
+    ap.add_argument("--oscar", action="store_true",
+                    help="time the OSCAR writer on the last step's hadrons")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.cells is None:

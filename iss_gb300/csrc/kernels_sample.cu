@@ -726,12 +726,50 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         const unsigned long long Q = qtot[b * cfg.n_species + s];
         const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
         const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
-        for (int64_t d = d_begin + lane; d < d_end; d += 32) {
-            const uint4 w = block(0u, static_cast<uint32_t>(d), eg, c3, cfg.key0, cfg.key1);
-            const unsigned long long r =
-                (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
-            cell_of[base + d * mult] = static_cast<int32_t>(sg.c0) + cell_search(row, sg.n, gd, sg.g, Q, r);
+        // an item has at most 64 draws: each lane takes two and issues both
+        // guide lookups before either search, so their latencies overlap
+        static_assert(kItem == 64, "two draws per lane");
+        const int64_t d0 = d_begin + lane, d1 = d0 + 32;
+        const bool v0 = d0 < d_end, v1 = d1 < d_end;
+        unsigned long long r0 = 0, r1 = 0;
+        if (v0) {
+            const uint4 w = block(0u, static_cast<uint32_t>(d0), eg, c3, cfg.key0, cfg.key1);
+            r0 = (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
         }
+        if (v1) {
+            const uint4 w = block(0u, static_cast<uint32_t>(d1), eg, c3, cfg.key0, cfg.key1);
+            r1 = (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
+        }
+        const int last = static_cast<int>(sg.n - 1);
+        const unsigned j0 = static_cast<unsigned>(r0 >> (64 - sg.g));
+        const unsigned j1 = static_cast<unsigned>(r1 >> (64 - sg.g));
+        int lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+        if (v0) {
+            lo0 = __ldg(gd + j0);
+            hi0 = __ldg(gd + j0 + 1);
+        }
+        if (v1) {
+            lo1 = __ldg(gd + j1);
+            hi1 = __ldg(gd + j1 + 1);
+        }
+        const unsigned long long q0 = __umul64hi(r0, Q), q1 = __umul64hi(r1, Q);
+        lo0 = min(max(lo0, 0), last);
+        hi0 = min(max(hi0, lo0), last);
+        lo1 = min(max(lo1, 0), last);
+        hi1 = min(max(hi1, lo1), last);
+        while (lo0 < hi0 || lo1 < hi1) {
+            const int m0 = (lo0 + hi0 + 1) >> 1, m1 = (lo1 + hi1 + 1) >> 1;
+            const unsigned long long c0 = lo0 < hi0 ? __ldg(row + m0) : 0ull;
+            const unsigned long long c1 = lo1 < hi1 ? __ldg(row + m1) : 0ull;
+            if (lo0 < hi0) {
+                if (c0 <= q0) lo0 = m0; else hi0 = m0 - 1;
+            }
+            if (lo1 < hi1) {
+                if (c1 <= q1) lo1 = m1; else hi1 = m1 - 1;
+            }
+        }
+        if (v0) cell_of[base + d0 * mult] = static_cast<int32_t>(sg.c0) + lo0;
+        if (v1) cell_of[base + d1 * mult] = static_cast<int32_t>(sg.c0) + lo1;
     }
 }
 

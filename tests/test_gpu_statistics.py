@@ -149,6 +149,12 @@ def test_momentum_magnitude_matches_analytic_spectrum():
         assert len(p) > 20000
         pv = gof_chi2(np.histogram(p, edges)[0], _expected_p(mass, T, sign, edges))
         assert pv > 1e-3, f"|p| of {pid} vs p^2 f(E): p = {pv:.2e}"
+        # unbinned: Kolmogorov-Smirnov against the analytic CDF of p^2 f(E)
+        grid = np.linspace(0.0, 40 * T, 4001)
+        cdf = np.concatenate([[0.0], np.cumsum(_expected_p(mass, T, sign, grid))])[:-1]
+        cdf = np.append(cdf, 1.0)[: grid.size]
+        ks = stats.kstest(p, lambda x: np.interp(x, grid, cdf)).pvalue
+        assert ks > 1e-3, f"|p| of {pid}: KS p = {ks:.2e}"
         # isotropy in the rest frame
         cth = h["pz"].astype(float) / np.maximum(p, 1e-12)
         assert stats.kstest(cth, "uniform", args=(-1, 2)).pvalue > 1e-3
