@@ -456,6 +456,7 @@ CellArrays cell_arrays(iss_handle* h) {
     a.pi1 = b + 5 * n;
     a.pi2 = b + 6 * n;
     a.coef = b + 7 * n;
+    a.rec = b + 8 * n;   // 128-byte records, 128-byte aligned
     return a;
 }
 
@@ -472,7 +473,7 @@ iss_status run_cells(iss_handle* h) {
                                     cudaMemcpyHostToDevice, st));
         h->surface_on_device = true;
     }
-    CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 8));
+    CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 16));   // 8 SoA arrays + the records
     CUDA_TRY(h, h->d_yields.reserve(static_cast<size_t>(n) * S));
     const size_t rows = static_cast<size_t>(c.n_surfaces) * S;
     CUDA_TRY(h, h->d_cdf.reserve(static_cast<size_t>(std::max<int64_t>(h->cdf_len, 1))));

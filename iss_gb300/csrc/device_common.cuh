@@ -81,6 +81,10 @@ struct CellArrays {
     float4* pi1;    // pi_xx, pi_xy, pi_xz, pi_yy (LRF)
     float4* pi2;    // pi_yz, q_x, q_y, q_z (LRF)
     float4* coef;   // per-cell delta-f coefficients vis0, vis1, vis2, kappa_B
+    // the same eight float4 per cell as one 128-byte record (pos, da, u, th,
+    // th2, pi1, pi2, coef): the sampler reads a random cell's record as one
+    // cache line instead of eight
+    float4* rec;
 };
 
 // Resonance decay table (particle_decay::read_resonances_list): particles

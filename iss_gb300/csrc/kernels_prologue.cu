@@ -200,13 +200,14 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
         pl[k] = acc;
     }
 
-    cells.pos[l] = make_float4(tau, xpt, ypt, eta);
-    cells.da[l] = make_float4(dl[0], -dl[1], -dl[2], -dl[3]);
-    cells.u[l] = make_float4(ut, ux, uy, uz);
-    cells.th[l] = make_float4(Tdec, s[16], s[17], s[18]);
-    cells.th2[l] = make_float4(Edec, Pdec, Bn, s[29]);
-    cells.pi1[l] = make_float4(pl[0], pl[1], pl[2], pl[3]);
-    cells.pi2[l] = make_float4(pl[4], ql[1], ql[2], ql[3]);
+    float4* rec = cells.rec + 8 * l;
+    rec[0] = cells.pos[l] = make_float4(tau, xpt, ypt, eta);
+    rec[1] = cells.da[l] = make_float4(dl[0], -dl[1], -dl[2], -dl[3]);
+    rec[2] = cells.u[l] = make_float4(ut, ux, uy, uz);
+    rec[3] = cells.th[l] = make_float4(Tdec, s[16], s[17], s[18]);
+    rec[4] = cells.th2[l] = make_float4(Edec, Pdec, Bn, s[29]);
+    rec[5] = cells.pi1[l] = make_float4(pl[0], pl[1], pl[2], pl[3]);
+    rec[6] = cells.pi2[l] = make_float4(pl[4], ql[1], ql[2], ql[3]);
 
     double c[3] = {0.0, 0.0, 0.0};
     double kappa = 1.0;
@@ -217,8 +218,8 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
         else if (cfg.bulk_kind == 1) bulk_rta_coeff(Tdec, c);
     }
     if (cfg.include_diff) kappa = qmu_coeff(cfg.tab.qmu, Tdec, s[16]);
-    cells.coef[l] = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]),
-                                static_cast<float>(c[2]), static_cast<float>(kappa));
+    rec[7] = cells.coef[l] = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]),
+                                         static_cast<float>(c[2]), static_cast<float>(kappa));
 }
 
 }  // namespace

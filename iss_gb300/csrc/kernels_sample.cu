@@ -429,12 +429,13 @@ __device__ __forceinline__ int cell_search(const unsigned long long* __restrict_
 // returns false when m/T - mu/T is outside the reference's momentum tables
 __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
                            int l, Prop& p) {
-    const float4 th = cells.th[l];
-    const float4 th2 = cells.th2[l];
-    const float4 pi1 = cells.pi1[l];
-    const float4 pi2 = cells.pi2[l];
-    const float4 cf = cells.coef[l];
-    const float4 da = cells.da[l];
+    const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
+    const float4 da = __ldg(rec + 1);
+    const float4 th = __ldg(rec + 3);
+    const float4 th2 = __ldg(rec + 4);
+    const float4 pi1 = __ldg(rec + 5);
+    const float4 pi2 = __ldg(rec + 6);
+    const float4 cf = __ldg(rec + 7);
     const float T = th.x;
     const float beta = 1.0f / T;
     const float m = sp.m_hi + sp.m_lo;
@@ -664,8 +665,9 @@ __device__ __forceinline__ void write_hadron(HadronRec* out, int64_t slot, int p
 
 __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& p, int l, int pid,
                      float4 pl, float u_rap, HadronRec* out, int64_t slot) {
-    const float4 u = cells.u[l];
-    const float4 pos = cells.pos[l];
+    const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
+    const float4 u = __ldg(rec + 2);
+    const float4 pos = __ldg(rec);
     const float pdu = pl.y * u.y + pl.z * u.z + pl.w * u.w;
     const float c = pdu / (u.x + 1.0f) + pl.x;
     const float lx = pl.y + c * u.y;
