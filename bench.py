@@ -117,25 +117,35 @@ def profiled_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms from before
+    the warm-up; stop() keeps the samples whose timestamps fall inside the
+    timed region (mark_begin / mark_end)."""
 
     def __init__(self, index=0):
         self.index = index
         self.proc = None
         self.file = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.file = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}",
-                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=self.file, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+
+    def mark_begin(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def stop(self):
         if self.proc is None:
@@ -147,25 +157,34 @@ class ClockSampler:
             self.proc.kill()
         self.file.flush()
         self.file.seek(0)
-        sm, mx, reasons = [], [], set()
+        import datetime
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.file.read().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 8:
+            if len(f) < 9:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[1]), float(f[2]),
+                             {n for n, v in zip(names, f[5:9]) if v.lower() == "active"}))
             except ValueError:
                 continue
-            for name, v in zip(names, f[4:8]):
-                if v.lower() == "active":
-                    reasons.add(name)
         os.unlink(self.file.name)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if self.t0 is not None and self.t0 <= r[0] <= self.t1]
+        window = "timed region"
+        if not inside:
+            # region shorter than the sampling gap: the samples around it
+            ts = [r[0] for r in rows]
+            mid = 0.5 * (self.t0 + self.t1) if self.t0 is not None else ts[-1]
+            inside = sorted(rows, key=lambda r: abs(r[0] - mid))[:2]
+            window = "nearest samples to the timed region"
+        reasons = set().union(*[r[3] for r in inside])
+        return {"sm_mhz": statistics.median([r[1] for r in inside]),
+                "sm_max_mhz": max(r[2] for r in inside), "reasons": sorted(reasons),
+                "samples": len(inside), "window": window}
 
 
 def dist_setup():
@@ -294,15 +313,18 @@ def run_gpu(args, ws, rank, local):
             import torch.distributed as dist
             dist.barrier()
 
+    # clocks: nvidia-smi is started before the warm-up so that it samples
+    # throughout the timed region
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         s.generate_samples()
     torch.cuda.synchronize()
 
     # device-timed steps
-    clocks = ClockSampler(local)
-    clocks.start()
     barrier()
     torch.cuda.synchronize()
+    clocks.mark_begin()
     dev_ms, hadrons, t_sample, t_yields = [], [], [], []
     phases = {k: 0.0 for k in ("ms_prologue", "ms_yields", "ms_cdf", "ms_counts", "ms_sample")}
     wall0 = time.perf_counter()
@@ -321,6 +343,7 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier()
     wall = time.perf_counter() - wall0
+    clocks.mark_end()
     clk = clocks.stop()
     timings = s.timings()
     launches = args.steps * int(timings["kernel_launches"])

@@ -271,3 +271,68 @@ def test_resonance_decays_final_state():
     assert np.median(np.abs(rel)) < 2e-6
     t = b.timings()
     assert t["ms_decays"] > 0 and t["n_failures"] == 0
+
+
+def _viscous_params(**kw):
+    return dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
+                include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1, **kw)
+
+
+def test_full_size_surface_properties():
+    """The 200,000-cell viscous surface (the benchmark's surface), 200 events:
+    size-independent properties of the output.  Every record has the mass
+    and PDG id of its (event, species) segment, is on shell, and sits on a
+    kept cell's transverse position; segment sizes are the counts; the mean
+    multiplicity of each abundant species matches its Poisson mean."""
+    surf = S.viscous_3d(200_000, seed=2)
+    fo = surf.fo_surf()
+    s = iSS(".", inputfile="")
+    s.set_params(**_viscous_params(number_of_repeated_sampling=200))
+    s.set_surface(fo)
+    s.set_random_seed(2026)
+    s.generate_samples()
+    had, off = s.all_hadrons()
+    cnt = s.counts()
+    nev, nsp = cnt.shape
+    assert nev == 200 and len(had) == cnt.sum() > 1_000_000
+    assert np.array_equal(np.diff(off), cnt.sum(1))
+    pids = s.species()
+    seg_pid = np.repeat(np.tile(pids, nev), cnt.ravel())
+    assert np.array_equal(had["pid"], seg_pid)
+    E, px, py, pz, m = (had[k].astype(np.float64) for k in ("E", "px", "py", "pz", "mass"))
+    assert np.allclose(E * E - px * px - py * py - pz * pz, m * m, rtol=0, atol=2e-3 * np.maximum(E, 1) ** 2)
+    lrf = s.lrf_cells()
+    kept = lrf[lrf[:, 4] >= 0]
+    xy = set(map(tuple, np.round(kept[:, 1:3].astype(np.float64), 4)))
+    pick = np.random.default_rng(0).choice(len(had), 5000, replace=False)
+    assert all((round(float(had["x"][i]), 4), round(float(had["y"][i]), 4)) in xy for i in pick)
+    tot = s.species_yields()
+    big = tot > 5
+    z = (cnt[:, big].mean(0) - tot[big]) / np.sqrt(tot[big] / nev)
+    assert np.all(np.abs(z) < 5), z
+
+
+def test_edge_case_surfaces():
+    """Every cell dropped (u.dsigma < 0), a single cell, and zero events:
+    no failure, and the expected empty or tiny outputs."""
+    params = _viscous_params(number_of_repeated_sampling=5)
+    s = iSS(".", inputfile="")
+    s.set_params(**params)
+    surf = S.viscous_3d(64, seed=3)
+    rec = surf.records.copy()
+    rec[:, 4:8] *= -1.0                       # dsigma against the flow: all dropped
+    s.set_surface(S.Surface(rec, hydro_mode=2, bulk=1).fo_surf())
+    s.set_random_seed(1)
+    s.generate_samples()
+    had, off = s.all_hadrons()
+    assert len(had) == 0 and np.all(off == 0) and s.get_number_of_sampled_events() == 5
+    assert np.all(s.species_yields() == 0)
+    one = S.viscous_3d(1, seed=4)
+    s.set_surface(one.fo_surf())
+    s.generate_samples()
+    h1, _ = s.all_hadrons()
+    assert len(h1) == s.counts().sum()
+    s.setVal("number_of_repeated_sampling", 0)
+    s.generate_samples()
+    h0, off0 = s.all_hadrons()
+    assert len(h0) == 0 and s.get_number_of_sampled_events() == 0 and off0.tolist() == [0]
