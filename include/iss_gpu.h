@@ -246,6 +246,44 @@ const char* iss_gpu_last_error(const iss_handle* h);
 /* Static name of a status code. */
 const char* iss_gpu_status_string(int status);
 
+/* ---- the learned proposal ------------------------------------------------
+ *
+ * No counterpart in the reference: the reference has one momentum sampler
+ * (FSSW::sample_momemtum_from_a_fluid_cell, src/FSSW.cpp:1852-1966).  The
+ * learned sampler keeps that sampler's target density and accept step and
+ * changes only where proposals come from: a mixture of the plain proposal
+ * and a conditional density network (18 features of the cell and species ->
+ * 4 x 128 ReLU -> an 8-component log-normal x von Mises-Fisher mixture over
+ * the rest-frame momentum).  The network runs on the tensor cores (bf16
+ * weights, FP32 accumulation) for training and inference.
+ *
+ * Features of a (cell, species) pair, in this order (rest-frame cell values):
+ *   (T - 0.15) / 0.02, (mu / T) / 2, pi_xx, pi_xy, pi_xz, pi_yy, pi_yz each
+ *   / (e + P) / 0.1, Pi / (e + P) / 0.05, (0, q_x, q_y, q_z) / (e + P) / 0.1,
+ *   dsigma_mu / (|dsigma_0| + |dsigma_vec|), (m / T) / 10, statistics sign.
+ * Targets: (K, n_x, n_y, n_z) with K = (E - m) / T and n = p / |p|.
+ * Network outputs (64 per row, 48 used): 8 logits, 8 locations of ln K,
+ * 8 ln sigma, 8 x 3 vectors v (direction v / |v|, concentration |v|). */
+
+/* Number of FP32 weights of the network (flat layout: per layer W[out][in]
+ * row-major, then b[out]). */
+int64_t iss_gpu_learned_num_weights(void);
+/* Deterministic initial weights from a seed. */
+iss_status iss_gpu_learned_init_weights(iss_handle* h, uint64_t seed);
+iss_status iss_gpu_learned_set_weights(iss_handle* h, const float* weights, int64_t n);
+iss_status iss_gpu_learned_get_weights(iss_handle* h, float* out, int64_t capacity);
+/* Network outputs for n feature rows (host FP32 [n][18] -> host FP32 [n][64]). */
+iss_status iss_gpu_learned_forward(iss_handle* h, const float* features, int64_t n, float* out);
+/* Mean negative log-likelihood of n targets (host FP32 [n][4]) and its
+ * gradient with respect to the weights (host FP32 [num_weights]). */
+iss_status iss_gpu_learned_loss_grad(iss_handle* h, const float* features, const float* targets,
+                                     int64_t n, double* loss, float* grad);
+/* Self-test of the tensor-core GEMM the network is built from:
+ * c[128][n] = a[128][k] * b[n][k]^T with bf16 inputs (raw 16-bit patterns,
+ * row-major) and FP32 output; n in {32, 64, ..., 256}, k in {16, 32, ..., 256}. */
+iss_status iss_gpu_mma_selftest(const uint16_t* a, const uint16_t* b, int32_t n, int32_t k,
+                                float* c);
+
 /* ---- count-to-slot scan without allocation ----------------------------- */
 
 /* No counterpart in the reference.  Callers that cannot allocate device

@@ -24,13 +24,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INCLUDES = [f"-I{CSRC}", f"-I{os.path.join(REPO, 'include')}", f"-I{CUDA_HOME}/include"]
 
 CU_SOURCES = ["kernels_prologue.cu", "kernels_cells.cu", "kernels_sample.cu", "kernels_output.cu",
-              "kernels_decay.cu", "noalloc_scan.cu"]
+              "kernels_decay.cu", "noalloc_scan.cu", "kernels_mlp.cu"]
 # the prologue reproduces the reference's float/double rounding points exactly,
 # so mul+add must not be contracted into FMAs there
 CU_EXTRA = {"kernels_prologue.cu": ["--fmad=false"],
             # the sampler's acceptance tests tolerate approximate transcendentals
             "kernels_sample.cu": ["--use_fast_math"]}
-CXX_SOURCES = ["api.cpp", "host/params.cpp", "host/tables.cpp", "host/surface_io.cpp",
+CXX_SOURCES = ["api.cpp", "learned.cpp", "host/params.cpp", "host/tables.cpp", "host/surface_io.cpp",
                "host/writers.cpp", "shim/iSS.cpp"]
 CLI_SOURCES = ["cli/main.cpp"]
 

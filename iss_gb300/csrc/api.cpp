@@ -18,37 +18,19 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "devbuf.h"
 #include "host/params.h"
 #include "host/surface_io.h"
 #include "host/tables.h"
 #include "host/writers.h"
 #include "iss_gpu.h"
 #include "kernels.h"
+#include "kernels_mlp.h"
+#include "learned.h"
 
 using namespace iss;
 
 namespace {
-
-template <typename T>
-struct DevBuf {
-    T* ptr = nullptr;
-    size_t cap = 0;   // elements
-    cudaError_t reserve(size_t n) {
-        if (n <= cap && ptr) return cudaSuccess;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        cap = 0;
-        const size_t want = std::max<size_t>(n, 1);
-        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&ptr), want * sizeof(T));
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        cap = 0;
-    }
-};
 
 struct TableKey {
     std::string table_path;
@@ -141,6 +123,8 @@ struct iss_handle {
     bool host_valid = false;
     std::vector<double> totals;
     iss_timings_t timings{};
+    // the learned proposal: network, training set, per-pair mixture tables
+    Learned learned;
 
     ~iss_handle() {
         if (cuda_ready) {
@@ -179,6 +163,7 @@ struct iss_handle {
             d_dparticles.release();
             d_dchannels.release();
             d_dsorted.release();
+            learned.release_all();
             if (copy_stream) cudaStreamDestroy(copy_stream);
             if (stream) cudaStreamDestroy(stream);
         }
@@ -1384,6 +1369,93 @@ iss_status iss_gpu_copy_counts(iss_handle* h, int32_t* out, int64_t capacity) {
 iss_status iss_gpu_get_timings(iss_handle* h, iss_timings_t* out) {
     if (!h || !out) return ISS_ERR_INVALID_ARG;
     *out = h->timings;
+    return ISS_OK;
+}
+
+
+// ---- the learned proposal network -------------------------------------------
+
+iss_status iss_gpu_mma_selftest(const uint16_t* a, const uint16_t* b, int32_t n, int32_t k,
+                                float* c) {
+    if (!a || !b || !c || n < 32 || n > 256 || (n % 32) != 0 || k < 16 || k > 256 || (k % 16) != 0)
+        return ISS_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ISS_ERR_CUDA;
+    void *da = nullptr, *db = nullptr;
+    float* dc = nullptr;
+    int* derr = nullptr;
+    cudaStream_t s = nullptr;
+    iss_status st = ISS_ERR_CUDA;
+    int herr = 0;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+        cudaMalloc(&da, 2 * 128 * static_cast<size_t>(k)) == cudaSuccess &&
+        cudaMalloc(&db, 2 * static_cast<size_t>(n) * k) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&dc), 4 * 128 * static_cast<size_t>(n)) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&derr), sizeof(int)) == cudaSuccess &&
+        cudaMemcpyAsync(da, a, 2 * 128 * static_cast<size_t>(k), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+        cudaMemcpyAsync(db, b, 2 * static_cast<size_t>(n) * k, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+        cudaMemsetAsync(derr, 0, sizeof(int), s) == cudaSuccess &&
+        launch_mma_selftest(da, db, n, k, dc, derr, s) == cudaSuccess &&
+        cudaMemcpyAsync(c, dc, 4 * 128 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+        cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+        cudaStreamSynchronize(s) == cudaSuccess)
+        st = herr == 0 ? ISS_OK : ISS_ERR_SAMPLING;
+    if (da) cudaFree(da);
+    if (db) cudaFree(db);
+    if (dc) cudaFree(dc);
+    if (derr) cudaFree(derr);
+    if (s) cudaStreamDestroy(s);
+    return st;
+}
+
+int64_t iss_gpu_learned_num_weights(void) { return mlp::kNumParams; }
+
+iss_status iss_gpu_learned_init_weights(iss_handle* h, uint64_t seed) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    iss_status st = ensure_cuda(h);
+    if (st != ISS_OK) return st;
+    std::vector<float> p;
+    Learned::initial_params(seed, &p);
+    CUDA_TRY(h, h->learned.set_params(p.data(), h->stream));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_set_weights(iss_handle* h, const float* weights, int64_t n) {
+    if (!h || !weights) return ISS_ERR_INVALID_ARG;
+    if (n != mlp::kNumParams)
+        return fail(h, ISS_ERR_INVALID_ARG, "%lld weights given, the network has %lld",
+                    static_cast<long long>(n), static_cast<long long>(mlp::kNumParams));
+    iss_status st = ensure_cuda(h);
+    if (st != ISS_OK) return st;
+    CUDA_TRY(h, h->learned.set_params(weights, h->stream));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_get_weights(iss_handle* h, float* out, int64_t capacity) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    if (!h->learned.have_weights) return fail(h, ISS_ERR_NO_SAMPLES, "the network has no weights yet");
+    if (capacity < mlp::kNumParams) return fail(h, ISS_ERR_CAPACITY, "need %lld floats",
+                                                static_cast<long long>(mlp::kNumParams));
+    CUDA_TRY(h, h->learned.get_params(out, h->stream));
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_forward(iss_handle* h, const float* features, int64_t n, float* out) {
+    if (!h || !features || !out || n < 0) return ISS_ERR_INVALID_ARG;
+    if (!h->learned.have_weights) return fail(h, ISS_ERR_NO_SAMPLES, "the network has no weights yet");
+    CUDA_TRY(h, h->learned.forward_host(features, n, out, h->num_sms, h->stream));
+    if (h->learned.device_error(h->stream) != 0)
+        return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the forward pass timed out");
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_loss_grad(iss_handle* h, const float* features, const float* targets,
+                                     int64_t n, double* loss, float* grad) {
+    if (!h || !features || !targets || !loss || !grad || n <= 0) return ISS_ERR_INVALID_ARG;
+    if (!h->learned.have_weights) return fail(h, ISS_ERR_NO_SAMPLES, "the network has no weights yet");
+    CUDA_TRY(h, h->learned.loss_grad_host(features, targets, n, loss, grad, h->num_sms, h->stream));
+    if (h->learned.device_error(h->stream) != 0)
+        return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the backward pass timed out");
     return ISS_OK;
 }
 

@@ -37,6 +37,9 @@ EXPORTED = [
     "iss_gpu_species_yields", "iss_gpu_num_cells", "iss_gpu_copy_lrf_cells",
     "iss_gpu_copy_cell_yields", "iss_gpu_copy_counts", "iss_gpu_get_timings",
     "iss_gpu_last_error", "iss_gpu_status_string", "iss_gpu_scan_counts_noalloc",
+    "iss_gpu_learned_num_weights", "iss_gpu_learned_init_weights", "iss_gpu_learned_set_weights",
+    "iss_gpu_learned_get_weights", "iss_gpu_learned_forward", "iss_gpu_learned_loss_grad",
+    "iss_gpu_mma_selftest",
 ]
 
 
@@ -102,9 +105,17 @@ def lib():
         L.iss_gpu_status_string.argtypes = [C.c_int]
         L.iss_gpu_status_string.restype = C.c_char_p
         L.iss_gpu_scan_counts_noalloc.argtypes = [v, C.c_int64, v, v]
+        L.iss_gpu_learned_num_weights.argtypes = []
+        L.iss_gpu_learned_init_weights.argtypes = [h, C.c_uint64]
+        L.iss_gpu_learned_set_weights.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_learned_get_weights.argtypes = [h, v, C.c_int64]
+        L.iss_gpu_learned_forward.argtypes = [h, v, C.c_int64, v]
+        L.iss_gpu_learned_loss_grad.argtypes = [h, v, v, C.c_int64, C.POINTER(C.c_double), v]
+        L.iss_gpu_mma_selftest.argtypes = [v, v, C.c_int32, C.c_int32, v]
         for name in EXPORTED:
             if name not in ("iss_gpu_last_error", "iss_gpu_status_string"):
                 getattr(L, name).restype = C.c_int
+        L.iss_gpu_learned_num_weights.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -304,3 +315,43 @@ class iSS:
         t = Timings()
         self._check(self._L.iss_gpu_get_timings(self._h, C.byref(t)))
         return t.as_dict()
+
+    # the learned proposal network
+    def learned_init_weights(self, seed=0):
+        self._check(self._L.iss_gpu_learned_init_weights(self._h, int(seed)))
+
+    def learned_set_weights(self, w):
+        a = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self._L.iss_gpu_learned_set_weights(self._h, _ptr(a), a.size))
+
+    def learned_get_weights(self):
+        out = np.zeros(self._L.iss_gpu_learned_num_weights(), dtype=np.float32)
+        self._check(self._L.iss_gpu_learned_get_weights(self._h, _ptr(out), out.size))
+        return out
+
+    def learned_forward(self, features):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.zeros((f.shape[0], 64), dtype=np.float32)
+        self._check(self._L.iss_gpu_learned_forward(self._h, _ptr(f), f.shape[0], _ptr(out)))
+        return out
+
+    def learned_loss_grad(self, features, targets):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(self._L.iss_gpu_learned_num_weights(), dtype=np.float32)
+        loss = C.c_double()
+        self._check(self._L.iss_gpu_learned_loss_grad(self._h, _ptr(f), _ptr(t), f.shape[0],
+                                                      C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+
+def mma_selftest(a_bf16, b_bf16):
+    """c = a @ b.T on one tensor-core tile (a: [128][k], b: [n][k], raw bf16
+    bit patterns as uint16)."""
+    a = np.ascontiguousarray(a_bf16, dtype=np.uint16)
+    b = np.ascontiguousarray(b_bf16, dtype=np.uint16)
+    c = np.zeros((128, b.shape[0]), dtype=np.float32)
+    st = lib().iss_gpu_mma_selftest(_ptr(a), _ptr(b), b.shape[0], a.shape[1], _ptr(c))
+    if st != ISS_OK:
+        raise IssError(st, "tensor-core self-test failed")
+    return c
