@@ -22,6 +22,13 @@ finished events overlap the sampling of later ones).
 --impl reference times the CPU implementation of the path (the oracle port
 of the reference's algorithm, oracle/) on the host cores with one process per
 core, each sampling a disjoint share of the events on a 10 % cell sample.
+
+--sampler learned first trains the proposal network (5e7 momenta of the
+plain sampler from seeds 10..19, Adam on the tensor cores, reported apart),
+then times the same steps with the learned proposal (gpu_sampler = 1,
+alpha = 0.8) and reports its acceptance against the plain sampler's on the
+same species, the network's tensor-core throughput, and two-sample
+chi-square / KS p-values of pT, y, phi and v2 against the plain sampler.
 """
 from __future__ import annotations
 
@@ -50,6 +57,8 @@ PARAMS = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1, include_
               bulk_deltaf_kind=11, turn_on_bulk=1, quantum_statistics=1,
               dN_dy_sampling_model=30, number_of_repeated_sampling=N_EVENTS)
 ALG_BYTES_PER_HADRON = 40 + 96 + 4     # record write + LRF cell gather + slot/index
+# network forward per (species, cell) pair: 2 x (18 x 128 + 3 x 128 x 128 + 128 x 48)
+MLP_FLOPS_PER_PAIR = 2 * (18 * 128 + 3 * 128 * 128 + 128 * 48)
 
 # the other configurations of the benchmark set, for --workload (the default
 # line is always the viscous one above)
@@ -270,6 +279,78 @@ def run_reference(args, ws, rank):
 # ---------------------------------------------------------------------------
 # GPU leg
 
+def _chi2_two_sample(a, b):
+    from scipy import stats
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    m = (a + b) >= 10
+    a, b = a[m], b[m]
+    Na, Nb = a.sum(), b.sum()
+    chi2 = np.sum((np.sqrt(Nb / Na) * a - np.sqrt(Na / Nb) * b) ** 2 / (a + b))
+    return float(stats.chi2.sf(chi2, m.sum() - 1))
+
+
+def learned_report(s, timings, args):
+    """Acceptance of the learned proposal against the plain sampler's on the
+    same species (alpha -> 0 with the envelope at 1), the plain sampler's step
+    time, and spectra of the learned species against the plain sampler (100
+    events, same seed, so the counts agree)."""
+    from scipy import stats
+    st = s.learned_stats()
+    out = {"species": st["n_species"], "pairs": st["n_pairs"], "ms_network": st["ms_network"],
+           "ms_forward": st["ms_forward"], "tries_per_hadron": st["n_tries"] / max(st["n_hadrons"], 1),
+           "violations_per_try": st["n_violations"] / max(st["n_tries"], 1)}
+    s.set_params(gpu_learned_alpha=1e-4, gpu_learned_safety=1e6)
+    s.generate_samples()
+    st0 = s.learned_stats()
+    out["tries_per_hadron_without_network"] = st0["n_tries"] / max(st0["n_hadrons"], 1)
+    s.set_params(gpu_learned_alpha=0.8, gpu_learned_safety=1.15)
+    s.set_params(gpu_sampler=0)
+    s.generate_samples()
+    out["plain_ms_per_step"] = s.timings()["ms_total"]
+    out["plain_tries_per_hadron_all_species"] = (s.timings()["n_tries"] /
+                                                 max(s.timings()["n_hadrons"], 1))
+    ev = s.getVal("number_of_repeated_sampling")
+    s.set_params(number_of_repeated_sampling=min(100, int(ev)))
+    s.set_random_seed(99)
+    s.generate_samples()
+    plain, _ = s.all_hadrons()
+    s.set_params(gpu_sampler=1)
+    s.set_random_seed(99)
+    s.generate_samples()
+    lrn, _ = s.all_hadrons()
+    s.set_params(number_of_repeated_sampling=int(ev))
+    pv = {}
+    for pid in (211, -211, 111, 321, -321, 2212):
+        a, b = plain[plain["pid"] == pid], lrn[lrn["pid"] == pid]
+        if len(a) < 1000:
+            continue
+        obs = []
+        for h in (a, b):
+            pt = np.hypot(h["px"], h["py"]).astype(np.float64)
+            y = 0.5 * np.log((h["E"].astype(np.float64) + h["pz"]) / (h["E"].astype(np.float64) - h["pz"]))
+            ph = np.arctan2(h["py"], h["px"]).astype(np.float64)
+            obs.append((pt, y, ph))
+        (pa, ya, fa), (pb, yb, fb) = obs
+        e = np.quantile(np.concatenate([pa, pb]), np.linspace(0, 1, 41))
+        pv[f"{pid}_pT_chi2"] = _chi2_two_sample(np.histogram(pa, e)[0], np.histogram(pb, e)[0])
+        pv[f"{pid}_pT_ks"] = float(stats.ks_2samp(pa, pb).pvalue)
+        e = np.linspace(-4.5, 4.5, 37)
+        pv[f"{pid}_y_chi2"] = _chi2_two_sample(np.histogram(ya, e)[0], np.histogram(yb, e)[0])
+        e = np.linspace(-np.pi, np.pi, 37)
+        pv[f"{pid}_phi_chi2"] = _chi2_two_sample(np.histogram(fa, e)[0], np.histogram(fb, e)[0])
+        zs = []
+        for lo, hi in ((0, 0.5), (0.5, 1.0), (1.0, 2.0), (2.0, 4.0)):
+            ca, cb = np.cos(2 * fa[(pa >= lo) & (pa < hi)]), np.cos(2 * fb[(pb >= lo) & (pb < hi)])
+            if len(ca) > 100 and len(cb) > 100:
+                zs.append((ca.mean() - cb.mean()) / np.sqrt(ca.var() / len(ca) + cb.var() / len(cb)))
+        pv[f"{pid}_v2_chi2"] = float(stats.chi2.sf(np.sum(np.square(zs)), len(zs))) if zs else 1.0
+    out["spectra_vs_plain"] = {"events": min(100, int(ev)), "min_p": min(pv.values()) if pv else None,
+                               "tests": len(pv), "p_values": pv}
+    s.set_params(gpu_sampler=1)
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -306,6 +387,21 @@ def run_gpu(args, ws, rank, local):
         fo_pinned = torch.from_numpy(fo).pin_memory().numpy()
         s.set_surface(fo_pinned)
     s.set_random_seed(20261203)
+    learned = None
+    if args.sampler == "learned":
+        t0 = time.perf_counter()
+        curve = s.learned_train(n_momenta=args.train_momenta, first_seed=10, n_seeds=10,
+                                n_steps=args.train_steps, batch=8192, learning_rate=2e-3,
+                                init_seed=1)
+        t_train = time.perf_counter() - t0
+        st = s.learned_stats()
+        learned = {"train_momenta": st["n_train_rows"], "train_steps": args.train_steps,
+                   "train_batch": 8192, "train_s_total": t_train,
+                   "train_ms_adam_steps": st["ms_train"],
+                   "loss_first": float(curve[:20].mean()), "loss_last": float(curve[-100:].mean()),
+                   "nll_plain_proposal": st["train_nll_plain"]}
+        s.set_params(gpu_sampler=1, gpu_learned_alpha=0.8)
+        s.set_random_seed(20261203)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -404,6 +500,8 @@ def run_gpu(args, ws, rank, local):
         e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps,
                [1e3 * x / args.steps for x in parts], max(link)]
 
+    if learned is not None:
+        learned.update(learned_report(s, timings, args))
     sec = sum(dev_ms) / 1e3
     local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
     if e2e:
@@ -459,7 +557,7 @@ def run_gpu(args, ws, rank, local):
                            "species": wl["species"],
                            "delta_f": {k: v for k, v in wl["params"].items()
                                        if k.startswith("include_") or k == "bulk_deltaf_kind"},
-                           "sampler": "plain", "decays": bool(args.decays),
+                           "sampler": args.sampler, "decays": bool(args.decays),
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
                            "wall_s_timed": wall},
@@ -474,6 +572,19 @@ def run_gpu(args, ws, rank, local):
                 "hadrons_per_step": nh / args.steps,
                 "phase_ms_per_step": phases,
                 "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
+        if learned is not None:
+            peak_tf = 1922.0
+            try:
+                with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+                    peak_tf = float(json.load(f)["bf16_tflops"])
+            except Exception:
+                pass
+            fl = learned["pairs"] * MLP_FLOPS_PER_PAIR
+            tf = fl / (learned["ms_forward"] * 1e-3) / 1e12
+            learned["tensor_roofline"] = {"bound": "tensor", "kernel": "mlp_fwd_kernel",
+                                          "achieved": tf, "peak": peak_tf, "unit": "TFLOP/s",
+                                          "frac": tf / peak_tf, "flops_per_launch": fl}
+            line["learned"] = learned
         if args.decays:
             line["decays"] = {"ms_per_step": timings["ms_decays"],
                               "final_hadrons_per_step": timings["n_hadrons"]}
@@ -503,6 +614,10 @@ def main():
                     help="perform_decays = 1 (resonance decays after sampling, timed apart)")
     ap.add_argument("--oscar", action="store_true",
                     help="time the OSCAR writer on the last step's hadrons")
+    ap.add_argument("--sampler", choices=["plain", "learned"], default="plain",
+                    help="learned: train the proposal network first, then sample with it")
+    ap.add_argument("--train-momenta", type=int, default=50_000_000)
+    ap.add_argument("--train-steps", type=int, default=3000)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.cells is None:

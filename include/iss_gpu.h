@@ -278,6 +278,61 @@ iss_status iss_gpu_learned_forward(iss_handle* h, const float* features, int64_t
  * gradient with respect to the weights (host FP32 [num_weights]). */
 iss_status iss_gpu_learned_loss_grad(iss_handle* h, const float* features, const float* targets,
                                      int64_t n, double* loss, float* grad);
+/* Training of the network (no counterpart in the reference).  The plain
+ * sampler draws n_momenta hadrons on the handle's surface with the handle's
+ * parameters, split evenly over the seeds first_seed .. first_seed + n_seeds
+ * - 1 (resonance decays off); each hadron becomes one training row: its
+ * (cell, species) features and its rest-frame (K, n).  Then n_steps Adam
+ * steps minimise the mean negative log-likelihood of the mixture on batches
+ * of `batch` rows drawn with replacement (forward, loss, backward and update
+ * on the tensor cores, replayed as one CUDA graph per step).  A network
+ * without weights starts from iss_gpu_learned_init_weights(init_seed).  The
+ * handle's parameters and seed are restored afterwards; the rows stay on the
+ * device for further calls.  loss_curve (optional, capacity >= n_steps)
+ * receives the mean loss of every step. */
+typedef struct iss_learned_train {
+    int64_t n_momenta;       /* training rows (the rows of the last call are replaced);
+                                0: more steps on the rows and weights already held */
+    int32_t first_seed;
+    int32_t n_seeds;
+    int32_t n_steps;
+    int32_t batch;
+    double learning_rate;
+    uint64_t init_seed;      /* initial weights and batch draws */
+} iss_learned_train_t;
+iss_status iss_gpu_learned_train(iss_handle* h, const iss_learned_train_t* options,
+                                 double* loss_curve, int32_t capacity);
+
+/* Sampling with the learned proposal: gpu_sampler = 1.  Species whose
+ * expected hadrons per cell over all events reach
+ * gpu_learned_min_hadrons_per_cell (default 1) are proposed from
+ * gpu_learned_alpha (default 0.8) x network mixture + (1 - alpha) x the
+ * plain proposal; the others keep the plain sampler.  The accept step keeps
+ * the plain sampler's target: P a / (M q), with M per (species, cell) from
+ * gpu_learned_pilot (default 64) pilot proposals times gpu_learned_safety
+ * (default 1.15), capped by 1 / (1 - alpha).  A proposal whose ratio exceeds
+ * 1 is counted as a violation. */
+typedef struct iss_learned_stats {
+    int32_t n_species;       /* species sampled with the learned proposal   */
+    int64_t n_pairs;         /* (species, cell) pairs evaluated by the network */
+    double ms_network;       /* pair inputs + network + mixture records + envelopes */
+    int64_t n_tries;         /* proposals made for those species           */
+    int64_t n_hadrons;       /* hadrons of those species                    */
+    int64_t n_violations;    /* proposals whose ratio exceeded 1            */
+    int64_t n_train_rows;    /* training rows held on the device            */
+    double ms_train;         /* wall time of the Adam steps of the last training */
+    int32_t train_events_per_seed;  /* events of each plain run that drew training rows */
+    double train_nll_plain;  /* mean -ln P of the training rows under the plain proposal
+                                (same units as the network's loss) */
+    double ms_forward;       /* the network's forward pass alone (part of ms_network) */
+} iss_learned_stats_t;
+iss_status iss_gpu_learned_stats(iss_handle* h, iss_learned_stats_t* out);
+/* Training rows first .. first + count - 1 of the last training: features
+ * (FP32 [count][18], the bf16 values the network reads) and targets
+ * (FP32 [count][4]); either pointer may be NULL. */
+iss_status iss_gpu_learned_copy_rows(iss_handle* h, int64_t first, int64_t count, float* features,
+                                     float* targets);
+
 /* Self-test of the tensor-core GEMM the network is built from:
  * c[128][n] = a[128][k] * b[n][k]^T with bf16 inputs (raw 16-bit patterns,
  * row-major) and FP32 output; n in {32, 64, ..., 256}, k in {16, 32, ..., 256}. */

@@ -43,7 +43,8 @@ struct TableKey {
     }
 };
 
-enum Phase { kEvStart = 0, kEvPrologue, kEvYields, kEvCdf, kEvCounts, kEvSampleStart, kEvSample, kEvCount };
+enum Phase { kEvStart = 0, kEvPrologue, kEvYields, kEvCdf, kEvCounts, kEvSampleStart, kEvSample,
+             kEvLearnStart, kEvLearnEnd, kEvFwdStart, kEvFwdEnd, kEvCount };
 
 }  // namespace
 
@@ -125,6 +126,10 @@ struct iss_handle {
     iss_timings_t timings{};
     // the learned proposal: network, training set, per-pair mixture tables
     Learned learned;
+    bool use_learned = false;            // gpu_sampler = 1
+    DevBuf<int32_t> d_lslot, d_lspecies, d_spid;
+    DevBuf<float> d_lpairs;
+    iss_learned_stats_t lstats{};
 
     ~iss_handle() {
         if (cuda_ready) {
@@ -164,6 +169,10 @@ struct iss_handle {
             d_dchannels.release();
             d_dsorted.release();
             learned.release_all();
+            d_lslot.release();
+            d_lspecies.release();
+            d_spid.release();
+            d_lpairs.release();
             if (copy_stream) cudaStreamDestroy(copy_stream);
             if (stream) cudaStreamDestroy(stream);
         }
@@ -280,6 +289,18 @@ iss_status prepare(iss_handle* h) {
     c.max_tries = static_cast<int>(h->params.get_or("gpu_max_tries", 10000));
     c.max_redraws = static_cast<int>(h->params.get_or("gpu_max_redraws", 64));
     c.event_offset = static_cast<uint32_t>(h->params.get_or("gpu_event_offset", 0));
+    {
+        const int smp = static_cast<int>(h->params.get_or("gpu_sampler", 0));
+        if (smp != 0 && smp != 1)
+            return fail(h, ISS_ERR_UNSUPPORTED, "gpu_sampler = %d (0: plain, 1: learned)", smp);
+        h->use_learned = smp == 1;
+        const double alpha = h->params.get_or("gpu_learned_alpha", 0.8);
+        if (h->use_learned && !(alpha > 0.0 && alpha < 1.0))
+            return fail(h, ISS_ERR_INVALID_ARG, "gpu_learned_alpha = %g must lie in (0, 1)", alpha);
+        c.lalpha = static_cast<float>(alpha);
+        c.lslot = nullptr;
+        c.lpairs = nullptr;
+    }
     c.key0 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed));
     c.key1 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed) >> 32);
     c.n_species = static_cast<int>(h->species.size());
@@ -666,6 +687,63 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
 // second stream while the next chunk is sampled.
 constexpr int kMaxChunks = 16;
 
+// Learned proposal of one generate: the species whose expected hadrons per
+// cell (over all events) reach gpu_learned_min_hadrons_per_cell, the network
+// on every (species, cell) pair of them, and the pairs' mixture records and
+// envelope constants.  Sets cfg.lslot / lpairs for the sampler.
+iss_status run_learned_pairs(iss_handle* h) {
+    DevConfig& c = h->cfg;
+    const int S = c.n_species;
+    cudaStream_t s = h->stream;
+    if (!h->learned.have_weights)
+        return fail(h, ISS_ERR_NO_SAMPLES,
+                    "gpu_sampler = 1 needs network weights (iss_gpu_learned_train or "
+                    "iss_gpu_learned_set_weights)");
+    const double thr = h->params.get_or("gpu_learned_min_hadrons_per_cell", 1.0);
+    const int n_pilot = static_cast<int>(h->params.get_or("gpu_learned_pilot", 64));
+    const float safety = static_cast<float>(h->params.get_or("gpu_learned_safety", 1.15));
+    if (n_pilot < 1 || n_pilot > 4096 || !(safety >= 1.0f))
+        return fail(h, ISS_ERR_INVALID_ARG, "gpu_learned_pilot = %d, gpu_learned_safety = %g", n_pilot,
+                    static_cast<double>(safety));
+    std::vector<int32_t> slot(static_cast<size_t>(S), -1), lspecies;
+    for (int k = 0; k < S; k++) {
+        double n = 0.0;
+        for (int b = 0; b < c.n_surfaces; b++)
+            n += h->totals[static_cast<size_t>(b) * S + k] * c.ymult * h->segs[b].ne;
+        if (n >= thr * static_cast<double>(c.n_cells)) {
+            slot[k] = static_cast<int32_t>(lspecies.size());
+            lspecies.push_back(k);
+        }
+    }
+    const int n_slots = static_cast<int>(lspecies.size());
+    const int64_t n_pairs = static_cast<int64_t>(n_slots) * c.n_cells;
+    h->lstats.n_species = n_slots;
+    h->lstats.n_pairs = n_pairs;
+    CUDA_TRY(h, h->d_lslot.reserve(static_cast<size_t>(std::max(S, 1))));
+    CUDA_TRY(h, h->d_lspecies.reserve(static_cast<size_t>(std::max(n_slots, 1))));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_lslot.ptr, slot.data(), 4 * slot.size(), cudaMemcpyHostToDevice, s));
+    if (n_slots > 0)
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_lspecies.ptr, lspecies.data(), 4 * lspecies.size(),
+                                    cudaMemcpyHostToDevice, s));
+    Learned& L = h->learned;
+    CUDA_TRY(h, L.x.reserve(static_cast<size_t>(std::max<int64_t>(n_pairs, 1)) * mlp::kIn0));
+    CUDA_TRY(h, h->d_lpairs.reserve(static_cast<size_t>(std::max<int64_t>(n_pairs, 1)) * kPairFloats));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvLearnStart], s));
+    const CellArrays cells = cell_arrays(h);
+    CUDA_TRY(h, launch_learned_pairs(c, cells, h->d_species.ptr, h->d_lspecies.ptr, n_slots, L.x.ptr, s));
+    CUDA_TRY(h, cudaMemsetAsync(L.err.ptr, 0, sizeof(int), s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvFwdStart], s));
+    CUDA_TRY(h, launch_mlp_forward(L.img.ptr, L.params.ptr, L.x.ptr, n_pairs, nullptr, nullptr,
+                                   L.err.ptr, h->num_sms, s, h->d_lpairs.ptr));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvFwdEnd], s));
+    c.lslot = h->d_lslot.ptr;
+    c.lpairs = h->d_lpairs.ptr;
+    CUDA_TRY(h, launch_learned_envelopes(c, cells, h->d_species.ptr, h->d_lspecies.ptr, n_slots,
+                                         n_pilot, safety, h->d_lpairs.ptr, s));
+    CUDA_TRY(h, cudaEventRecord(h->ev[kEvLearnEnd], s));
+    return ISS_OK;
+}
+
 iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
                         bool* copied = nullptr) {
     if (copied) *copied = false;
@@ -746,6 +824,12 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, cudaMemcpyAsync(&sizes[1], h->d_item_off.ptr + nseg, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(&count_err, h->d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (h->use_learned) {
+        // per-species totals: which species the learned proposal takes
+        h->totals.resize(static_cast<size_t>(S) * c.n_surfaces);
+        CUDA_TRY(h, cudaMemcpyAsync(h->totals.data(), h->d_totals.ptr, 8 * h->totals.size(),
+                                    cudaMemcpyDeviceToHost, s));
+    }
     if (S > 0) {
         // event offsets: offsets[e * S] for e = 0..n_events
         CUDA_TRY(h, cudaMemcpy2DAsync(h->event_offsets.data(), sizeof(int64_t), h->d_offsets.ptr,
@@ -765,6 +849,19 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, h->d_item_seg.reserve(static_cast<size_t>(std::max<int64_t>(n_items, 1))));
     CUDA_TRY(h, launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
+    {
+        // per-generate fields; the training fields stay
+        const iss_learned_stats_t keep = h->lstats;
+        h->lstats = iss_learned_stats_t{};
+        h->lstats.n_train_rows = keep.n_train_rows;
+        h->lstats.ms_train = keep.ms_train;
+        h->lstats.train_events_per_seed = keep.train_events_per_seed;
+        h->lstats.train_nll_plain = keep.train_nll_plain;
+    }
+    if (h->use_learned) {
+        const iss_status lst = run_learned_pairs(h);
+        if (lst != ISS_OK) return lst;
+    }
 
     // with decays the records change after sampling: no copies during it
     const bool to_host = host_out != nullptr && n_units <= capacity && n_units > 0 && !h->decays;
@@ -845,6 +942,14 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures + decay_failures);
     t.kernel_launches = 15 + 2 * n_chunks;
+    if (h->use_learned) {
+        t.kernel_launches += 4;
+        h->lstats.n_tries = static_cast<int64_t>(ctr.learned_tries);
+        h->lstats.n_hadrons = static_cast<int64_t>(ctr.learned_hadrons);
+        h->lstats.n_violations = static_cast<int64_t>(ctr.learned_violations);
+        h->lstats.ms_network = elapsed(h, kEvLearnStart, kEvLearnEnd);
+        h->lstats.ms_forward = elapsed(h, kEvFwdStart, kEvFwdEnd);
+    }
     h->samples_valid = true;
     if (ctr.error_code == 1) {
         const int k = ctr.error_species;
@@ -852,6 +957,8 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
                     "momentum sampler out of range for species %d (m/T - mu/T off the tables)",
                     (k >= 0 && k < S) ? h->species[k].pid : 0);
     }
+    if (h->use_learned && h->learned.device_error(s) != 0)
+        return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the proposal network timed out");
     if (ctr.failures > 0)
         return fail(h, ISS_ERR_SAMPLING, "%llu hadrons abandoned after %d cell redraws",
                     static_cast<unsigned long long>(ctr.failures), c.max_redraws);
@@ -1456,6 +1563,171 @@ iss_status iss_gpu_learned_loss_grad(iss_handle* h, const float* features, const
     CUDA_TRY(h, h->learned.loss_grad_host(features, targets, n, loss, grad, h->num_sms, h->stream));
     if (h->learned.device_error(h->stream) != 0)
         return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the backward pass timed out");
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_stats(iss_handle* h, iss_learned_stats_t* out) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    *out = h->lstats;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_train(iss_handle* h, const iss_learned_train_t* opt, double* loss_curve,
+                                 int32_t capacity) {
+    if (!h || !opt) return ISS_ERR_INVALID_ARG;
+    if (opt->n_momenta < 0 || opt->n_seeds <= 0 || opt->n_steps < 0 || opt->batch <= 0 ||
+        !(opt->learning_rate > 0.0))
+        return fail(h, ISS_ERR_INVALID_ARG, "training options out of range");
+    if (opt->n_momenta == 0) {
+        // more steps on the rows already held
+        Learned& L0 = h->learned;
+        if (L0.n_data <= 0 || !L0.have_weights)
+            return fail(h, ISS_ERR_NO_SAMPLES, "n_momenta = 0 needs training rows and weights");
+        iss_status st0 = ensure_cuda(h);
+        if (st0 != ISS_OK) return st0;
+        const auto t0 = std::chrono::steady_clock::now();
+        CUDA_TRY(h, L0.train(opt->n_steps, opt->batch, static_cast<float>(opt->learning_rate),
+                             static_cast<uint32_t>(opt->init_seed),
+                             static_cast<uint32_t>(opt->init_seed >> 32) ^ 0x7A11u, loss_curve,
+                             h->num_sms, h->stream));
+        h->lstats.ms_train =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (L0.device_error(h->stream) != 0)
+            return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the training step timed out");
+        return ISS_OK;
+    }
+    if (loss_curve && capacity < opt->n_steps)
+        return fail(h, ISS_ERR_CAPACITY, "the loss curve needs %d entries", opt->n_steps);
+    if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface: call iss_gpu_read_surface first");
+    iss_status st = ensure_cuda(h);
+    if (st != ISS_OK) return st;
+    if (h->params.get_or("local_charge_conservation", 0) == 1)
+        return fail(h, ISS_ERR_UNSUPPORTED, "training rows with local_charge_conservation");
+    if (!h->batch_cells.empty())
+        return fail(h, ISS_ERR_UNSUPPORTED, "training rows from a batch of surfaces");
+    // the plain sampler draws the training momenta; the caller's settings come back afterwards
+    const char* keys[] = {"gpu_sampler", "perform_decays", "number_of_repeated_sampling",
+                          "sample_upto_desired_particle_number", "gpu_event_offset"};
+    double saved[5];
+    bool had[5];
+    for (int i = 0; i < 5; i++) had[i] = h->params.get(keys[i], &saved[i]);
+    const int64_t saved_seed = h->seed;
+    const bool saved_seed_set = h->seed_set;
+    auto restore = [&]() {
+        for (int i = 0; i < 5; i++) {
+            if (had[i]) h->params.set(keys[i], saved[i]);
+            else h->params.erase(keys[i]);
+        }
+        h->seed = saved_seed;
+        h->seed_set = saved_seed_set;
+        h->samples_valid = false;
+    };
+    h->params.set("gpu_sampler", 0);
+    h->params.set("perform_decays", 0);
+    h->params.set("sample_upto_desired_particle_number", 0);
+    h->params.set("gpu_event_offset", 0);
+    Learned& L = h->learned;
+    // hadrons per event from a one-event generate
+    h->params.set("number_of_repeated_sampling", 1);
+    h->seed = opt->first_seed;
+    st = run_generate(h);
+    if (st != ISS_OK) {
+        restore();
+        return st;
+    }
+    double per_event = 0.0;
+    {
+        std::vector<double> tot(h->species.size());
+        CUDA_TRY(h, cudaMemcpy(tot.data(), h->d_totals.ptr, 8 * tot.size(), cudaMemcpyDeviceToHost));
+        for (double v : tot) per_event += v * h->cfg.ymult;
+    }
+    if (!(per_event > 0.0)) {
+        restore();
+        return fail(h, ISS_ERR_SAMPLING, "the surface emits no hadrons");
+    }
+    const int64_t per_seed = (opt->n_momenta + opt->n_seeds - 1) / opt->n_seeds;
+    const int ev = static_cast<int>(std::min<double>(1e7, std::ceil(1.02 * per_seed / per_event) + 1));
+    // sorted PDG ids -> species index
+    {
+        std::vector<std::pair<int32_t, int32_t>> sp;
+        for (size_t k = 0; k < h->species.size(); k++)
+            sp.emplace_back(h->species[k].pid, static_cast<int32_t>(k));
+        std::sort(sp.begin(), sp.end());
+        std::vector<int32_t> tab(2 * sp.size());
+        for (size_t k = 0; k < sp.size(); k++) {
+            tab[k] = sp[k].first;
+            tab[sp.size() + k] = sp[k].second;
+        }
+        CUDA_TRY(h, h->d_spid.reserve(std::max<size_t>(tab.size(), 1)));
+        CUDA_TRY(h, cudaMemcpy(h->d_spid.ptr, tab.data(), 4 * tab.size(), cudaMemcpyHostToDevice));
+    }
+    const int S = static_cast<int>(h->species.size());
+    CUDA_TRY(h, L.data_x.reserve(static_cast<size_t>(opt->n_momenta) * mlp::kIn0));
+    CUDA_TRY(h, L.data_t.reserve(static_cast<size_t>(opt->n_momenta)));
+    CUDA_TRY(h, L.loss.reserve(std::max<size_t>(static_cast<size_t>(opt->n_steps), 1)));
+    CUDA_TRY(h, cudaMemsetAsync(L.loss.ptr, 0, sizeof(double), h->stream));
+    int64_t filled = 0;
+    for (int k = 0; k < opt->n_seeds && filled < opt->n_momenta; k++) {
+        h->params.set("number_of_repeated_sampling", ev);
+        h->seed = static_cast<int64_t>(opt->first_seed) + k;
+        st = run_generate(h);
+        if (st != ISS_OK) {
+            restore();
+            return st;
+        }
+        const int64_t take = std::min<int64_t>({h->n_hadrons, per_seed, opt->n_momenta - filled});
+        CUDA_TRY(h, launch_learned_train_rows(h->cfg, cell_arrays(h), h->d_species.ptr, h->d_spid.ptr,
+                                              h->d_spid.ptr + S, S, h->d_hadrons.ptr, h->d_cell_of.ptr,
+                                              take, L.data_x.ptr + filled * mlp::kIn0,
+                                              L.data_t.ptr + filled, L.loss.ptr, h->stream));
+        filled += take;
+    }
+    double nll_plain = 0.0;
+    CUDA_TRY(h, cudaMemcpyAsync(&nll_plain, L.loss.ptr, sizeof(double), cudaMemcpyDeviceToHost,
+                                h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    restore();
+    L.n_data = filled;
+    h->lstats.train_nll_plain = filled > 0 ? nll_plain / static_cast<double>(filled) : 0.0;
+    h->lstats.n_train_rows = filled;
+    h->lstats.train_events_per_seed = ev;
+    if (!L.have_weights) {
+        std::vector<float> p;
+        Learned::initial_params(opt->init_seed, &p);
+        CUDA_TRY(h, L.set_params(p.data(), h->stream));
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    CUDA_TRY(h, L.train(opt->n_steps, opt->batch, static_cast<float>(opt->learning_rate),
+                        static_cast<uint32_t>(opt->init_seed), static_cast<uint32_t>(opt->init_seed >> 32) ^ 0x7A11u,
+                        loss_curve, h->num_sms, h->stream));
+    h->lstats.ms_train = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (L.device_error(h->stream) != 0)
+        return fail(h, ISS_ERR_SAMPLING, "a tensor-core wait of the training step timed out");
+    return ISS_OK;
+}
+
+iss_status iss_gpu_learned_copy_rows(iss_handle* h, int64_t first, int64_t count, float* features,
+                                     float* targets) {
+    if (!h || first < 0 || count < 0) return ISS_ERR_INVALID_ARG;
+    Learned& L = h->learned;
+    if (first + count > L.n_data)
+        return fail(h, ISS_ERR_CAPACITY, "%lld training rows held", static_cast<long long>(L.n_data));
+    if (count == 0) return ISS_OK;
+    if (features) {
+        std::vector<uint16_t> x(static_cast<size_t>(count) * mlp::kIn0);
+        CUDA_TRY(h, cudaMemcpy(x.data(), L.data_x.ptr + first * mlp::kIn0, 2 * x.size(),
+                               cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < count; r++)
+            for (int j = 0; j < mlp::kFeatures; j++) {
+                const uint32_t b = static_cast<uint32_t>(x[r * mlp::kIn0 + j]) << 16;
+                float v;
+                std::memcpy(&v, &b, 4);
+                features[r * mlp::kFeatures + j] = v;
+            }
+    }
+    if (targets)
+        CUDA_TRY(h, cudaMemcpy(targets, L.data_t.ptr + first, sizeof(float4) * count,
+                               cudaMemcpyDeviceToHost));
     return ISS_OK;
 }
 

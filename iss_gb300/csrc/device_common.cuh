@@ -61,7 +61,19 @@ struct DevConfig {
     const SurfSeg* surf;     // [n_surfaces]
     const int32_t* ev_surf;  // [n_events] surface of each event
     DevTables tab;
+    // learned proposal (gpu_sampler = 1): slot of each species in the pair
+    // tables (-1: plain proposal), the per-(slot, cell) mixture records of
+    // kPairFloats floats, and the mixture weight of the network component
+    const int32_t* lslot;
+    const float* lpairs;
+    float lalpha;
 };
+
+// floats per (species slot, cell) record of the learned proposal: for each of
+// the 8 mixture components (cumulative weight, log-normaliser c, mu, sigma,
+// v_x, v_y, v_z, |v|); the last component's cumulative weight (always 1) is
+// replaced by the envelope constant M of the pair
+constexpr int kPairFloats = 64;
 
 // Species record in the sampler's mass order (32 bytes).
 struct SpeciesDev {
@@ -114,6 +126,9 @@ struct SampleCounters {
     unsigned long long redraws;
     unsigned long long failures;
     unsigned long long bound_violations;
+    unsigned long long learned_tries;       // proposals of the learned sampler
+    unsigned long long learned_violations;  // of these, ratios above the envelope M
+    unsigned long long learned_hadrons;     // hadrons of species in the pair tables
     int error_code;          // 1: m/T - mu/T off the momentum tables
     int error_species;
 };
@@ -124,7 +139,8 @@ struct HadronRec {
     float mass, E, px, py, pz, t, x, y, z;
 };
 
-enum : uint32_t { kTagCell = 1u, kTagTry = 2u, kTagCount = 3u };
+enum : uint32_t { kTagCell = 1u, kTagTry = 2u, kTagCount = 3u, kTagLearn = 5u, kTagPilot = 6u,
+                  kTagLearnRap = 7u };
 
 // ---------------------------------------------------------------------------
 // Fixed-point cell CDF.

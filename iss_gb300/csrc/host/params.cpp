@@ -44,6 +44,11 @@ void ParamStore::set(const std::string& key, double value) {
 
 bool ParamStore::has(const std::string& key) const { return find(key) >= 0; }
 
+void ParamStore::erase(const std::string& key) {
+    const long i = find(key);
+    if (i >= 0) items_.erase(items_.begin() + i);
+}
+
 bool ParamStore::get(const std::string& key, double* value) const {
     const long i = find(key);
     if (i < 0) return false;

@@ -24,6 +24,8 @@ class ParamStore {
     bool has(const std::string& key) const;
     bool get(const std::string& key, double* value) const;
     double get_or(const std::string& key, double fallback) const;
+    // removes a key (a temporary setting put back to "not set")
+    void erase(const std::string& key);
     const std::vector<std::pair<std::string, double>>& items() const { return items_; }
 
  private:

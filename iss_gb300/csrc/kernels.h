@@ -49,6 +49,24 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                            unsigned long long* work_counter, SampleCounters* counters, int num_sms,
                            cudaStream_t stream);
 
+// learned proposal (kernels_sample.cu): network inputs of the pairs
+// (slot, cell), slot < n_slots, as bf16 rows [n_slots * n_cells][32]; the
+// envelope constants of the pairs' mixture records (n_pilot proposals, times
+// safety; the records come from the network's fused epilogue); training rows
+// (features, (K, n) targets) from n sampled hadrons and their cells, with the
+// plain proposal's negative log-likelihood of the rows added to *nll_plain
+cudaError_t launch_learned_pairs(const DevConfig& cfg, const CellArrays& cells,
+                                 const SpeciesDev* species, const int32_t* lspecies, int n_slots,
+                                 void* x, cudaStream_t stream);
+cudaError_t launch_learned_envelopes(const DevConfig& cfg, const CellArrays& cells,
+                                     const SpeciesDev* species, const int32_t* lspecies, int n_slots,
+                                     int n_pilot, float safety, float* lpairs, cudaStream_t stream);
+cudaError_t launch_learned_train_rows(const DevConfig& cfg, const CellArrays& cells,
+                                      const SpeciesDev* species, const int32_t* sorted_pid,
+                                      const int32_t* sorted_idx, int S, const HadronRec* had,
+                                      const int32_t* cell_of, int64_t n, void* x, void* tg,
+                                      double* nll_plain, cudaStream_t stream);
+
 // kernels_decay.cu: one generation of resonance decays over all events
 // (event-sorted input with event ids; first[e] = index of event e's first
 // element), event ids from event offsets, event bounds of an event-sorted

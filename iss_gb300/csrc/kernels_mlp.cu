@@ -12,6 +12,7 @@
 
 #include "device_common.cuh"
 #include "kernels_mlp.h"
+#include "learned_record.cuh"
 #include "mlp.h"
 #include "tc05.cuh"
 
@@ -96,7 +97,8 @@ constexpr int kFwdSmem = static_cast<int>(kFwdImgElems * 2) + kTile * kIn0 * 2 +
 __global__ void __launch_bounds__(128, 1)
 mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ params,
                const __nv_bfloat16* __restrict__ X, int64_t n, float* __restrict__ out,
-               __nv_bfloat16* __restrict__ acts, int* __restrict__ err) {
+               __nv_bfloat16* __restrict__ acts, float* __restrict__ records,
+               int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sW = smem;
     uint8_t* sX = sW + kFwdImgElems * 2;
@@ -171,6 +173,22 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
                                                       c0 + 8 * q) = pk;
                     }
                 }
+            } else if (records) {
+                // fused epilogue: the row's mixture record, staged in shared
+                // memory (sH is free once the last GEMM has completed), then
+                // stored for the whole tile with coalesced 16-byte stores
+                float z[64];
+                tmem_ld32(tmem_lane_addr(tmem, warp, 0), *reinterpret_cast<float(*)[32]>(z));
+                tmem_ld32(tmem_lane_addr(tmem, warp, 32), *reinterpret_cast<float(*)[32]>(z + 32));
+#pragma unroll
+                for (int j = 0; j < kOutUsed; j++) z[j] += __ldg(bias + j);
+                float* r = reinterpret_cast<float*>(sH) + t * kOut;
+                mixture_record(z, r);
+                __syncthreads();
+                const int64_t rows = min(static_cast<int64_t>(kTile), n - tile * kTile);
+                const float4* src = reinterpret_cast<const float4*>(sH);
+                float4* dst = reinterpret_cast<float4*>(records + tile * kTile * kOut);
+                for (int i = t; i < rows * (kOut / 4); i += 128) dst[i] = src[i];
             } else {
                 for (int c0 = 0; c0 < kOut; c0 += 32) {
                     float v[32];
@@ -218,7 +236,10 @@ mlp_loss_kernel(const float* __restrict__ out, const float4* __restrict__ target
                 const int* __restrict__ step) {
     const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     float nll = 0.0f;
-    if (row < n) {
+    if (row < n && !(target[row].x > 0.0f)) {
+        // a row without a target (K <= 0) contributes nothing
+        for (int j = 0; j < kOut; j++) dout[row * kOut + j] = 0.0f;
+    } else if (row < n) {
         const float* z = out + row * kOut;
         const float4 tg = target[row];
         const float lK = logf(tg.x);
@@ -576,7 +597,8 @@ cudaError_t launch_features_to_bf16(const float* f, int64_t n, void* x, cudaStre
 }
 
 cudaError_t launch_mlp_forward(const void* img, const float* params, const void* X, int64_t n,
-                               float* out, void* acts, int* err, int num_sms, cudaStream_t s) {
+                               float* out, void* acts, int* err, int num_sms, cudaStream_t s,
+                               float* records) {
     if (n <= 0) return cudaSuccess;
     cudaError_t e = smem_opt_in(mlp_fwd_kernel, kFwdSmem, &g_fwd_attr);
     if (e != cudaSuccess) return e;
@@ -584,7 +606,7 @@ cudaError_t launch_mlp_forward(const void* img, const float* params, const void*
     const int grid = static_cast<int>(tiles < num_sms ? tiles : num_sms);
     mlp_fwd_kernel<<<grid, 128, kFwdSmem, s>>>(static_cast<const __nv_bfloat16*>(img), params,
                                                static_cast<const __nv_bfloat16*>(X), n, out,
-                                               static_cast<__nv_bfloat16*>(acts), err);
+                                               static_cast<__nv_bfloat16*>(acts), records, err);
     return cudaGetLastError();
 }
 

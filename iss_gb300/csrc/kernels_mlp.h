@@ -17,9 +17,12 @@ cudaError_t launch_mlp_images(const float* params, void* img, cudaStream_t s);
 // FP32 features [n][18] -> bf16 network input [n][32]
 cudaError_t launch_features_to_bf16(const float* f, int64_t n, void* x, cudaStream_t s);
 // out[n][64] = network(X); acts (optional, [4][n][128] bf16) keeps the hidden
-// activations for the backward pass
+// activations for the backward pass; with `records` the outputs are not
+// written: the epilogue turns each row into its mixture record (64 floats,
+// learned_record.cuh) instead
 cudaError_t launch_mlp_forward(const void* img, const float* params, const void* X, int64_t n,
-                               float* out, void* acts, int* err, int num_sms, cudaStream_t s);
+                               float* out, void* acts, int* err, int num_sms, cudaStream_t s,
+                               float* records = nullptr);
 // mean mixture negative log-likelihood of targets (K, nx, ny, nz): dout[n][64]
 // = d(mean loss)/d(out); loss_base[step ? *step : 0] += sum of the row losses
 cudaError_t launch_mlp_loss(const float* out, const void* target, int64_t n, float* dout,

@@ -27,10 +27,12 @@
 // clamp01((1 + delta f)/2) of src/FSSW.cpp:1942 are applied as one acceptance
 // probability, so the accepted density is the reference's p^2 f(E) x accept.  The support is cut at the end of the reference's
 // momentum table for the selected sampler (src/MomentumSamplerShell.cpp:24-48).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "learned_record.cuh"
 
 namespace iss {
 
@@ -404,6 +406,7 @@ struct Unit {
     uint32_t t;                // tries made so far (proposal counter)
     int mult;                  // records per draw (2: local charge conservation pair)
     int phase;                 // 1: sampling the partner of a pair
+    const float* lp;           // learned sampler: the pair's mixture record (null: plain)
 };
 
 // Cell draw from 64 random bits r on the fixed-point CDF row C[0..n]
@@ -651,6 +654,182 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Learned proposal.  The target density of a (cell, species) pair in the
+// rest frame, per dK dOmega with K = (E - m)/T, is P(K, n) a(K, n): P is the
+// plain proposal above (Gamma mixture in K, flux-linear direction) and a its
+// acceptance (quantum statistics, pE/(E^2 - m^2/2), flux remainder, delta f),
+// so both samplers accept exactly the reference's p^2 f(E) x weight.  The
+// learned sampler proposes from q = alpha Q + (1 - alpha) P, Q the network's
+// mixture, and accepts with P a / (M q); M is the pair's envelope constant
+// (pair_prepare_kernel).  A ratio above 1 means M was too small there; such
+// proposals are counted (learned_violations).
+
+constexpr float kTwoPi = 6.283185307179586f;
+
+// plain proposal density P and acceptance a at (K, n); false where the
+// target is zero (K beyond the momentum table, p.dsigma < 0).  pl receives
+// the rest-frame four-momentum.
+__device__ __forceinline__ bool plain_target(const DevConfig& cfg, const Prop& p, float K, float nx,
+                                             float ny, float nz, float& P, float& a, float4& pl) {
+    if (!(K > 0.0f) || K > p.Kmax) return false;
+    const float k2 = K * (K + 2.0f * p.mt);
+    const float Et = K + p.mt;
+    const float ptil = sqrtf(k2);
+    const float beta = ptil / Et;
+    const float bD = beta * p.D;
+    float c_lo = -1.0f, r_flux = 1.0f;
+    if (bD > p.d0) {
+        c_lo = -p.d0 / bD;
+        const float s0 = p.d0 + p.D;
+        r_flux = (p.d0 + bD) * (p.d0 + bD) / (beta * s0 * s0);
+    } else if (p.D > p.d0) {
+        const float s0 = p.d0 + p.D;
+        r_flux = 4.0f * p.d0 * p.D / (s0 * s0);
+    }
+    const float cosa = nx * p.nx + ny * p.ny + nz * p.nz;
+    if (cosa < c_lo) return false;
+    const float a_lin = p.d0 + bD * c_lo;
+    const float L = 1.0f - c_lo;
+    const float Zd = a_lin * L + 0.5f * bD * L * L;
+    const float PK = (K * K + 2.0f * p.mt * K + 0.5f * p.mt * p.mt) * expf(-K) / p.W;
+    P = PK * fmaxf(p.d0 + bD * cosa, 0.0f) / (kTwoPi * Zd);
+    const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
+    const float Etil = p.a + K;
+    const float em = expf(-Etil);
+    const float a_q = p.boson ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
+    const float a_c = p.compat ? fminf(compat_ratio(p, Etil) / p.rmax, 1.0f) : 1.0f;
+    const float T = p.T;
+    const float pm = T * ptil;
+    const float p0 = T * Et;
+    const float px = pm * nx, py = pm * ny, pz = pm * nz;
+    const float sgn = static_cast<float>(p.sign);
+    const float f0 = em / (1.0f + sgn * em);
+    const float one_m = 1.0f - sgn * f0;
+    float df = 0.0f;
+    if (cfg.include_shear) {
+        const float Wf = px * px * p.pxx + 2.0f * px * py * p.pxy + 2.0f * px * pz * p.pxz +
+                         py * py * p.pyy + 2.0f * py * pz * p.pyz + pz * pz * (-p.pxx - p.pyy);
+        float ds = one_m * Wf * p.shear_c;
+        if (p.shear_over_p0T) ds /= p0;
+        df += ds;
+    }
+    if (cfg.include_bulk) df += one_m * (p.bi0 / p0 + p.b0 + p.b1 * p0 + p.b2 * p0 * p0);
+    if (cfg.include_diff) {
+        const float qf = -(px * p.qx + py * p.qy + pz * p.qz);
+        df += one_m * (p.pq - p.Bq / p0) * qf;
+    }
+    a = a_pE * a_q * a_c * r_flux * clamp01((1.0f + df) * 0.5f);
+    pl = make_float4(p0, px, py, pz);
+    return true;
+}
+
+// the network's mixture density Q(K, n) per dK dOmega from a pair record
+__device__ __forceinline__ float learned_density(const float* __restrict__ lp, float K, float nx,
+                                                 float ny, float nz) {
+    const float lK = logf(K);
+    const float4* r = reinterpret_cast<const float4*>(lp);
+    float q = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float4 c = __ldg(r + 2 * k);
+        const float4 v = __ldg(r + 2 * k + 1);
+        const float d = (lK - c.z) / c.w;
+        q += expf(c.y - 0.5f * d * d + v.x * nx + v.y * ny + v.z * nz);
+    }
+    return q / K;
+}
+
+// unit vector n around the pair's axis: frame (e1, e2) perpendicular to m
+__device__ __forceinline__ void around(float mx, float my, float mz, float c, float sphi,
+                                       float cphi, float& nx, float& ny, float& nz) {
+    float tx = 0.f, tz = 0.f;
+    if (fabsf(mz) < 0.9f) tz = 1.f; else tx = 1.f;
+    float ex = -tz * my, ey = tz * mx - tx * mz, ez = tx * my;
+    const float inv = rsqrtf(ex * ex + ey * ey + ez * ez);
+    ex *= inv;
+    ey *= inv;
+    ez *= inv;
+    const float fx = my * ez - mz * ey, fy = mz * ex - mx * ez, fz = mx * ey - my * ex;
+    const float s = sqrtf(fmaxf(1.0f - c * c, 0.0f));
+    nx = c * mx + s * (cphi * ex + sphi * fx);
+    ny = c * my + s * (cphi * ey + sphi * fy);
+    nz = c * mz + s * (cphi * ez + sphi * fz);
+}
+
+// one proposal from q = alpha Q + (1 - alpha) P, from the uniforms of A and
+// B (A.x selects the component of q); false when it falls outside the support
+__device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __restrict__ lp,
+                                                float alpha, const uint4& A, const uint4& B,
+                                                float& K, float& nx, float& ny, float& nz) {
+    if (u01f(A.x) < alpha) {
+        const float uc = u01f(A.y);
+        int k = 0;
+        while (k < 7 && uc >= __ldg(lp + 8 * k)) k++;
+        const float4 c = __ldg(reinterpret_cast<const float4*>(lp) + 2 * k);
+        const float4 v = __ldg(reinterpret_cast<const float4*>(lp) + 2 * k + 1);
+        const float uz = (static_cast<float>(A.z >> 8) + 0.5f) * (1.0f / 16777216.0f);
+        const float z = 1.4142135623730951f * erfinvf(2.0f * uz - 1.0f);
+        K = expf(c.z + c.w * z);
+        const float kap = v.w;
+        float mx = 0.f, my = 0.f, mz = 1.f;
+        if (kap > 1e-6f) {
+            mx = v.x / kap;
+            my = v.y / kap;
+            mz = v.z / kap;
+        }
+        const float uw = u01f(A.w);
+        const float w = kap < 1e-4f ? 2.0f * uw - 1.0f
+                                    : fmaxf(-1.0f, 1.0f + log1pf((1.0f - uw) * expm1f(-2.0f * kap)) / kap);
+        float sphi, cphi;
+        sincospif(2.0f * u01f(B.y), &sphi, &cphi);
+        around(mx, my, mz, fminf(w, 1.0f), sphi, cphi, nx, ny, nz);
+        return true;
+    }
+    const float sel = u01f(A.y) * p.W;
+    float prod = u01f_pos(A.z);
+    if (sel < p.w32) prod *= u01f_pos(A.w);
+    if (sel < p.w3) prod *= u01f_pos(B.x);
+    K = -logf(prod);
+    if (K > p.Kmax) return false;
+    const float k2 = K * (K + 2.0f * p.mt);
+    const float beta = sqrtf(k2) / (K + p.mt);
+    const float bD = beta * p.D;
+    const float c_lo = bD > p.d0 ? -p.d0 / bD : -1.0f;
+    const float a_lin = p.d0 + bD * c_lo;
+    const float L = 1.0f - c_lo;
+    const float uZ = u01f(B.y) * (a_lin * L + 0.5f * bD * L * L);
+    const float cth = fminf(c_lo + 2.0f * uZ / (a_lin + sqrtf(a_lin * a_lin + 2.0f * bD * uZ)), 1.0f);
+    float sphi, cphi;
+    sincospif(2.0f * u01f(B.z), &sphi, &cphi);
+    around(p.nx, p.ny, p.nz, cth, sphi, cphi, nx, ny, nz);
+    return true;
+}
+
+// one learned proposal and its accept step
+__device__ __forceinline__ bool try_learned(const DevConfig& cfg, const Prop& p, const Unit& u,
+                                            const float* __restrict__ lp, float4& pl, float& u_rap,
+                                            unsigned& violations) {
+    const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagLearn << 16);
+    const uint4 A = block(2u * u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    const uint4 B = block(2u * u.t + 1u, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    float K, nx, ny, nz, P, a;
+    if (!propose_mixture(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) return false;
+    if (!plain_target(cfg, p, K, nx, ny, nz, P, a, pl)) return false;
+    const float Q = learned_density(lp, K, nx, ny, nz);
+    const float M = __ldg(lp + 56);
+    const float r = P * a / (M * (cfg.lalpha * Q + (1.0f - cfg.lalpha) * P));
+    if (r > 1.0f) violations++;
+    if (!(u01f(B.w) < r)) return false;
+    u_rap = 0.0f;
+    if (cfg.hydro_mode != 2) {
+        const uint4 C = block(u.t, u.i, u.eg, static_cast<uint32_t>(u.s) | (kTagLearnRap << 16),
+                              cfg.key0, cfg.key1);
+        u_rap = u01f(C.x);
+    }
+    return true;
+}
+
 __device__ __forceinline__ void write_hadron(HadronRec* out, int64_t slot, int pid, float mass,
                                              float E, float px, float py, float pz, float t,
                                              float x, float y, float z) {
@@ -779,14 +958,14 @@ constexpr int kSampleThreads = 256;
 
 // kLcc: local_charge_conservation pairs (a separate instantiation, so the
 // common case carries none of the pair state)
-template <bool kLcc>
+template <bool kLcc, bool kLearned>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
                const int32_t* __restrict__ guide,
                const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
-               int64_t k_begin, int64_t k_end, const int32_t* __restrict__ cell_of,
+               int64_t k_begin, int64_t k_end, int32_t* __restrict__ cell_of,
                HadronRec* __restrict__ out,
                unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
     const unsigned FULL = 0xffffffffu;
@@ -801,6 +980,7 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
     int pid = 0;
     unsigned long long n_tries = 0, n_redraws = 0, n_fail = 0;
     unsigned n_viol = 0;
+    unsigned n_ltries = 0, n_lviol = 0, n_lhad = 0;
 
     for (;;) {
         // hand out units to the lanes that have none
@@ -838,6 +1018,7 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                 u.t = 0;
                 u.tries_cell = 0;
                 u.cell = -1;
+                u.lp = nullptr;
                 pid = pids[u.s];
                 active = true;
             }
@@ -887,6 +1068,11 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                 }
                 u.cell = l;
                 u.tries_cell = 0;
+                if (kLearned) {
+                    const int sl = cfg.lslot[u.s];
+                    u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
+                                   : nullptr;
+                }
                 if (!setup_prop(cfg, cells, species[u.s], l, p)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
@@ -899,11 +1085,21 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
             }
             float4 pl;
             float u_rap;
-            const bool ok = try_once(cfg, p, u, pl, u_rap, n_viol);
+            bool ok;
+            if (kLearned && u.lp) {
+                ok = try_learned(cfg, p, u, u.lp, pl, u_rap, n_lviol);
+                n_ltries++;
+                n_lhad += ok;
+            } else {
+                ok = try_once(cfg, p, u, pl, u_rap, n_viol);
+            }
             u.t++;
             u.tries_cell++;
             n_tries++;
             if (ok) {
+                // the final cell of a redrawn hadron (cell_of then holds every
+                // hadron's cell: the training rows of the learned proposal)
+                if (u.redraw > 0 && u.phase == 0) cell_of[u.slot] = u.cell;
                 if (kLcc)
                     emit(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out, u.slot + u.phase);
                 else
@@ -916,6 +1112,7 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                     sp2.charge = -sp2.charge;
                     u.phase = 1;
                     u.tries_cell = 0;
+                    u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
                     if (!setup_prop(cfg, cells, sp2, u.cell, p)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
@@ -936,13 +1133,195 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
         n_redraws += __shfl_down_sync(FULL, n_redraws, o);
         n_fail += __shfl_down_sync(FULL, n_fail, o);
         n_viol += __shfl_down_sync(FULL, n_viol, o);
+        if (kLearned) {
+            n_ltries += __shfl_down_sync(FULL, n_ltries, o);
+            n_lviol += __shfl_down_sync(FULL, n_lviol, o);
+            n_lhad += __shfl_down_sync(FULL, n_lhad, o);
+        }
     }
     if (lane == 0) {
         atomicAdd(&ctrs->tries, n_tries);
         if (n_redraws) atomicAdd(&ctrs->redraws, n_redraws);
         if (n_fail) atomicAdd(&ctrs->failures, n_fail);
         if (n_viol) atomicAdd(&ctrs->bound_violations, static_cast<unsigned long long>(n_viol));
+        if (kLearned) {
+            if (n_ltries) atomicAdd(&ctrs->learned_tries, static_cast<unsigned long long>(n_ltries));
+            if (n_lviol) atomicAdd(&ctrs->learned_violations, static_cast<unsigned long long>(n_lviol));
+            if (n_lhad) atomicAdd(&ctrs->learned_hadrons, static_cast<unsigned long long>(n_lhad));
+        }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Learned proposal: network inputs, per-pair mixture records, envelope
+// constants, and training rows from sampled hadrons.
+
+// the 18 conditioning features of a (cell, species) pair (order and scales
+// as declared in iss_gpu.h)
+__device__ __forceinline__ void pair_features(const float4* __restrict__ rec, const SpeciesDev& sp,
+                                              float (&f)[18]) {
+    const float4 da = __ldg(rec + 1), th = __ldg(rec + 3), th2 = __ldg(rec + 4);
+    const float4 pi1 = __ldg(rec + 5), pi2 = __ldg(rec + 6);
+    const float T = th.x;
+    const float m = sp.m_hi + sp.m_lo;
+    const float mu = fminf(m, static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
+                                  static_cast<float>(sp.charge) * th.w);
+    const float iep = 1.0f / (th2.x + th2.y);
+    f[0] = (T - 0.15f) * 50.0f;
+    f[1] = 0.5f * mu / T;
+    f[2] = pi1.x * iep * 10.0f;
+    f[3] = pi1.y * iep * 10.0f;
+    f[4] = pi1.z * iep * 10.0f;
+    f[5] = pi1.w * iep * 10.0f;
+    f[6] = pi2.x * iep * 10.0f;
+    f[7] = th2.w * iep * 20.0f;
+    f[8] = 0.0f;
+    f[9] = pi2.y * iep * 10.0f;
+    f[10] = pi2.z * iep * 10.0f;
+    f[11] = pi2.w * iep * 10.0f;
+    const float D = sqrtf(da.y * da.y + da.z * da.z + da.w * da.w);
+    const float nrm = fabsf(da.x) + D;
+    const float inrm = nrm > 0.0f ? 1.0f / nrm : 0.0f;
+    f[12] = da.x * inrm;
+    f[13] = da.y * inrm;
+    f[14] = da.z * inrm;
+    f[15] = da.w * inrm;
+    f[16] = 0.1f * m / T;
+    f[17] = static_cast<float>(sp.sign);
+}
+
+__device__ __forceinline__ void store_features(const float (&f)[18], __nv_bfloat16* __restrict__ x) {
+    uint4 w[4];
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(w);
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const float a = 2 * j < 18 ? f[2 * j < 18 ? 2 * j : 0] : 0.0f;
+        const float b = 2 * j + 1 < 18 ? f[2 * j + 1 < 18 ? 2 * j + 1 : 0] : 0.0f;
+        h[j] = __floats2bfloat162_rn(a, b);
+    }
+    uint4* o = reinterpret_cast<uint4*>(x);
+#pragma unroll
+    for (int j = 0; j < 4; j++) o[j] = w[j];
+}
+
+// network input of pair (slot, cell) = slot * n_cells + cell
+__global__ void learned_pair_features_kernel(CellArrays cells, const SpeciesDev* __restrict__ species,
+                                             const int32_t* __restrict__ lspecies, int64_t n_cells,
+                                             int64_t n_pairs, __nv_bfloat16* __restrict__ x) {
+    const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const int slot = static_cast<int>(q / n_cells);
+    const int64_t l = q - slot * n_cells;
+    float f[18];
+    pair_features(cells.rec + 8 * l, species[lspecies[slot]], f);
+    store_features(f, x + q * 32);
+}
+
+// envelope constant M of every pair: safety x the largest ratio
+// P a / (alpha Q + (1 - alpha) P) over n_pilot proposals from q (Philox
+// counter (draw, pair low, pair high, tag)), capped by the bound 1/(1 - alpha)
+// that holds for every Q >= 0
+__global__ void learned_pair_envelope_kernel(DevConfig cfg, CellArrays cells,
+                                             const SpeciesDev* __restrict__ species,
+                                             const int32_t* __restrict__ lspecies, int64_t n_cells,
+                                             int64_t n_pairs, int n_pilot, float safety,
+                                             float* __restrict__ lpairs) {
+    const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const int slot = static_cast<int>(q / n_cells);
+    const int64_t l = q - slot * n_cells;
+    float* lp = lpairs + q * kPairFloats;
+    const float cap = 1.0f / (1.0f - cfg.lalpha);
+    Prop p;
+    const float4 da = __ldg(cells.rec + 8 * l + 1);
+    float best = 0.0f;
+    if (da.x >= 0.0f && setup_prop(cfg, cells, species[lspecies[slot]], static_cast<int>(l), p)) {
+        for (int j = 0; j < n_pilot; j++) {
+            const uint32_t c3 = static_cast<uint32_t>(q >> 32) | (kTagPilot << 16);
+            const uint4 A = block(2u * j, static_cast<uint32_t>(q), 0u, c3, cfg.key0, cfg.key1);
+            const uint4 B = block(2u * j + 1u, static_cast<uint32_t>(q), 0u, c3, cfg.key0, cfg.key1);
+            float K, nx, ny, nz, P, a;
+            float4 pl;
+            if (!propose_mixture(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) continue;
+            if (!plain_target(cfg, p, K, nx, ny, nz, P, a, pl)) continue;
+            const float Q = learned_density(lp, K, nx, ny, nz);
+            const float r = P * a / (cfg.lalpha * Q + (1.0f - cfg.lalpha) * P);
+            if (r > best) best = r;
+        }
+    }
+    lp[56] = best > 0.0f ? fminf(safety * best, cap) : cap;
+}
+
+// training rows from sampled hadrons: the pair's features and the rest-frame
+// target (K, n); the species from the PDG id (sorted_pid / sorted_idx), the
+// cell from cell_of.  Rows whose id is not a sampled species get K = 0 and
+// are skipped by the host.
+__device__ __forceinline__ void learned_train_row(
+    const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* __restrict__ species,
+    const int32_t* __restrict__ sorted_pid, const int32_t* __restrict__ sorted_idx, int S,
+    const HadronRec* __restrict__ had, const int32_t* __restrict__ cell_of, int64_t n,
+    __nv_bfloat16* __restrict__ x, float4* __restrict__ tg, int64_t i, float& nll) {
+    if (i >= n) return;
+    const HadronRec h = had[i];
+    int lo = 0, hi = S - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sorted_pid[mid] < h.pid) lo = mid + 1; else hi = mid;
+    }
+    float f[18];
+    if (S == 0 || sorted_pid[lo] != h.pid) {
+        for (int j = 0; j < 18; j++) f[j] = 0.0f;
+        store_features(f, x + i * 32);
+        tg[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        return;
+    }
+    const SpeciesDev sp = species[sorted_idx[lo]];
+    const int64_t l = cell_of[i];
+    const float4* rec = cells.rec + 8 * l;
+    pair_features(rec, sp, f);
+    store_features(f, x + i * 32);
+    const float4 u = __ldg(rec + 2), pos = __ldg(rec), th = __ldg(rec + 3);
+    const float m = sp.m_hi + sp.m_lo;
+    float E = h.E, pz = h.pz;
+    if (cfg.hydro_mode != 2) {
+        // boost-invariant records carry a drawn rapidity: back to the cell's frame
+        const float mT = sqrtf(m * m + h.px * h.px + h.py * h.py);
+        const float y = asinhf(h.pz / mT) - atanhf(h.z / h.t) + pos.w;
+        E = mT * coshf(y);
+        pz = mT * sinhf(y);
+    }
+    const float udp = u.y * h.px + u.z * h.py + u.w * pz;
+    const float c = E - udp / (u.x + 1.0f);
+    const float px = h.px - c * u.y, py = h.py - c * u.z, pzr = pz - c * u.w;
+    const float p2 = px * px + py * py + pzr * pzr;
+    const float pm = sqrtf(p2);
+    const float K = p2 / (sqrtf(m * m + p2) + m) / th.x;
+    const float ip = pm > 0.0f ? 1.0f / pm : 0.0f;
+    tg[i] = make_float4(K, px * ip, py * ip, pzr * ip);
+    Prop p;
+    float P, a;
+    float4 pl;
+    if (setup_prop(cfg, cells, sp, static_cast<int>(l), p) &&
+        plain_target(cfg, p, K, px * ip, py * ip, pzr * ip, P, a, pl) && P > 0.0f)
+        nll = -logf(P);
+}
+
+__global__ void learned_train_rows_kernel(DevConfig cfg, CellArrays cells,
+                                          const SpeciesDev* __restrict__ species,
+                                          const int32_t* __restrict__ sorted_pid,
+                                          const int32_t* __restrict__ sorted_idx, int S,
+                                          const HadronRec* __restrict__ had,
+                                          const int32_t* __restrict__ cell_of, int64_t n,
+                                          __nv_bfloat16* __restrict__ x, float4* __restrict__ tg,
+                                          double* __restrict__ nll_plain) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    float nll = 0.0f;
+    learned_train_row(cfg, cells, species, sorted_pid, sorted_idx, S, had, cell_of, n, x, tg, i, nll);
+    // the plain proposal's negative log-likelihood of the rows (the network's
+    // loss on the same rows measures what it gains over the plain proposal)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nll += __shfl_xor_sync(0xffffffffu, nll, o);
+    if ((threadIdx.x & 31) == 0 && nll != 0.0f) atomicAdd(nll_plain, static_cast<double>(nll));
 }
 
 }  // namespace
@@ -1003,10 +1382,43 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    auto kernel = cfg.lcc ? sampler_kernel<true> : sampler_kernel<false>;
+    auto kernel = cfg.lpairs ? (cfg.lcc ? sampler_kernel<true, true> : sampler_kernel<false, true>)
+                             : (cfg.lcc ? sampler_kernel<true, false> : sampler_kernel<false, false>);
     kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_learned_pairs(const DevConfig& cfg, const CellArrays& cells,
+                                 const SpeciesDev* species, const int32_t* lspecies, int n_slots,
+                                 void* x, cudaStream_t stream) {
+    const int64_t n_pairs = static_cast<int64_t>(n_slots) * cfg.n_cells;
+    if (n_pairs <= 0) return cudaSuccess;
+    learned_pair_features_kernel<<<static_cast<unsigned>((n_pairs + 255) / 256), 256, 0, stream>>>(
+        cells, species, lspecies, cfg.n_cells, n_pairs, static_cast<__nv_bfloat16*>(x));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_learned_envelopes(const DevConfig& cfg, const CellArrays& cells,
+                                     const SpeciesDev* species, const int32_t* lspecies, int n_slots,
+                                     int n_pilot, float safety, float* lpairs, cudaStream_t stream) {
+    const int64_t n_pairs = static_cast<int64_t>(n_slots) * cfg.n_cells;
+    if (n_pairs <= 0) return cudaSuccess;
+    learned_pair_envelope_kernel<<<static_cast<unsigned>((n_pairs + 127) / 128), 128, 0, stream>>>(
+        cfg, cells, species, lspecies, cfg.n_cells, n_pairs, n_pilot, safety, lpairs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_learned_train_rows(const DevConfig& cfg, const CellArrays& cells,
+                                      const SpeciesDev* species, const int32_t* sorted_pid,
+                                      const int32_t* sorted_idx, int S, const HadronRec* had,
+                                      const int32_t* cell_of, int64_t n, void* x, void* tg,
+                                      double* nll_plain, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    learned_train_rows_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(
+        cfg, cells, species, sorted_pid, sorted_idx, S, had, cell_of, n,
+        static_cast<__nv_bfloat16*>(x), static_cast<float4*>(tg), nll_plain);
     return cudaGetLastError();
 }
 

@@ -39,7 +39,8 @@ EXPORTED = [
     "iss_gpu_last_error", "iss_gpu_status_string", "iss_gpu_scan_counts_noalloc",
     "iss_gpu_learned_num_weights", "iss_gpu_learned_init_weights", "iss_gpu_learned_set_weights",
     "iss_gpu_learned_get_weights", "iss_gpu_learned_forward", "iss_gpu_learned_loss_grad",
-    "iss_gpu_mma_selftest",
+    "iss_gpu_mma_selftest", "iss_gpu_learned_train", "iss_gpu_learned_stats",
+    "iss_gpu_learned_copy_rows",
 ]
 
 
@@ -49,6 +50,23 @@ class Timings(C.Structure):
                 ("n_hadrons", C.c_int64), ("n_tries", C.c_int64),
                 ("n_cell_redraws", C.c_int64), ("n_failures", C.c_int64),
                 ("kernel_launches", C.c_int32), ("ms_decays", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LearnedTrain(C.Structure):
+    _fields_ = [("n_momenta", C.c_int64), ("first_seed", C.c_int32), ("n_seeds", C.c_int32),
+                ("n_steps", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_double),
+                ("init_seed", C.c_uint64)]
+
+
+class LearnedStats(C.Structure):
+    _fields_ = [("n_species", C.c_int32), ("n_pairs", C.c_int64), ("ms_network", C.c_double),
+                ("n_tries", C.c_int64), ("n_hadrons", C.c_int64), ("n_violations", C.c_int64),
+                ("n_train_rows", C.c_int64), ("ms_train", C.c_double),
+                ("train_events_per_seed", C.c_int32), ("train_nll_plain", C.c_double),
+                ("ms_forward", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -112,6 +130,9 @@ def lib():
         L.iss_gpu_learned_forward.argtypes = [h, v, C.c_int64, v]
         L.iss_gpu_learned_loss_grad.argtypes = [h, v, v, C.c_int64, C.POINTER(C.c_double), v]
         L.iss_gpu_mma_selftest.argtypes = [v, v, C.c_int32, C.c_int32, v]
+        L.iss_gpu_learned_train.argtypes = [h, C.POINTER(LearnedTrain), v, C.c_int32]
+        L.iss_gpu_learned_stats.argtypes = [h, C.POINTER(LearnedStats)]
+        L.iss_gpu_learned_copy_rows.argtypes = [h, C.c_int64, C.c_int64, v, v]
         for name in EXPORTED:
             if name not in ("iss_gpu_last_error", "iss_gpu_status_string"):
                 getattr(L, name).restype = C.c_int
@@ -343,6 +364,28 @@ class iSS:
         self._check(self._L.iss_gpu_learned_loss_grad(self._h, _ptr(f), _ptr(t), f.shape[0],
                                                       C.byref(loss), _ptr(g)))
         return loss.value, g
+
+
+    def learned_train(self, n_momenta=50_000_000, first_seed=10, n_seeds=10, n_steps=2000,
+                      batch=8192, learning_rate=1e-3, init_seed=0):
+        """Train the proposal network on momenta of the plain sampler; returns
+        the mean loss of every step."""
+        o = LearnedTrain(int(n_momenta), int(first_seed), int(n_seeds), int(n_steps), int(batch),
+                         float(learning_rate), int(init_seed))
+        curve = np.zeros(max(int(n_steps), 1), dtype=np.float64)
+        self._check(self._L.iss_gpu_learned_train(self._h, C.byref(o), _ptr(curve), curve.size))
+        return curve[:int(n_steps)]
+
+    def learned_stats(self):
+        st = LearnedStats()
+        self._check(self._L.iss_gpu_learned_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def learned_rows(self, first, count):
+        f = np.zeros((count, 18), dtype=np.float32)
+        t = np.zeros((count, 4), dtype=np.float32)
+        self._check(self._L.iss_gpu_learned_copy_rows(self._h, int(first), int(count), _ptr(f), _ptr(t)))
+        return f, t
 
 
 def mma_selftest(a_bf16, b_bf16):
