@@ -310,16 +310,18 @@ def learned_report(s, timings, args):
     out["plain_ms_per_step"] = s.timings()["ms_total"]
     out["plain_tries_per_hadron_all_species"] = (s.timings()["n_tries"] /
                                                  max(s.timings()["n_hadrons"], 1))
-    ev = s.getVal("number_of_repeated_sampling")
-    s.set_params(number_of_repeated_sampling=min(100, int(ev)))
+    # the same events as the timed steps (so the same species take the
+    # learned proposal); spectra of the first 100 events
+    n_cmp = min(100, int(s.getVal("number_of_repeated_sampling")))
     s.set_random_seed(99)
     s.generate_samples()
-    plain, _ = s.all_hadrons()
+    plain, off = s.all_hadrons()
+    plain = plain[:off[n_cmp]]
     s.set_params(gpu_sampler=1)
     s.set_random_seed(99)
     s.generate_samples()
-    lrn, _ = s.all_hadrons()
-    s.set_params(number_of_repeated_sampling=int(ev))
+    lrn, off = s.all_hadrons()
+    lrn = lrn[:off[n_cmp]]
     pv = {}
     for pid in (211, -211, 111, 321, -321, 2212):
         a, b = plain[plain["pid"] == pid], lrn[lrn["pid"] == pid]
@@ -345,7 +347,7 @@ def learned_report(s, timings, args):
             if len(ca) > 100 and len(cb) > 100:
                 zs.append((ca.mean() - cb.mean()) / np.sqrt(ca.var() / len(ca) + cb.var() / len(cb)))
         pv[f"{pid}_v2_chi2"] = float(stats.chi2.sf(np.sum(np.square(zs)), len(zs))) if zs else 1.0
-    out["spectra_vs_plain"] = {"events": min(100, int(ev)), "min_p": min(pv.values()) if pv else None,
+    out["spectra_vs_plain"] = {"events": n_cmp, "min_p": min(pv.values()) if pv else None,
                                "tests": len(pv), "p_values": pv}
     s.set_params(gpu_sampler=1)
     return out

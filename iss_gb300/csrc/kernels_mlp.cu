@@ -90,42 +90,76 @@ mma_selftest_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __
 }
 
 // ---------------------------------------------------------------------------
-// forward: out = f(X) for n rows; hidden activations kept for training
+// forward: out = f(X) for n rows; hidden activations kept for training.
+//
+// kFwdWG warpgroups per CTA share the weight images in shared memory; each
+// warpgroup g owns one 128-row tile at a time, its own activation buffer
+// (which first holds the tile's inputs), TMEM columns [128 g, 128 g + 128),
+// an mbarrier and a named barrier, so one tile's epilogue overlaps another
+// tile's GEMMs on the tensor core.
 
-constexpr int kFwdSmem = static_cast<int>(kFwdImgElems * 2) + kTile * kIn0 * 2 + kTile * kHid * 2 + 64;
+constexpr int kFwdWG = 3;
+constexpr int kFwdThreads = 128 * kFwdWG;
+constexpr int kFwdSmem = static_cast<int>(kFwdImgElems * 2) + kFwdWG * kTile * kHid * 2 + 64;
 
-__global__ void __launch_bounds__(128, 1)
+// barrier over the 128 threads of warpgroup `id - 1` (named barrier `id`)
+__device__ __forceinline__ void wg_sync(int id) {
+    asm volatile("bar.sync %0, 128;" :: "r"(id) : "memory");
+}
+__device__ __forceinline__ bool wg_sync_and(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r) : "r"(static_cast<uint32_t>(v)), "r"(id) : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void wg_sync_for_mma(int id) {
+    fence_smem_to_async();
+    fence_before_sync();
+    wg_sync(id);
+    fence_after_sync();
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1)
 mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ params,
                const __nv_bfloat16* __restrict__ X, int64_t n, float* __restrict__ out,
                __nv_bfloat16* __restrict__ acts, float* __restrict__ records,
                int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sW = smem;
-    uint8_t* sX = sW + kFwdImgElems * 2;
-    uint8_t* sH = sX + kTile * kIn0 * 2;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sH + kTile * kHid * 2);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-    const int t = threadIdx.x, warp = t >> 5;
+    const int g = threadIdx.x >> 7;            // warpgroup
+    const int t = threadIdx.x & 127;           // row of the warpgroup's tile
+    const int warp = threadIdx.x >> 5;
+    const int bar_id = 1 + g;
+    uint8_t* sH = sW + kFwdImgElems * 2 + g * (kTile * kHid * 2);   // inputs, then activations
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sW + kFwdImgElems * 2 + kFwdWG * kTile * kHid * 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kFwdWG);
     {
         const uint4* src = reinterpret_cast<const uint4*>(img);
         uint4* dst = reinterpret_cast<uint4*>(sW);
-        for (int i = t; i < static_cast<int>(kFwdImgElems * 2 / 16); i += 128) dst[i] = src[i];
+        for (int i = threadIdx.x; i < static_cast<int>(kFwdImgElems * 2 / 16); i += kFwdThreads)
+            dst[i] = src[i];
     }
-    if (t == 0) {
-        mbar_init(bar, 1);
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < kFwdWG; w++) mbar_init(bars + w, 1);
         barrier_init_fence();
     }
     if (warp == 0) {
-        tmem_alloc(tslot, 128);
+        tmem_alloc(tslot, 512);
         tmem_relinquish();
     }
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    const uint32_t tmem = *tslot;
+    const uint32_t tmem = *tslot + 128u * g;
+    uint64_t* bar = bars + g;
     uint32_t phase = 0;
     const int64_t n_tiles = (n + kTile - 1) / kTile;
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kFwdWG + g; tile < n_tiles;
+         tile += static_cast<int64_t>(gridDim.x) * kFwdWG) {
         const int64_t row = tile * kTile + t;
         const bool valid = row < n;
         {
@@ -133,22 +167,22 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
 #pragma unroll
             for (int c = 0; c < kIn0 / 8; c++) {
                 const uint4 v = valid ? xs[c] : make_uint4(0, 0, 0, 0);
-                *reinterpret_cast<uint4*>(sX + kmajor_offset(t, 8 * c, kIn0)) = v;
+                *reinterpret_cast<uint4*>(sH + kmajor_offset(t, 8 * c, kIn0)) = v;
             }
         }
-        sync_for_mma();
+        wg_sync_for_mma(bar_id);
         bool ok = true;
         for (int l = 0; l < kLayers; l++) {
             const int K = dim_in(l), N = dim_out(l);
             if (t == 0) {
-                const uint32_t a = smem_addr(l == 0 ? sX : sH);
+                const uint32_t a = smem_addr(sH);
                 const uint32_t b = smem_addr(sW) + static_cast<uint32_t>(fwd_img_offset(l) * 2);
                 const uint32_t id = idesc_bf16_f32(128, N);
                 for (int ks = 0; ks < K / 16; ks++)
                     mma_bf16(tmem, kslice_desc(a, K, ks), kslice_desc(b, K, ks), id, ks > 0);
                 mma_commit(bar);
             }
-            ok = __syncthreads_and(mbar_wait(bar, phase, err, 2));
+            ok = wg_sync_and(bar_id, mbar_wait(bar, phase, err, 2));
             phase ^= 1u;
             if (!ok) break;
             fence_after_sync();
@@ -174,9 +208,9 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
                     }
                 }
             } else if (records) {
-                // fused epilogue: the row's mixture record, staged in shared
-                // memory (sH is free once the last GEMM has completed), then
-                // stored for the whole tile with coalesced 16-byte stores
+                // fused epilogue: the row's mixture record, staged in the
+                // warpgroup's buffer (free once the last GEMM has completed),
+                // then stored for the whole tile with coalesced 16-byte stores
                 float z[64];
                 tmem_ld32(tmem_lane_addr(tmem, warp, 0), *reinterpret_cast<float(*)[32]>(z));
                 tmem_ld32(tmem_lane_addr(tmem, warp, 32), *reinterpret_cast<float(*)[32]>(z + 32));
@@ -184,7 +218,7 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
                 for (int j = 0; j < kOutUsed; j++) z[j] += __ldg(bias + j);
                 float* r = reinterpret_cast<float*>(sH) + t * kOut;
                 mixture_record(z, r);
-                __syncthreads();
+                wg_sync(bar_id);
                 const int64_t rows = min(static_cast<int64_t>(kTile), n - tile * kTile);
                 const float4* src = reinterpret_cast<const float4*>(sH);
                 float4* dst = reinterpret_cast<float4*>(records + tile * kTile * kOut);
@@ -204,13 +238,13 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
                     }
                 }
             }
-            sync_for_mma();
+            wg_sync_for_mma(bar_id);
         }
         if (!ok) break;
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 128);
+    if (warp == 0) tmem_dealloc(*tslot, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -602,9 +636,9 @@ cudaError_t launch_mlp_forward(const void* img, const float* params, const void*
     if (n <= 0) return cudaSuccess;
     cudaError_t e = smem_opt_in(mlp_fwd_kernel, kFwdSmem, &g_fwd_attr);
     if (e != cudaSuccess) return e;
-    const int64_t tiles = (n + kTile - 1) / kTile;
-    const int grid = static_cast<int>(tiles < num_sms ? tiles : num_sms);
-    mlp_fwd_kernel<<<grid, 128, kFwdSmem, s>>>(static_cast<const __nv_bfloat16*>(img), params,
+    const int64_t groups = (n + kTile * kFwdWG - 1) / (kTile * kFwdWG);
+    const int grid = static_cast<int>(groups < num_sms ? groups : num_sms);
+    mlp_fwd_kernel<<<grid, kFwdThreads, kFwdSmem, s>>>(static_cast<const __nv_bfloat16*>(img), params,
                                                static_cast<const __nv_bfloat16*>(X), n, out,
                                                static_cast<__nv_bfloat16*>(acts), records, err);
     return cudaGetLastError();

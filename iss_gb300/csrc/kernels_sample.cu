@@ -724,16 +724,29 @@ __device__ __forceinline__ bool plain_target(const DevConfig& cfg, const Prop& p
     return true;
 }
 
+// a pair record's float4 j: through the read-only cache (global records) or
+// a plain load (records staged in shared memory)
+template <bool kShared>
+__device__ __forceinline__ float4 rec4(const float* lp, int j) {
+    if (kShared) return reinterpret_cast<const float4*>(lp)[j];
+    return __ldg(reinterpret_cast<const float4*>(lp) + j);
+}
+template <bool kShared>
+__device__ __forceinline__ float rec1(const float* lp, int j) {
+    if (kShared) return lp[j];
+    return __ldg(lp + j);
+}
+
 // the network's mixture density Q(K, n) per dK dOmega from a pair record
+template <bool kShared = false>
 __device__ __forceinline__ float learned_density(const float* __restrict__ lp, float K, float nx,
                                                  float ny, float nz) {
     const float lK = logf(K);
-    const float4* r = reinterpret_cast<const float4*>(lp);
     float q = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        const float4 c = __ldg(r + 2 * k);
-        const float4 v = __ldg(r + 2 * k + 1);
+        const float4 c = rec4<kShared>(lp, 2 * k);
+        const float4 v = rec4<kShared>(lp, 2 * k + 1);
         const float d = (lK - c.z) / c.w;
         q += expf(c.y - 0.5f * d * d + v.x * nx + v.y * ny + v.z * nz);
     }
@@ -759,15 +772,16 @@ __device__ __forceinline__ void around(float mx, float my, float mz, float c, fl
 
 // one proposal from q = alpha Q + (1 - alpha) P, from the uniforms of A and
 // B (A.x selects the component of q); false when it falls outside the support
+template <bool kShared = false>
 __device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __restrict__ lp,
                                                 float alpha, const uint4& A, const uint4& B,
                                                 float& K, float& nx, float& ny, float& nz) {
     if (u01f(A.x) < alpha) {
         const float uc = u01f(A.y);
         int k = 0;
-        while (k < 7 && uc >= __ldg(lp + 8 * k)) k++;
-        const float4 c = __ldg(reinterpret_cast<const float4*>(lp) + 2 * k);
-        const float4 v = __ldg(reinterpret_cast<const float4*>(lp) + 2 * k + 1);
+        while (k < 7 && uc >= rec1<kShared>(lp, 8 * k)) k++;
+        const float4 c = rec4<kShared>(lp, 2 * k);
+        const float4 v = rec4<kShared>(lp, 2 * k + 1);
         const float uz = (static_cast<float>(A.z >> 8) + 0.5f) * (1.0f / 16777216.0f);
         const float z = 1.4142135623730951f * erfinvf(2.0f * uz - 1.0f);
         K = expf(c.z + c.w * z);
@@ -1217,6 +1231,8 @@ __global__ void learned_pair_features_kernel(CellArrays cells, const SpeciesDev*
     store_features(f, x + q * 32);
 }
 
+constexpr int kEnvThreads = 128;
+
 // envelope constant M of every pair: safety x the largest ratio
 // P a / (alpha Q + (1 - alpha) P) over n_pilot proposals from q (Philox
 // counter (draw, pair low, pair high, tag)), capped by the bound 1/(1 - alpha)
@@ -1226,11 +1242,25 @@ __global__ void learned_pair_envelope_kernel(DevConfig cfg, CellArrays cells,
                                              const int32_t* __restrict__ lspecies, int64_t n_cells,
                                              int64_t n_pairs, int n_pilot, float safety,
                                              float* __restrict__ lpairs) {
-    const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // the block's records, staged once: every pilot proposal reads its
+    // pair's record twice (component draw and density)
+    // (a row stride of 17 float4: the lanes of a warp reading float4 j of
+    // their own records hit distinct banks)
+    constexpr int kRow = kPairFloats / 4 + 1;
+    __shared__ float4 s_rec[kEnvThreads * kRow];
+    const int64_t q0 = static_cast<int64_t>(blockIdx.x) * kEnvThreads;
+    const int64_t nq = min(static_cast<int64_t>(kEnvThreads), n_pairs - q0);
+    {
+        const float4* src = reinterpret_cast<const float4*>(lpairs + q0 * kPairFloats);
+        for (int i = threadIdx.x; i < nq * (kPairFloats / 4); i += kEnvThreads)
+            s_rec[(i / (kPairFloats / 4)) * kRow + i % (kPairFloats / 4)] = src[i];
+    }
+    __syncthreads();
+    const int64_t q = q0 + threadIdx.x;
     if (q >= n_pairs) return;
     const int slot = static_cast<int>(q / n_cells);
     const int64_t l = q - slot * n_cells;
-    float* lp = lpairs + q * kPairFloats;
+    const float* lp = reinterpret_cast<const float*>(s_rec + threadIdx.x * kRow);
     const float cap = 1.0f / (1.0f - cfg.lalpha);
     Prop p;
     const float4 da = __ldg(cells.rec + 8 * l + 1);
@@ -1242,14 +1272,14 @@ __global__ void learned_pair_envelope_kernel(DevConfig cfg, CellArrays cells,
             const uint4 B = block(2u * j + 1u, static_cast<uint32_t>(q), 0u, c3, cfg.key0, cfg.key1);
             float K, nx, ny, nz, P, a;
             float4 pl;
-            if (!propose_mixture(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) continue;
+            if (!propose_mixture<true>(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) continue;
             if (!plain_target(cfg, p, K, nx, ny, nz, P, a, pl)) continue;
-            const float Q = learned_density(lp, K, nx, ny, nz);
+            const float Q = learned_density<true>(lp, K, nx, ny, nz);
             const float r = P * a / (cfg.lalpha * Q + (1.0f - cfg.lalpha) * P);
             if (r > best) best = r;
         }
     }
-    lp[56] = best > 0.0f ? fminf(safety * best, cap) : cap;
+    lpairs[q * kPairFloats + 56] = best > 0.0f ? fminf(safety * best, cap) : cap;
 }
 
 // training rows from sampled hadrons: the pair's features and the rest-frame
@@ -1405,7 +1435,8 @@ cudaError_t launch_learned_envelopes(const DevConfig& cfg, const CellArrays& cel
                                      int n_pilot, float safety, float* lpairs, cudaStream_t stream) {
     const int64_t n_pairs = static_cast<int64_t>(n_slots) * cfg.n_cells;
     if (n_pairs <= 0) return cudaSuccess;
-    learned_pair_envelope_kernel<<<static_cast<unsigned>((n_pairs + 127) / 128), 128, 0, stream>>>(
+    learned_pair_envelope_kernel<<<static_cast<unsigned>((n_pairs + kEnvThreads - 1) / kEnvThreads),
+                                   kEnvThreads, 0, stream>>>(
         cfg, cells, species, lspecies, cfg.n_cells, n_pairs, n_pilot, safety, lpairs);
     return cudaGetLastError();
 }
