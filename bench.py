@@ -13,6 +13,10 @@ are synthetic (iss_gb300.surfaces, seed 2).  Intermediate buffers (yields
 256 MB, CDF 510 MB, hadrons ~0.8 GB) exceed L2 and a 256 MB buffer is
 written between steps.
 
+The launch shape comes from the library's autotuner (untimed, before the
+warm-up) and each generate of the device leg replays one captured CUDA graph
+(gpu_graph = 1); --no-autotune / --no-graph turn these off.
+
 `value` is device time (CUDA events on the library's stream); `e2e` is the
 same metric through the C ABI with the surface copied from pinned host
 memory and all hadrons read back to pinned host memory every step
@@ -380,6 +384,8 @@ def run_gpu(args, ws, rank, local):
     params["gpu_event_offset"] = rank * n_events
     if args.decays:
         params["perform_decays"] = 1
+    if args.graph:
+        params["gpu_graph"] = 1
     s = iSS(".", inputfile="")
     s.set_params(**params)
     if batch is not None:
@@ -405,6 +411,15 @@ def run_gpu(args, ws, rank, local):
         s.set_params(gpu_sampler=1, gpu_learned_alpha=0.8)
         s.set_random_seed(20261203)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    tuning = None
+    if args.autotune:
+        # the library's autotuner on this workload (untimed; results do not
+        # depend on the launch shape)
+        shape, ms_before, ms_after = s.autotune()
+        tuning = {"shape": shape, "ms_default": ms_before, "ms_tuned": ms_after}
+        s.set_random_seed(20261203)
+    else:
+        tuning = {"shape": s.get_tuning(), "autotuned": False}
 
     def barrier():
         if ws > 1:
@@ -560,6 +575,7 @@ def run_gpu(args, ws, rank, local):
                            "delta_f": {k: v for k, v in wl["params"].items()
                                        if k.startswith("include_") or k == "bulk_deltaf_kind"},
                            "sampler": args.sampler, "decays": bool(args.decays),
+                           "graph_replay": bool(args.graph), "launch_shape": tuning,
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
                            "wall_s_timed": wall},
@@ -616,6 +632,12 @@ def main():
                     help="perform_decays = 1 (resonance decays after sampling, timed apart)")
     ap.add_argument("--oscar", action="store_true",
                     help="time the OSCAR writer on the last step's hadrons")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="eager launches (default: gpu_graph = 1, each generate of the device "
+                         "leg replays one captured CUDA graph)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="default launch shape (default: the library's autotuner picks it on "
+                         "the workload before the warm-up)")
     ap.add_argument("--sampler", choices=["plain", "learned"], default="plain",
                     help="learned: train the proposal network first, then sample with it")
     ap.add_argument("--train-momenta", type=int, default=50_000_000)

@@ -246,6 +246,33 @@ const char* iss_gpu_last_error(const iss_handle* h);
 /* Static name of a status code. */
 const char* iss_gpu_status_string(int status);
 
+/* ---- launch shape and autotuning -----------------------------------------
+ *
+ * No counterpart in the reference (its loops are serial).  The launch shape
+ * of the kernels never changes a result: every random number is keyed by
+ * (draw, hadron, event, species), so any shape gives the same hadrons bit
+ * for bit.  It changes only the time. */
+typedef struct iss_tuning {
+    int32_t item_size;      /* draws per sampler work item: 32, 64, ..., 1024 (default 64) */
+    int32_t yield_groups;   /* species groups per cell in the yields kernel: 1..32 (4)     */
+    int32_t sampler_ctas;   /* sampler blocks of 256 threads per SM: 1..3 (3)               */
+    int32_t assign_blocks;  /* cell-assignment blocks per SM: 1..32 (8)                     */
+    int32_t copy_chunks;    /* event chunks copied out by iss_gpu_generate_into: 1..64 (16) */
+} iss_tuning_t;
+iss_status iss_gpu_get_tuning(iss_handle* h, iss_tuning_t* out);
+iss_status iss_gpu_set_tuning(iss_handle* h, const iss_tuning_t* tuning);
+/* Times the handle's own workload (its surface and parameters) under
+ * candidate launch shapes and keeps the fastest: species groups per cell by
+ * the yields phase, then draws per work item, sampler blocks per SM and
+ * cell-assignment blocks per SM by the sample phase (coordinate descent, two
+ * generates per candidate, a 2 % margin to switch).  The result is cached per
+ * workload shape (cells, surfaces, events, species, local charge
+ * conservation, sampler, hydro mode) for every handle of the process; with
+ * gpu_autotune = 1 the first generate of a new shape tunes or takes the
+ * cached shape.  Leaves the samples of its last trial; ms_before / ms_after
+ * (optional) are the device times of one generate. */
+iss_status iss_gpu_autotune(iss_handle* h, iss_tuning_t* best, double* ms_before, double* ms_after);
+
 /* ---- the learned proposal ------------------------------------------------
  *
  * No counterpart in the reference: the reference has one momentum sampler

@@ -12,6 +12,9 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <memory>
 #include <random>
 #include <string>
@@ -41,6 +44,15 @@ struct TableKey {
                bulk_kind == o.bulk_kind && include_bulk == o.include_bulk &&
                include_diff == o.include_diff && neos == o.neos && fix_c0 == o.fix_c0;
     }
+};
+
+// Pinned host results of a graph replay: written by the graph's copies.
+struct GraphHost {
+    int64_t units, items, limits[2];
+    int32_t count_err, pad;
+    SampleCounters ctr;
+    uint32_t run[4];            // seed and event offset uploaded before a replay
+    int64_t event_offsets[1];   // n_events + 1 entries (allocated with the struct)
 };
 
 enum Phase { kEvStart = 0, kEvPrologue, kEvYields, kEvCdf, kEvCounts, kEvSampleStart, kEvSample,
@@ -124,6 +136,20 @@ struct iss_handle {
     bool host_valid = false;
     std::vector<double> totals;
     iss_timings_t timings{};
+    // graph replay of a generate (gpu_graph = 1): the executable graph, the
+    // call shape it was captured for, its buffer capacities, and pinned host
+    // memory its copies write to
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_unavailable = false;
+    std::vector<unsigned char> graph_key;
+    int64_t graph_cap_units = 0, graph_cap_items = 0;
+    DevBuf<uint32_t> d_run;
+    DevBuf<int64_t> d_limits;
+    GraphHost* gh = nullptr;
+    size_t gh_events = 0;
+    // launch shape of the kernels (iss_gpu_set_tuning / iss_gpu_autotune)
+    iss_tuning_t tune{64, 4, 3, 8, 16};
+    bool tuned = false;
     // the learned proposal: network, training set, per-pair mixture tables
     Learned learned;
     bool use_learned = false;            // gpu_sampler = 1
@@ -169,6 +195,10 @@ struct iss_handle {
             d_dchannels.release();
             d_dsorted.release();
             learned.release_all();
+            if (graph_exec) cudaGraphExecDestroy(graph_exec);
+            if (gh) cudaFreeHost(gh);
+            d_run.release();
+            d_limits.release();
             d_lslot.release();
             d_lspecies.release();
             d_spid.release();
@@ -301,6 +331,10 @@ iss_status prepare(iss_handle* h) {
         c.lslot = nullptr;
         c.lpairs = nullptr;
     }
+    c.item_size = h->tune.item_size;
+    c.yield_groups = h->tune.yield_groups;
+    c.sampler_ctas = h->tune.sampler_ctas;
+    c.assign_bps = h->tune.assign_blocks;
     c.key0 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed));
     c.key1 = static_cast<uint32_t>(static_cast<uint64_t>(h->seed) >> 32);
     c.n_species = static_cast<int>(h->species.size());
@@ -685,7 +719,6 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
 // host_out != nullptr: iss_gpu_generate_into -- the sampler runs in chunks of
 // consecutive events and each chunk's records are copied to host_out on a
 // second stream while the next chunk is sampled.
-constexpr int kMaxChunks = 16;
 
 // Learned proposal of one generate: the species whose expected hadrons per
 // cell (over all events) reach gpu_learned_min_hadrons_per_cell, the network
@@ -744,6 +777,238 @@ iss_status run_learned_pairs(iss_handle* h) {
     return ISS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Graph replay of a generate (gpu_graph = 1).  The first eligible call runs
+// eagerly, then captures the whole device sequence of a generate -- cell
+// prologue, yields, CDF, counts, slot scans, the bound check, item map, cell
+// assignment, sampler and the copies of the sizes, counters and event
+// offsets into pinned host memory -- as one CUDA graph.  Later calls of the
+// same shape upload their seed and event offset (12 bytes, read by the
+// kernels through DevConfig::run), launch the graph and wait once.  The
+// graph's buffers have 15 % headroom over the captured call; a call whose
+// draws do not fit samples nothing (graph_limits_kernel) and runs eagerly.
+
+bool graph_eligible(iss_handle* h, const iss_hadron_t* host_out) {
+    return h->params.get_or("gpu_graph", 0) == 1 && !h->graph_unavailable && host_out == nullptr &&
+           !h->decays &&
+           !h->use_learned && h->params.get_or("sample_upto_desired_particle_number", 0) != 1;
+}
+
+void drop_graph(iss_handle* h) {
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+    h->graph_key.clear();
+}
+
+// everything a captured generate depends on besides the seed and event offset
+std::vector<unsigned char> graph_key_of(iss_handle* h) {
+    DevConfig c = h->cfg;
+    c.key0 = c.key1 = 0;
+    c.event_offset = 0;
+    c.run = h->d_run.ptr;
+    c.ev_surf = h->d_ev_surf.ptr;
+    c.chunk_events = std::max(c.n_events, 1);
+    std::vector<unsigned char> k(sizeof(c));
+    std::memcpy(k.data(), &c, sizeof(c));
+    const void* ptrs[] = {h->d_fo34.ptr,     h->d_cells.ptr,    h->d_yields.ptr,   h->d_cdf.ptr,
+                          h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr,     h->d_totals.ptr,
+                          h->d_ymax.ptr,     h->d_guide.ptr,    h->d_counts.ptr,   h->d_items.ptr,
+                          h->d_offsets.ptr,  h->d_off_tiles.ptr, h->d_item_off.ptr, h->d_item_seg.ptr,
+                          h->d_hadrons.ptr,  h->d_cell_of.ptr,  h->d_work.ptr,     h->d_counters.ptr,
+                          h->d_error.ptr,    h->d_pois.ptr,     h->d_species.ptr,  h->d_pids.ptr,
+                          h->d_surf.ptr,     h->d_limits.ptr,   h->gh};
+    const unsigned char* pb = reinterpret_cast<const unsigned char*>(ptrs);
+    k.insert(k.end(), pb, pb + sizeof(ptrs));
+    const int64_t nums[] = {h->n_cells, h->n_tiles, h->cdf_len, h->guide_len, h->graph_cap_units,
+                            h->graph_cap_items, h->num_sms, static_cast<int64_t>(h->gh_events)};
+    const unsigned char* nb = reinterpret_cast<const unsigned char*>(nums);
+    k.insert(k.end(), nb, nb + sizeof(nums));
+    const unsigned char* tb = reinterpret_cast<const unsigned char*>(&h->tune);
+    k.insert(k.end(), tb, tb + sizeof(h->tune));
+    return k;
+}
+
+void record(iss_handle* h, int ev, bool capturing) {
+    if (capturing)
+        cudaEventRecordWithFlags(h->ev[ev], h->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(h->ev[ev], h->stream);
+}
+
+// the device sequence of one generate, with device-side sizes (no host sync)
+cudaError_t enqueue_generate(iss_handle* h, const DevConfig& c) {
+    cudaStream_t s = h->stream;
+    const int64_t n = h->n_cells;
+    const int S = c.n_species;
+    const int64_t nseg = static_cast<int64_t>(c.n_events) * S;
+    const CellArrays cells = cell_arrays(h);
+    cudaError_t e;
+#define GTRY(call)                      \
+    if ((e = (call)) != cudaSuccess) {  \
+        return e;                       \
+    }
+    record(h, kEvStart, true);
+    GTRY(launch_cell_prologue(c, h->d_fo34.ptr, n, cells, s));
+    record(h, kEvPrologue, true);
+    GTRY(launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, s));
+    record(h, kEvYields, true);
+    GTRY(launch_cdf(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S, h->d_ymax.ptr,
+                    h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
+                    h->d_guide.ptr, s));
+    record(h, kEvCdf, true);
+    GTRY(cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
+    GTRY(launch_counts(c, h->d_species.ptr, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr,
+                       h->d_items.ptr, h->d_error.ptr, s));
+    GTRY(launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
+    GTRY(launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
+    GTRY(launch_graph_limits(h->d_offsets.ptr, h->d_item_off.ptr, nseg, h->graph_cap_units,
+                             h->graph_cap_items, h->d_limits.ptr, s));
+    GTRY(launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s, h->d_limits.ptr));
+    record(h, kEvCounts, true);
+    GTRY(cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long), s));
+    GTRY(cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
+    record(h, kEvSampleStart, true);
+    GTRY(launch_sampler(c, cells, h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr, h->d_guide.ptr,
+                        h->d_qtot.ptr, h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr, 0,
+                        h->graph_cap_items, h->d_cell_of.ptr, h->d_hadrons.ptr, h->d_work.ptr,
+                        h->d_counters.ptr, h->num_sms, s, h->d_limits.ptr));
+    record(h, kEvSample, true);
+    GraphHost* g = h->gh;
+    GTRY(cudaMemcpyAsync(&g->units, h->d_offsets.ptr + nseg, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GTRY(cudaMemcpyAsync(&g->items, h->d_item_off.ptr + nseg, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GTRY(cudaMemcpyAsync(g->limits, h->d_limits.ptr, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GTRY(cudaMemcpyAsync(&g->count_err, h->d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GTRY(cudaMemcpyAsync(&g->ctr, h->d_counters.ptr, sizeof(SampleCounters), cudaMemcpyDeviceToHost, s));
+    if (S > 0)
+        GTRY(cudaMemcpy2DAsync(g->event_offsets, sizeof(int64_t), h->d_offsets.ptr,
+                               sizeof(int64_t) * static_cast<size_t>(S), sizeof(int64_t),
+                               static_cast<size_t>(c.n_events) + 1, cudaMemcpyDeviceToHost, s));
+#undef GTRY
+    return cudaSuccess;
+}
+
+// after an eager generate that fitted: capture the call's graph
+iss_status capture_graph(iss_handle* h, int64_t n_items) {
+    drop_graph(h);
+    DevConfig c = h->cfg;
+    const int E = c.n_events;
+    CUDA_TRY(h, h->d_run.reserve(4));
+    CUDA_TRY(h, h->d_limits.reserve(2));
+    if (!h->gh || h->gh_events < static_cast<size_t>(E)) {
+        if (h->gh) cudaFreeHost(h->gh);
+        h->gh = nullptr;
+        CUDA_TRY(h, cudaMallocHost(reinterpret_cast<void**>(&h->gh),
+                                   sizeof(GraphHost) + sizeof(int64_t) * static_cast<size_t>(E + 1)));
+        h->gh_events = static_cast<size_t>(E);
+    }
+    h->graph_cap_units = static_cast<int64_t>(h->d_hadrons.cap);
+    h->graph_cap_items = static_cast<int64_t>(h->d_item_seg.cap);
+    if (h->graph_cap_items < n_items) return ISS_OK;
+    c.run = h->d_run.ptr;
+    c.chunk_events = std::max(E, 1);
+    cudaStream_t s = h->stream;
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t ce = enqueue_generate(h, c);
+    const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    // a graph that cannot be captured leaves the calls eager (the samples of
+    // this call are complete either way)
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        h->graph_unavailable = true;
+        h->last_error = std::string("generate runs eagerly: graph capture failed: ") +
+                        cudaGetErrorString(ce != cudaSuccess ? ce : ee);
+        return ISS_OK;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        h->graph_exec = nullptr;
+        cudaGetLastError();
+        h->graph_unavailable = true;
+        h->last_error = std::string("generate runs eagerly: graph instantiation failed: ") +
+                        cudaGetErrorString(ie);
+        return ISS_OK;
+    }
+    h->graph_key = graph_key_of(h);
+    return ISS_OK;
+}
+
+// a call of the captured shape: upload the seed, launch, read the results;
+// *done = false (graph dropped) when the call has to run eagerly
+iss_status replay_graph(iss_handle* h, bool* done) {
+    *done = false;
+    DevConfig& c = h->cfg;
+    cudaStream_t s = h->stream;
+    if (!h->surface_on_device) {
+        CUDA_TRY(h, h->d_fo34.reserve(static_cast<size_t>(h->n_cells) * kFoSurfFloats));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_fo34.ptr, h->fo34.data(),
+                                    sizeof(float) * static_cast<size_t>(h->n_cells) * kFoSurfFloats,
+                                    cudaMemcpyHostToDevice, s));
+        h->surface_on_device = true;
+    }
+    if (graph_key_of(h) != h->graph_key) {
+        drop_graph(h);
+        return ISS_OK;
+    }
+    // the surface of every event (a batch may spread the same total
+    // differently over its surfaces)
+    {
+        std::vector<int32_t>& ev_surf = h->ev_surf;
+        ev_surf.assign(static_cast<size_t>(std::max(c.n_events, 1)), 0);
+        for (int b = 0; b < c.n_surfaces; b++)
+            for (int e = 0; e < h->segs[b].ne; e++) ev_surf[h->segs[b].e0 + e] = b;
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_ev_surf.ptr, ev_surf.data(), 4 * ev_surf.size(),
+                                    cudaMemcpyHostToDevice, s));
+    }
+    GraphHost* g = h->gh;
+    g->run[0] = c.key0;
+    g->run[1] = c.key1;
+    g->run[2] = c.event_offset;
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_run.ptr, g->run, 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaGraphLaunch(h->graph_exec, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    h->yields_valid = true;
+    if (g->count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
+    if (g->count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
+    if (g->limits[1] != 0) {
+        // more draws than the captured buffers hold: nothing was sampled
+        drop_graph(h);
+        return ISS_OK;
+    }
+    const int E = c.n_events;
+    h->event_offsets.assign(g->event_offsets, g->event_offsets + E + 1);
+    h->n_events = E;
+    h->n_hadrons = g->units;
+    const SampleCounters ctr = g->ctr;
+    iss_timings_t& t = h->timings;
+    t.ms_decays = 0.0;
+    t.ms_prologue = elapsed(h, kEvStart, kEvPrologue);
+    t.ms_yields = elapsed(h, kEvPrologue, kEvYields);
+    t.ms_cdf = elapsed(h, kEvYields, kEvCdf);
+    t.ms_counts = elapsed(h, kEvCdf, kEvCounts);
+    t.ms_sample = elapsed(h, kEvSampleStart, kEvSample);
+    t.ms_total = elapsed(h, kEvStart, kEvSample);
+    t.n_hadrons = h->n_hadrons;
+    t.n_tries = static_cast<int64_t>(ctr.tries);
+    t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
+    t.n_failures = static_cast<int64_t>(ctr.failures);
+    t.kernel_launches = 18;   // one graph launch of the 18 kernels of a generate
+    h->samples_valid = true;
+    *done = true;
+    if (ctr.error_code == 1) {
+        const int k = ctr.error_species;
+        return fail(h, ISS_ERR_OUT_OF_RANGE,
+                    "momentum sampler out of range for species %d (m/T - mu/T off the tables)",
+                    (k >= 0 && k < c.n_species) ? h->species[k].pid : 0);
+    }
+    if (ctr.failures > 0)
+        return fail(h, ISS_ERR_SAMPLING, "%llu hadrons abandoned after %d cell redraws",
+                    static_cast<unsigned long long>(ctr.failures), c.max_redraws);
+    return ISS_OK;
+}
+
 iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
                         bool* copied = nullptr) {
     if (copied) *copied = false;
@@ -754,6 +1019,11 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     if (st != ISS_OK) return st;
     h->samples_valid = false;
     h->host_valid = false;
+    if (graph_eligible(h, host_out) && h->graph_exec) {
+        bool done = false;
+        st = replay_graph(h, &done);
+        if (st != ISS_OK || done) return st;
+    }
     st = run_cells(h);
     if (st != ISS_OK) return st;
     DevConfig& c = h->cfg;
@@ -800,7 +1070,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     CUDA_TRY(h, h->d_off_tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(nseg), 1))));
     // sampling chunks: one without a host destination, else up to kMaxChunks
     const int E = c.n_events;
-    int n_chunks = (host_out && !h->decays) ? std::min(kMaxChunks, std::max(E, 1)) : 1;
+    int n_chunks = (host_out && !h->decays) ? std::min(h->tune.copy_chunks, std::max(E, 1)) : 1;
     c.chunk_events = std::max(1, (E + n_chunks - 1) / n_chunks);
     n_chunks = std::max(1, (E + c.chunk_events - 1) / c.chunk_events);
     CUDA_TRY(h, h->d_error.reserve(1));
@@ -846,7 +1116,11 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     chunk_item[n_chunks] = n_items;
     if (count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
     if (count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
-    CUDA_TRY(h, h->d_item_seg.reserve(static_cast<size_t>(std::max<int64_t>(n_items, 1))));
+    const bool graph_mode = graph_eligible(h, host_out);
+    // a call that will be captured gets 15 % headroom in the buffers whose
+    // size depends on the draws, so that later calls fit the same graph
+    const auto headroom = [&](int64_t v) { return graph_mode ? v + v / 7 + 1024 : std::max<int64_t>(v, 1); };
+    CUDA_TRY(h, h->d_item_seg.reserve(static_cast<size_t>(headroom(n_items))));
     CUDA_TRY(h, launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvCounts], s));
     {
@@ -874,8 +1148,8 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
             h->chunk_ev.push_back(e);
         }
     }
-    CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
-    CUDA_TRY(h, h->d_cell_of.reserve(static_cast<size_t>(std::max<int64_t>(n_units, 1))));
+    CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(headroom(n_units))));
+    CUDA_TRY(h, h->d_cell_of.reserve(static_cast<size_t>(headroom(n_units))));
     CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long) * n_chunks, s));
     CUDA_TRY(h, cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
@@ -962,7 +1236,125 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     if (ctr.failures > 0)
         return fail(h, ISS_ERR_SAMPLING, "%llu hadrons abandoned after %d cell redraws",
                     static_cast<unsigned long long>(ctr.failures), c.max_redraws);
+    if (graph_mode) return capture_graph(h, n_items);
     return ISS_OK;
+}
+
+bool tuning_valid(const iss_tuning_t& t) {
+    return t.item_size >= 32 && t.item_size <= 1024 && t.item_size % 32 == 0 && t.yield_groups >= 1 &&
+           t.yield_groups <= 32 && t.sampler_ctas >= 1 && t.sampler_ctas <= 3 && t.assign_blocks >= 1 &&
+           t.assign_blocks <= 32 && t.copy_chunks >= 1 && t.copy_chunks <= 64;
+}
+
+// Tuning results per workload shape, shared by the handles of the process.
+using TuneKey = std::tuple<int64_t, int64_t, int, int, int, int, int>;
+std::mutex g_tune_mutex;
+std::map<TuneKey, iss_tuning_t> g_tune_cache;
+
+TuneKey tune_key(iss_handle* h) {
+    return TuneKey{h->n_cells, static_cast<int64_t>(h->batch_events.size()),
+                   static_cast<int>(h->params.get_or("number_of_repeated_sampling", 0)),
+                   static_cast<int>(h->species.size()),
+                   static_cast<int>(h->params.get_or("local_charge_conservation", 0)),
+                   static_cast<int>(h->params.get_or("gpu_sampler", 0)),
+                   static_cast<int>(h->params.get_or("hydro_mode", 2))};
+}
+
+// Coordinate descent over the launch shape on the handle's own workload:
+// species groups per cell (objective: the yields phase), then draws per work
+// item, sampler CTAs per SM and cell-assignment blocks per SM (objective: the
+// sample phase).  Each candidate runs two generates and keeps the faster
+// device time; a candidate replaces the incumbent only when it is 2 % faster.
+iss_status autotune(iss_handle* h, double* ms_before, double* ms_after) {
+    auto measure = [&](const iss_tuning_t& t, double* y, double* smp, double* tot) -> iss_status {
+        h->tune = t;
+        *y = *smp = *tot = 1e300;
+        for (int r = 0; r < 2; r++) {
+            const iss_status st = run_generate(h);
+            if (st != ISS_OK) return st;
+            *y = std::min(*y, h->timings.ms_yields);
+            *smp = std::min(*smp, h->timings.ms_sample);
+            *tot = std::min(*tot, h->timings.ms_total);
+        }
+        return ISS_OK;
+    };
+    iss_tuning_t best = h->tune;
+    double by, bs, bt;
+    iss_status st = measure(best, &by, &bs, &bt);
+    if (st != ISS_OK) return st;
+    if (ms_before) *ms_before = bt;
+    const int groups[] = {1, 2, 4, 8, 16};
+    for (int g : groups) {
+        if (g == best.yield_groups || g > static_cast<int>(h->species.size())) continue;
+        iss_tuning_t t = best;
+        t.yield_groups = g;
+        double y, smp, tot;
+        if ((st = measure(t, &y, &smp, &tot)) != ISS_OK) return st;
+        if (y < 0.98 * by) {
+            best = t;
+            by = y;
+        }
+    }
+    // the sample phase: re-measure the incumbent with the chosen groups
+    if ((st = measure(best, &by, &bs, &bt)) != ISS_OK) return st;
+    const int items[] = {32, 64, 128, 256};
+    for (int it : items) {
+        if (it == best.item_size) continue;
+        iss_tuning_t t = best;
+        t.item_size = it;
+        double y, smp, tot;
+        if ((st = measure(t, &y, &smp, &tot)) != ISS_OK) return st;
+        if (smp < 0.98 * bs) {
+            best = t;
+            bs = smp;
+        }
+    }
+    const int ctas[] = {2, 3};
+    for (int c : ctas) {
+        if (c == best.sampler_ctas) continue;
+        iss_tuning_t t = best;
+        t.sampler_ctas = c;
+        double y, smp, tot;
+        if ((st = measure(t, &y, &smp, &tot)) != ISS_OK) return st;
+        if (smp < 0.98 * bs) {
+            best = t;
+            bs = smp;
+        }
+    }
+    const int assign[] = {4, 8, 16};
+    for (int a : assign) {
+        if (a == best.assign_blocks) continue;
+        iss_tuning_t t = best;
+        t.assign_blocks = a;
+        double y, smp, tot;
+        if ((st = measure(t, &y, &smp, &tot)) != ISS_OK) return st;
+        if (smp < 0.98 * bs) {
+            best = t;
+            bs = smp;
+        }
+    }
+    if ((st = measure(best, &by, &bs, &bt)) != ISS_OK) return st;
+    if (ms_after) *ms_after = bt;
+    h->tuned = true;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[tune_key(h)] = best;
+    return ISS_OK;
+}
+
+// gpu_autotune = 1: the first generate of a workload shape takes the cached
+// launch shape or tunes one
+iss_status maybe_autotune(iss_handle* h) {
+    if (h->tuned || h->params.get_or("gpu_autotune", 0) != 1) return ISS_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        const auto it = g_tune_cache.find(tune_key(h));
+        if (it != g_tune_cache.end()) {
+            h->tune = it->second;
+            h->tuned = true;
+            return ISS_OK;
+        }
+    }
+    return autotune(h, nullptr, nullptr);
 }
 
 iss_status ensure_host_copy(iss_handle* h) {
@@ -1264,6 +1656,8 @@ iss_status iss_gpu_generate(iss_handle* h) {
         iss_status st = iss_gpu_set_seed_from_params(h);
         if (st != ISS_OK) return st;
     }
+    const iss_status st = maybe_autotune(h);
+    if (st != ISS_OK) return st;
     return run_generate(h);
 }
 
@@ -1276,6 +1670,8 @@ iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capac
         iss_status st = iss_gpu_set_seed_from_params(h);
         if (st != ISS_OK) return st;
     }
+    const iss_status tst = maybe_autotune(h);
+    if (tst != ISS_OK) return tst;
     bool copied = false;
     const iss_status st = run_generate(h, out, capacity, &copied);
     if (n_total && h->samples_valid) *n_total = h->n_hadrons;
@@ -1728,6 +2124,38 @@ iss_status iss_gpu_learned_copy_rows(iss_handle* h, int64_t first, int64_t count
     if (targets)
         CUDA_TRY(h, cudaMemcpy(targets, L.data_t.ptr + first, sizeof(float4) * count,
                                cudaMemcpyDeviceToHost));
+    return ISS_OK;
+}
+
+// ---- launch shape -------------------------------------------------------------
+
+iss_status iss_gpu_get_tuning(iss_handle* h, iss_tuning_t* out) {
+    if (!h || !out) return ISS_ERR_INVALID_ARG;
+    *out = h->tune;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_set_tuning(iss_handle* h, const iss_tuning_t* t) {
+    if (!h || !t) return ISS_ERR_INVALID_ARG;
+    if (!tuning_valid(*t))
+        return fail(h, ISS_ERR_INVALID_ARG,
+                    "launch shape out of range (item_size %d, yield_groups %d, sampler_ctas %d, "
+                    "assign_blocks %d, copy_chunks %d)",
+                    t->item_size, t->yield_groups, t->sampler_ctas, t->assign_blocks, t->copy_chunks);
+    h->tune = *t;
+    h->tuned = true;
+    return ISS_OK;
+}
+
+iss_status iss_gpu_autotune(iss_handle* h, iss_tuning_t* best, double* ms_before, double* ms_after) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!h->seed_set) {
+        iss_status st = iss_gpu_set_seed_from_params(h);
+        if (st != ISS_OK) return st;
+    }
+    const iss_status st = autotune(h, ms_before, ms_after);
+    if (st != ISS_OK) return st;
+    if (best) *best = h->tune;
     return ISS_OK;
 }
 

@@ -67,6 +67,14 @@ struct DevConfig {
     const int32_t* lslot;
     const float* lpairs;
     float lalpha;
+    // launch shape (results do not depend on it; the autotuner picks it)
+    int item_size;       // draws per sampler work item (multiple of 32, <= 1024)
+    int yield_groups;    // species groups per cell in the yields kernel (grid y)
+    int sampler_ctas;    // sampler CTAs per SM (1..3)
+    int assign_bps;      // cell-assignment blocks per SM
+    // graph replays: (key0, key1, event_offset) of the call in device memory,
+    // so one captured graph serves every seed; null: the fields above
+    const uint32_t* run;
 };
 
 // floats per (species slot, cell) record of the learned proposal: for each of
@@ -243,6 +251,17 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 }
 
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// the configuration with the call's seed and event offset (DevConfig::run)
+__device__ __forceinline__ DevConfig with_run_keys(const DevConfig& c) {
+    DevConfig r = c;
+    if (c.run) {
+        r.key0 = c.run[0];
+        r.key1 = c.run[1];
+        r.event_offset = c.run[2];
+    }
+    return r;
+}
 #endif  // __CUDACC__
 
 }  // namespace iss

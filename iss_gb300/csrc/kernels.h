@@ -36,7 +36,13 @@ int offsets_num_tiles(int64_t n);
 cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_sum,
                                 int64_t* offsets, cudaStream_t stream);
 cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64_t nseg,
-                            int32_t* item_seg, cudaStream_t stream);
+                            int32_t* item_seg, cudaStream_t stream,
+                            const int64_t* limits = nullptr);
+// graph replays: limits[0] = the call's work items, limits[1] = 1 when the
+// call does not fit the captured buffers (cap_units records, cap_items items)
+cudaError_t launch_graph_limits(const int64_t* offsets, const int64_t* item_off, int64_t nseg,
+                                int64_t cap_units, int64_t cap_items, int64_t* limits,
+                                cudaStream_t stream);
 // work items [k_begin, k_end) in two launches: the first-draw cell of every
 // hadron (cell_of, one int32 per slot), then the sampler; work_counter must
 // be zero
@@ -47,7 +53,7 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                            const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
                            int64_t k_end, int32_t* cell_of, HadronRec* out,
                            unsigned long long* work_counter, SampleCounters* counters, int num_sms,
-                           cudaStream_t stream);
+                           cudaStream_t stream, const int64_t* k_end_dev = nullptr);
 
 // learned proposal (kernels_sample.cu): network inputs of the pairs
 // (slot, cell), slot < n_slots, as bf16 rows [n_slots * n_cells][32]; the

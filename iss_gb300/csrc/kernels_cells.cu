@@ -6,6 +6,8 @@
 //                         per-species fixed-point prefix sums of the cell yields
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -526,7 +528,8 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    const unsigned groups = static_cast<unsigned>(cfg.n_species < kYieldGroups ? 1 : kYieldGroups);
+    const int want = cfg.yield_groups > 0 ? cfg.yield_groups : kYieldGroups;
+    const unsigned groups = static_cast<unsigned>(std::max(1, std::min(want, cfg.n_species)));
     yields_kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
     return cudaGetLastError();
 }

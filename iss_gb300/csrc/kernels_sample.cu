@@ -30,6 +30,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 #include "learned_record.cuh"
@@ -184,7 +186,9 @@ __device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
     return -1.0;
 }
 
-constexpr int kItem = 64;   // hadrons per work item (one (event, species) segment)
+// a work item is cfg.item_size consecutive draws of one (event, species)
+// segment; the cell assignment takes them 64 at a time (two per lane)
+constexpr int kAssignSub = 64;
 
 // Work items are ordered by event chunk (cfg.chunk_events consecutive events),
 // then species, then event: warps that run at the same time mostly sample one
@@ -229,11 +233,12 @@ __global__ void count_consts_kernel(DevConfig cfg, const double* __restrict__ to
     poisson_inv_table(c, inv[s]);
 }
 
-__global__ void counts_kernel(DevConfig cfg, const SpeciesDev* __restrict__ species,
+__global__ void counts_kernel(DevConfig cfg_in, const SpeciesDev* __restrict__ species,
                               const double* __restrict__ totals,
                               const PoissonC* __restrict__ pois,
                               const PoissonInv* __restrict__ inv, int32_t* __restrict__ counts,
                               int32_t* __restrict__ items, int* __restrict__ error) {
+    const DevConfig cfg = with_run_keys(cfg_in);
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (idx >= total) return;
@@ -275,18 +280,33 @@ __global__ void counts_kernel(DevConfig cfg, const SpeciesDev* __restrict__ spec
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
     counts[idx] = c * records_per_draw(cfg, sp);       // records of the segment
-    items[item_index(cfg, e, s)] = (c + kItem - 1) / kItem;
+    items[item_index(cfg, e, s)] = (c + cfg.item_size - 1) / cfg.item_size;
 }
 
 // item -> segment map: item_seg[item_off[q] + k] = q for k < items[q], q the
 // work-item order index of the segment (item_index)
 __global__ void item_map_kernel(const int32_t* __restrict__ items, const int64_t* __restrict__ item_off,
-                                int64_t nseg, int32_t* __restrict__ item_seg) {
+                                int64_t nseg, int32_t* __restrict__ item_seg,
+                                const int64_t* __restrict__ limits) {
     const int64_t seg = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (seg >= nseg) return;
+    // graph replays: nothing is written when the buffers are too small
+    if (limits && limits[1] != 0) return;
     const int64_t b = item_off[seg];
     const int32_t k = items[seg];
     for (int32_t j = 0; j < k; j++) item_seg[b + j] = static_cast<int32_t>(seg);
+}
+
+// graph replays: the work-item count of this call (limits[0]) and whether the
+// call fits the buffers the graph was captured with (limits[1] = 1: it does
+// not; then nothing is sampled and the host reruns the call eagerly)
+__global__ void graph_limits_kernel(const int64_t* __restrict__ offsets,
+                                    const int64_t* __restrict__ item_off, int64_t nseg,
+                                    int64_t cap_units, int64_t cap_items, int64_t* __restrict__ limits) {
+    const int64_t units = offsets[nseg], n_items = item_off[nseg];
+    const bool fits = units <= cap_units && n_items <= cap_items;
+    limits[0] = fits ? n_items : 0;
+    limits[1] = fits ? 0 : 1;
 }
 
 // ------------------------------------------------------------------------
@@ -894,12 +914,14 @@ __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& 
 constexpr int kAssignThreads = 256;
 
 __global__ void __launch_bounds__(kAssignThreads)
-cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
+cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
                    const int32_t* __restrict__ guide,
                    const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                    const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
                    int64_t k_begin, int64_t k_end, const SpeciesDev* __restrict__ species,
-                   int32_t* __restrict__ cell_of) {
+                   int32_t* __restrict__ cell_of, const int64_t* __restrict__ k_end_dev) {
+    const DevConfig cfg = with_run_keys(cfg_in);
+    if (k_end_dev) k_end = *k_end_dev;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -912,8 +934,8 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         const int64_t base = offsets[seg];
         const int mult = records_per_draw(cfg, species[s]);
         const int64_t draws = (offsets[seg + 1] - base) / mult;
-        const int64_t d_begin = j * kItem;
-        const int64_t d_end = min(d_begin + kItem, draws);
+        const int64_t d_begin = j * cfg.item_size;
+        const int64_t d_end = min(d_begin + cfg.item_size, draws);
         const int b = cfg.ev_surf[e];
         const SurfSeg sg = cfg.surf[b];
         const unsigned long long* row = cdf + sg.cdf_base + static_cast<int64_t>(s) * (sg.n + 1);
@@ -921,10 +943,10 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         const unsigned long long Q = qtot[b * cfg.n_species + s];
         const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
         const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
-        // an item has at most 64 draws: each lane takes two and issues both
-        // guide lookups before either search, so their latencies overlap
-        static_assert(kItem == 64, "two draws per lane");
-        const int64_t d0 = d_begin + lane, d1 = d0 + 32;
+        // 64 draws at a time: each lane takes two and issues both guide
+        // lookups before either search, so their latencies overlap
+        for (int64_t d_sub = d_begin; d_sub < d_end; d_sub += kAssignSub) {
+        const int64_t d0 = d_sub + lane, d1 = d0 + 32;
         const bool v0 = d0 < d_end, v1 = d1 < d_end;
         unsigned long long r0 = 0, r1 = 0;
         if (v0) {
@@ -965,6 +987,7 @@ cell_assign_kernel(DevConfig cfg, const unsigned long long* __restrict__ cdf,
         }
         if (v0) cell_of[base + d0 * mult] = static_cast<int32_t>(sg.c0) + lo0;
         if (v1) cell_of[base + d1 * mult] = static_cast<int32_t>(sg.c0) + lo1;
+        }
     }
 }
 
@@ -974,14 +997,17 @@ constexpr int kSampleThreads = 256;
 // common case carries none of the pair state)
 template <bool kLcc, bool kLearned>
 __global__ void __launch_bounds__(kSampleThreads, 3)
-sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
+sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
                const int32_t* __restrict__ guide,
                const unsigned long long* __restrict__ qtot, const int64_t* __restrict__ offsets,
                const int64_t* __restrict__ item_off, const int32_t* __restrict__ item_seg,
                int64_t k_begin, int64_t k_end, int32_t* __restrict__ cell_of,
                HadronRec* __restrict__ out,
-               unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs) {
+               unsigned long long* __restrict__ work_counter, SampleCounters* __restrict__ ctrs,
+               const int64_t* __restrict__ k_end_dev) {
+    const DevConfig cfg = with_run_keys(cfg_in);
+    if (k_end_dev) k_end = *k_end_dev;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // the warp's current work item: units [next, end) of species cur_s in event cur_e
@@ -1015,8 +1041,8 @@ sampler_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ s
                 const int64_t seg = static_cast<int64_t>(cur_e) * cfg.n_species + cur_s;
                 seg_base = offsets[seg];
                 cur_mult = kLcc ? records_per_draw(cfg, species[cur_s]) : 1;
-                next = j * kItem;
-                end = min(next + kItem, (offsets[seg + 1] - seg_base) / cur_mult);
+                next = j * cfg.item_size;
+                end = min(next + cfg.item_size, (offsets[seg + 1] - seg_base) / cur_mult);
             }
             const int64_t avail = end - next;
             const int rank = __popc(need & ((1u << lane) - 1u));
@@ -1383,10 +1409,17 @@ cudaError_t launch_offsets_scan(const int32_t* counts, int64_t n, int64_t* tile_
 }
 
 cudaError_t launch_item_map(const int32_t* items, const int64_t* item_off, int64_t nseg,
-                            int32_t* item_seg, cudaStream_t stream) {
+                            int32_t* item_seg, cudaStream_t stream, const int64_t* limits) {
     if (nseg <= 0) return cudaSuccess;
-    item_map_kernel<<<static_cast<unsigned>((nseg + 255) / 256), 256, 0, stream>>>(items, item_off,
-                                                                                 nseg, item_seg);
+    item_map_kernel<<<static_cast<unsigned>((nseg + 255) / 256), 256, 0, stream>>>(
+        items, item_off, nseg, item_seg, limits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_graph_limits(const int64_t* offsets, const int64_t* item_off, int64_t nseg,
+                                int64_t cap_units, int64_t cap_items, int64_t* limits,
+                                cudaStream_t stream) {
+    graph_limits_kernel<<<1, 1, 0, stream>>>(offsets, item_off, nseg, cap_units, cap_items, limits);
     return cudaGetLastError();
 }
 
@@ -1397,17 +1430,20 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                            const int64_t* item_off, const int32_t* item_seg, int64_t k_begin,
                            int64_t k_end, int32_t* cell_of, HadronRec* out,
                            unsigned long long* work_counter, SampleCounters* counters, int num_sms,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, const int64_t* k_end_dev) {
+    // with k_end_dev (graph replays) the item count is read on the device and
+    // k_end is only the capacity that sizes the grids
     const int64_t n_items = k_end - k_begin;
     if (n_items <= 0) return cudaSuccess;
     {
-        int64_t blocks = static_cast<int64_t>(num_sms) * 8;
+        int64_t blocks = static_cast<int64_t>(num_sms) * std::max(1, cfg.assign_bps);
         const int64_t need = (n_items + (kAssignThreads / 32) - 1) / (kAssignThreads / 32);
         if (blocks > need) blocks = need;
         cell_assign_kernel<<<static_cast<unsigned>(blocks), kAssignThreads, 0, stream>>>(
-            cfg, cdf, guide, qtot, offsets, item_off, item_seg, k_begin, k_end, sp, cell_of);
+            cfg, cdf, guide, qtot, offsets, item_off, item_seg, k_begin, k_end, sp, cell_of,
+            k_end_dev);
     }
-    const int per_sm = 3;
+    const int per_sm = std::min(3, std::max(1, cfg.sampler_ctas));
     int64_t blocks = static_cast<int64_t>(num_sms) * per_sm;
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
@@ -1416,7 +1452,7 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
                              : (cfg.lcc ? sampler_kernel<true, false> : sampler_kernel<false, false>);
     kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
-        k_end, cell_of, out, work_counter, counters);
+        k_end, cell_of, out, work_counter, counters, k_end_dev);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@ EXPORTED = [
     "iss_gpu_learned_num_weights", "iss_gpu_learned_init_weights", "iss_gpu_learned_set_weights",
     "iss_gpu_learned_get_weights", "iss_gpu_learned_forward", "iss_gpu_learned_loss_grad",
     "iss_gpu_mma_selftest", "iss_gpu_learned_train", "iss_gpu_learned_stats",
-    "iss_gpu_learned_copy_rows",
+    "iss_gpu_learned_copy_rows", "iss_gpu_get_tuning", "iss_gpu_set_tuning", "iss_gpu_autotune",
 ]
 
 
@@ -67,6 +67,14 @@ class LearnedStats(C.Structure):
                 ("n_train_rows", C.c_int64), ("ms_train", C.c_double),
                 ("train_events_per_seed", C.c_int32), ("train_nll_plain", C.c_double),
                 ("ms_forward", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("item_size", C.c_int32), ("yield_groups", C.c_int32), ("sampler_ctas", C.c_int32),
+                ("assign_blocks", C.c_int32), ("copy_chunks", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -133,6 +141,10 @@ def lib():
         L.iss_gpu_learned_train.argtypes = [h, C.POINTER(LearnedTrain), v, C.c_int32]
         L.iss_gpu_learned_stats.argtypes = [h, C.POINTER(LearnedStats)]
         L.iss_gpu_learned_copy_rows.argtypes = [h, C.c_int64, C.c_int64, v, v]
+        L.iss_gpu_get_tuning.argtypes = [h, C.POINTER(Tuning)]
+        L.iss_gpu_set_tuning.argtypes = [h, C.POINTER(Tuning)]
+        L.iss_gpu_autotune.argtypes = [h, C.POINTER(Tuning), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]
         for name in EXPORTED:
             if name not in ("iss_gpu_last_error", "iss_gpu_status_string"):
                 getattr(L, name).restype = C.c_int
@@ -336,6 +348,24 @@ class iSS:
         t = Timings()
         self._check(self._L.iss_gpu_get_timings(self._h, C.byref(t)))
         return t.as_dict()
+
+    # launch shape
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self._L.iss_gpu_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = Tuning(**dict(self.get_tuning(), **kw))
+        self._check(self._L.iss_gpu_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self):
+        """Tunes the launch shape on this handle's workload; returns (shape,
+        ms before, ms after)."""
+        t = Tuning()
+        b, a = C.c_double(), C.c_double()
+        self._check(self._L.iss_gpu_autotune(self._h, C.byref(t), C.byref(b), C.byref(a)))
+        return t.as_dict(), b.value, a.value
 
     # the learned proposal network
     def learned_init_weights(self, seed=0):
