@@ -294,6 +294,38 @@ def _chi2_two_sample(a, b):
     return float(stats.chi2.sf(chi2, m.sum() - 1))
 
 
+def surface_spread(s, batch, b_cells, b_events, params, iSS):
+    """Per-surface spread of a batch: hadrons per surface of the last step
+    (from the event offsets) and the throughput of five surfaces (cell-count
+    quantiles 0, 0.25, 0.5, 0.75, 1) sampled alone with their own events."""
+    off = s.event_offsets()
+    e0 = np.concatenate([[0], np.cumsum(b_events)])
+    had = off[e0[1:]] - off[e0[:-1]]
+    per_ev = had / np.maximum(b_events, 1)
+    out = {"surfaces": len(batch), "hadrons_min": int(had.min()), "hadrons_median": float(np.median(had)),
+           "hadrons_max": int(had.max()), "hadrons_per_event_per_kcell_median":
+               float(np.median(per_ev / (b_cells / 1000.0)))}
+    order = np.argsort(b_cells)
+    alone = []
+    for q in (0.0, 0.25, 0.5, 0.75, 1.0):
+        b = int(order[int(round(q * (len(order) - 1)))])
+        one = iSS(".", inputfile="")
+        one.set_params(**dict(params, number_of_repeated_sampling=int(b_events[b])))
+        one.set_surface(batch[b])
+        one.set_random_seed(20261203)
+        ms = []
+        for _ in range(3):
+            one.generate_samples()
+            ms.append(one.timings()["ms_total"])
+        t = one.timings()
+        alone.append({"cells": int(b_cells[b]), "events": int(b_events[b]),
+                      "hadrons": int(t["n_hadrons"]), "ms": min(ms),
+                      "hadrons_per_s": t["n_hadrons"] / (min(ms) * 1e-3)})
+        one.close()
+    out["alone"] = alone
+    return out
+
+
 def learned_report(s, timings, args):
     """Acceptance of the learned proposal against the plain sampler's on the
     same species (alpha -> 0 with the envelope at 1), the plain sampler's step
@@ -519,6 +551,9 @@ def run_gpu(args, ws, rank, local):
 
     if learned is not None:
         learned.update(learned_report(s, timings, args))
+    per_surface = None
+    if batch is not None and rank == 0:
+        per_surface = surface_spread(s, batch, b_cells, b_events, params, iSS)
     sec = sum(dev_ms) / 1e3
     local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
     if e2e:
@@ -590,6 +625,8 @@ def run_gpu(args, ws, rank, local):
                 "hadrons_per_step": nh / args.steps,
                 "phase_ms_per_step": phases,
                 "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
+        if per_surface is not None:
+            line["per_surface"] = per_surface
         if learned is not None:
             peak_tf = 1922.0
             try:

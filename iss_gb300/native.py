@@ -284,6 +284,14 @@ class iSS:
             self._check(self._L.iss_gpu_copy_event(self._h, iev, _ptr(out), n.value, C.byref(n)))
         return out
 
+    def event_offsets(self):
+        """First hadron of every event (n_events + 1 entries), without copying hadrons."""
+        nev = self.get_number_of_sampled_events()
+        off = np.zeros(nev + 1, dtype=np.int64)
+        n = C.c_int64()
+        self._check(self._L.iss_gpu_copy_all(self._h, None, 0, _ptr(off), C.byref(n)))
+        return off
+
     def all_hadrons(self, out=None):
         """(hadrons, event_offsets): every event in one device->host copy."""
         n = C.c_int64()
