@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <sstream>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -105,6 +106,7 @@ struct iss_handle {
     cudaEvent_t ev[kEvCount] = {};
     DevBuf<float> d_fo34;
     DevBuf<float4> d_cells;          // 8 arrays of n_cells float4
+    DevBuf<float4> d_milne;          // MC_sampling = 2: regulated Milne cells, 6 float4 each
     DevBuf<SpeciesDev> d_species;
     DevBuf<int32_t> d_pids;
     DevBuf<float> d_yields;
@@ -162,6 +164,7 @@ struct iss_handle {
             DevBuf<float>* fb[] = {&d_fo34, &d_yields, &d_sfE};
             for (auto* b : fb) b->release();
             d_cells.release();
+            d_milne.release();
             d_species.release();
             d_pids.release();
             DevBuf<double>* db[] = {&d_totals, &d_b14c0, &d_b14c1, &d_b14c2, &d_ce, &d_qmu,
@@ -277,14 +280,31 @@ iss_status finish_surface(iss_handle* h) {
     return ISS_OK;
 }
 
+// sample_pT_up_to < 0: the last pT of the reference's gauss pT table
+// (src/emissionfunction.cpp:3323-3326 reads it from bin_tables/pT_gauss_table.dat;
+// 3.6943142 GeV in the reference's tables when the file is not at table_path)
+double sampling_pt_limit(const std::string& table_path) {
+    std::ifstream f(table_path + "/bin_tables/pT_gauss_table.dat");
+    double last = 3.6943142, a, b;
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream ls(line);
+        if (ls >> a >> b) last = a;
+    }
+    return last;
+}
+
 // configuration, tables and device buffers for the next generate
 iss_status prepare(iss_handle* h) {
     double v;
     if (!need(h, "MC_sampling", &v)) return ISS_ERR_PARAM_MISSING;
-    if (static_cast<int>(v) != 4)
-        return fail(h, ISS_ERR_UNSUPPORTED, "MC_sampling = %d: only the FSSW sampler (4) runs on the GPU",
-                    static_cast<int>(v));
+    const int mc = static_cast<int>(v);
+    if (mc != 4 && mc != 2)
+        return fail(h, ISS_ERR_UNSUPPORTED,
+                    "MC_sampling = %d: the GPU runs the FSSW sampler (4) and the lab-frame "
+                    "EmissionFunctionArray sampler (2)", mc);
     DevConfig c{};
+    c.mc_sampling = mc;
     const char* keys[] = {"hydro_mode", "include_deltaf_shear", "include_deltaf_bulk",
                           "bulk_deltaf_kind", "include_deltaf_diffusion",
                           "local_charge_conservation", "number_of_repeated_sampling",
@@ -330,6 +350,23 @@ iss_status prepare(iss_handle* h) {
         c.lalpha = static_cast<float>(alpha);
         c.lslot = nullptr;
         c.lpairs = nullptr;
+    }
+    if (mc == 2) {
+        // sample_using_dN_dxtdy_4all_particles_conventional (src/emissionfunction.cpp:3273-3340)
+        if (h->use_learned)
+            return fail(h, ISS_ERR_UNSUPPORTED, "gpu_sampler = 1 needs MC_sampling = 4");
+        if (c.include_bulk && c.bulk_kind != 1)
+            return fail(h, ISS_ERR_UNSUPPORTED,
+                        "MC_sampling = 2 with bulk_deltaf_kind = %d (the GPU supports kind 1)",
+                        c.bulk_kind);
+        double pt, range;
+        if (!need(h, "sample_pT_up_to", &pt) || !need(h, "sample_y_minus_eta_s_range", &range))
+            return ISS_ERR_PARAM_MISSING;
+        if (pt < 0) pt = sampling_pt_limit(h->table_path);
+        c.pt_max = static_cast<float>(pt);
+        c.yme_range = static_cast<float>(range);
+        c.restrict_df = static_cast<int>(h->params.get_or("restrict_deltaf", 1)) == 1;
+        c.df_max_ratio = static_cast<float>(h->params.get_or("deltaf_max_ratio", 1.0));
     }
     c.item_size = h->tune.item_size;
     c.yield_groups = h->tune.yield_groups;
@@ -497,6 +534,7 @@ CellArrays cell_arrays(iss_handle* h) {
     a.pi2 = b + 6 * n;
     a.coef = b + 7 * n;
     a.rec = b + 8 * n;   // 128-byte records, 128-byte aligned
+    a.milne = h->cfg.mc_sampling == 2 ? h->d_milne.ptr : nullptr;
     return a;
 }
 
@@ -514,6 +552,7 @@ iss_status run_cells(iss_handle* h) {
         h->surface_on_device = true;
     }
     CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 16));   // 8 SoA arrays + the records
+    if (c.mc_sampling == 2) CUDA_TRY(h, h->d_milne.reserve(static_cast<size_t>(n) * 6));
     CUDA_TRY(h, h->d_yields.reserve(static_cast<size_t>(n) * S));
     const size_t rows = static_cast<size_t>(c.n_surfaces) * S;
     CUDA_TRY(h, h->d_cdf.reserve(static_cast<size_t>(std::max<int64_t>(h->cdf_len, 1))));
@@ -816,7 +855,7 @@ std::vector<unsigned char> graph_key_of(iss_handle* h) {
                           h->d_offsets.ptr,  h->d_off_tiles.ptr, h->d_item_off.ptr, h->d_item_seg.ptr,
                           h->d_hadrons.ptr,  h->d_cell_of.ptr,  h->d_work.ptr,     h->d_counters.ptr,
                           h->d_error.ptr,    h->d_pois.ptr,     h->d_species.ptr,  h->d_pids.ptr,
-                          h->d_surf.ptr,     h->d_limits.ptr,   h->gh};
+                          h->d_surf.ptr,     h->d_limits.ptr,   h->gh,            h->d_milne.ptr};
     const unsigned char* pb = reinterpret_cast<const unsigned char*>(ptrs);
     k.insert(k.end(), pb, pb + sizeof(ptrs));
     const int64_t nums[] = {h->n_cells, h->n_tiles, h->cdf_len, h->guide_len, h->graph_cap_units,

@@ -75,6 +75,12 @@ struct DevConfig {
     // graph replays: (key0, key1, event_offset) of the call in device memory,
     // so one captured graph serves every seed; null: the fields above
     const uint32_t* run;
+    // MC_sampling = 2 (EmissionFunctionArray, src/emissionfunction.cpp:3273-3623,
+    // 4188-4421): pT sampled up to pt_max, y - eta_s in [-yme_range, yme_range],
+    // delta f restricted to df_max_ratio of f0 when restrict_df
+    int mc_sampling;         // 4: the FSSW sampler; 2: the lab-frame sampler
+    float pt_max, yme_range, df_max_ratio;
+    int restrict_df;
 };
 
 // floats per (species slot, cell) record of the learned proposal: for each of
@@ -105,6 +111,10 @@ struct CellArrays {
     // th2, pi1, pi2, coef): the sampler reads a random cell's record as one
     // cache line instead of eight
     float4* rec;
+    // MC_sampling = 2 only (else null): the regulated Milne-frame cell, six
+    // float4 per cell: (da0..da3), (u0..u3), (pi00 pi01 pi02 pi03),
+    // (pi11 pi12 pi13 pi22), (pi23 pi33 q0 q1), (q2 q3 bulkPi 0)
+    float4* milne;
 };
 
 // Resonance decay table (particle_decay::read_resonances_list): particles
@@ -148,7 +158,7 @@ struct HadronRec {
 };
 
 enum : uint32_t { kTagCell = 1u, kTagTry = 2u, kTagCount = 3u, kTagLearn = 5u, kTagPilot = 6u,
-                  kTagLearnRap = 7u };
+                  kTagLearnRap = 7u, kTagEfa = 8u, kTagEfaRap = 9u };
 
 // ---------------------------------------------------------------------------
 // Fixed-point cell CDF.

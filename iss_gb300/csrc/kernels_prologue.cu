@@ -200,6 +200,17 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
         pl[k] = acc;
     }
 
+    if (cells.milne) {
+        // the regulated surface cell in the Milne frame, as the reference's
+        // EmissionFunctionArray reads it (src/iSS.cpp:105-109)
+        float4* m = cells.milne + 6 * l;
+        m[0] = make_float4(da0, da1, da2, da3);
+        m[1] = make_float4(u0, u1, u2, u3);
+        m[2] = make_float4(pi[0], pi[1], pi[2], pi[3]);
+        m[3] = make_float4(pi[4], pi[5], pi[6], pi[7]);
+        m[4] = make_float4(pi[8], pi[9], q0, q1);
+        m[5] = make_float4(q2, q3, s[29], 0.0f);
+    }
     float4* rec = cells.rec + 8 * l;
     rec[0] = cells.pos[l] = make_float4(tau, xpt, ypt, eta);
     rec[1] = cells.da[l] = make_float4(dl[0], -dl[1], -dl[2], -dl[3]);

@@ -675,6 +675,183 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
 }
 
 // ---------------------------------------------------------------------------
+// MC_sampling = 2: the reference's EmissionFunctionArray sampler
+// (sample_using_dN_dxtdy_4all_particles_conventional and
+// sample_momemtum_from_a_fluid_cell, src/emissionfunction.cpp:3273-3623,
+// 4188-4309).  Per hadron a cell is drawn from the same per-species CDF as in
+// FSSW; then pT is proposed from pT dpT on [0, pT_max], phi uniformly and
+// y - eta_s uniformly in [-range, range] in the lab (Milne) frame, and the
+// proposal is accepted with f0 p.dsigma tau (1 + delta f) / maximum, where the
+// maximum is the reference's analytic upper bound of the emission function
+// (estimate_maximum, src/emissionfunction.cpp:4309-4421).  After 5,000 tries
+// the cell is drawn again (src/emissionfunction.cpp:3475-3480).
+
+constexpr float kEfaInvE = 0.3678794f;   // the reference's cut for 1/e
+
+// principal branch W0(x) for x >= -1/e: series about the branch point or a
+// logarithmic start, then Halley iterations
+__device__ float lambert_w0(float x) {
+    if (x <= -0.36787944f) return -1.0f;
+    float w;
+    if (x < -0.25f) {
+        const float pp = sqrtf(2.0f * (2.7182818f * x + 1.0f));
+        w = -1.0f + pp * (1.0f + pp * (-1.0f / 3.0f + pp * (11.0f / 72.0f)));
+    } else if (x < 3.0f) {
+        w = log1pf(x) * (1.0f - 0.25f * log1pf(x) / (1.0f + log1pf(x)));
+    } else {
+        const float l1 = logf(x), l2 = logf(l1);
+        w = l1 - l2 + l2 / l1;
+    }
+#pragma unroll
+    for (int it = 0; it < 5; it++) {
+        const float ew = expf(w);
+        const float f = w * ew - x;
+        const float wp1 = w + 1.0f;
+        if (fabsf(wp1) < 1e-6f) break;
+        w -= f / (ew * wp1 - (w + 2.0f) * f / (2.0f * wp1));
+    }
+    return w;
+}
+
+// max over E >= m of E^A f0(E) (estimate_ideal_maximum / the A = 2, 3 forms of
+// estimate_shear_viscous_maximum and estimate_diffusion_maximum): the
+// stationary point solves (beta E - A) exp(beta E - A) = sign A exp(beta mu - A)
+__device__ float ea_f0_max(int sign, int A, float m, float T, float mu, float f0m) {
+    const float iT = 1.0f / T;
+    const float mA = m * m * (A == 3 ? m : (A == 2 ? 1.0f : 1.0f / m));   // m^A
+    if (sign == 1) {
+        float Emax = T * (lambert_w0(A * expf(iT * mu - A)) + A);
+        if (Emax < m) Emax = m;
+        const float eA = A == 1 ? Emax : (A == 2 ? Emax * Emax : Emax * Emax * Emax);
+        return eA / (expf((Emax - mu) * iT) + sign);
+    }
+    const float rhs = A * expf(iT * mu - A);
+    if (rhs > kEfaInvE) return mA * f0m;
+    // z exp(-z) = rhs with z <= 1, i.e. z = -W0(-rhs)
+    const float Emax = T * (A + lambert_w0(-rhs));
+    if (Emax < m) return mA * f0m;
+    const float eA = A == 1 ? Emax : (A == 2 ? Emax * Emax : Emax * Emax * Emax);
+    return fmaxf(eA / (expf((Emax - mu) * iT) + sign), mA * f0m);
+}
+
+struct PropEfa {
+    float tau, T, mu, m, bmax;     // bmax: the reference's maximum / (degen prefactor)
+    float da0, da1, da2, da3, u0, u1, u2, u3;
+    float pi00, pi01, pi02, pi03, pi11, pi12, pi13, pi22, pi23, pi33;
+    float q0, q1, q2, q3;
+    float shear_pref, bulk_c0, bulk_c1, bulkPi, qpref, ikappa;
+    int sign, baryon;
+};
+
+// one (cell, species): the Milne cell and the maximum (estimate_maximum)
+__device__ bool setup_efa(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp, int l,
+                          PropEfa& p, bool keep_max) {
+    const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
+    const float4* mr = cells.milne + 6 * static_cast<int64_t>(l);
+    const float4 pos = __ldg(rec), th = __ldg(rec + 3), th2 = __ldg(rec + 4), cf = __ldg(rec + 7);
+    const float4 m0 = __ldg(mr), m1 = __ldg(mr + 1), m2 = __ldg(mr + 2), m3 = __ldg(mr + 3);
+    const float4 m4 = __ldg(mr + 4), m5 = __ldg(mr + 5);
+    p.tau = pos.x;
+    p.T = th.x;
+    p.m = sp.m_hi + sp.m_lo;
+    p.mu = static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
+           static_cast<float>(sp.charge) * th.w;
+    p.sign = sp.sign;
+    p.baryon = sp.baryon;
+    p.da0 = m0.x; p.da1 = m0.y; p.da2 = m0.z; p.da3 = m0.w;
+    p.u0 = m1.x; p.u1 = m1.y; p.u2 = m1.z; p.u3 = m1.w;
+    p.pi00 = m2.x; p.pi01 = m2.y; p.pi02 = m2.z; p.pi03 = m2.w;
+    p.pi11 = m3.x; p.pi12 = m3.y; p.pi13 = m3.z; p.pi22 = m3.w;
+    p.pi23 = m4.x; p.pi33 = m4.y; p.q0 = m4.z; p.q1 = m4.w;
+    p.q2 = m5.x; p.q3 = m5.y;
+    const float ep = th2.x + th2.y;
+    p.shear_pref = cfg.include_shear ? 1.0f / (2.0f * p.T * p.T * ep) : 0.0f;
+    p.bulkPi = cfg.include_bulk ? m5.z / 0.197327053f : 0.0f;   // fm^-4 (bulk_deltaf_kind 1)
+    p.bulk_c0 = cf.x;
+    p.bulk_c1 = cf.y;
+    p.qpref = cfg.include_diff ? th2.z / ep : 0.0f;
+    p.ikappa = cfg.include_diff ? 1.0f / cf.w : 0.0f;
+    if (keep_max) return true;
+    // estimate_maximum (src/emissionfunction.cpp:4309-4421)
+    const float udsig = p.tau * (p.u0 * p.da0 + p.u1 * p.da1 + p.u2 * p.da2 + p.u3 * p.da3 / p.tau);
+    const float dsig2 = p.tau * p.tau * (p.da0 * p.da0 - p.da1 * p.da1 - p.da2 * p.da2 -
+                                         p.da3 * p.da3 / (p.tau * p.tau));
+    const float dsigT = sqrtf(fabsf(dsig2 - udsig * udsig));
+    const float dsig_all = fabsf(udsig) + dsigT;
+    const float f0m = 1.0f / (expf((p.m - p.mu) / p.T) + p.sign);
+    const float g_ideal = ea_f0_max(p.sign, 1, p.m, p.T, p.mu, f0m);
+    float g = g_ideal;
+    const float tmpf = p.sign == -1 ? 2.0f : 1.0f;
+    if (cfg.include_shear) {
+        const float tr = p.pi00 * p.pi00 + p.pi11 * p.pi11 + p.pi22 * p.pi22 + p.pi33 * p.pi33 -
+                         2.f * p.pi01 * p.pi01 - 2.f * p.pi02 * p.pi02 - 2.f * p.pi03 * p.pi03 +
+                         2.f * p.pi12 * p.pi12 + 2.f * p.pi13 * p.pi13 + 2.f * p.pi23 * p.pi23;
+        const float pi_size = sqrtf(fmaxf(tr, 0.0f)) / ep;
+        g += ea_f0_max(p.sign, 3, p.m, p.T, p.mu, f0m) * tmpf / (2.0f * p.T * p.T) * pi_size;
+    }
+    if (cfg.include_bulk)
+        g += fabsf(p.bulkPi * p.bulk_c0) * p.m * p.m / p.T / 3.0f * f0m * (1.0f - p.sign * f0m);
+    if (cfg.include_diff) {
+        const float qsq = p.q0 * p.q0 - p.q1 * p.q1 - p.q2 * p.q2 - p.q3 * p.q3;
+        float gq = p.qpref * ea_f0_max(p.sign, 2, p.m, p.T, p.mu, f0m);
+        if (p.baryon > 0) gq += p.baryon * g_ideal;
+        g += gq * tmpf * sqrtf(fabsf(qsq)) * p.ikappa;
+    }
+    p.bmax = dsig_all * g;
+    return true;
+}
+
+// one lab-frame proposal (sample_momemtum_from_a_fluid_cell): pl = (pT, phi,
+// y - eta_s, -) on acceptance, u_rap the uniform of the rapidity draw
+__device__ __forceinline__ bool try_efa(const DevConfig& cfg, const PropEfa& p, const Unit& u,
+                                        float4& pl, float& u_rap, unsigned& violations) {
+    const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagEfa << 16);
+    const uint4 A = block(u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    const float pT = sqrtf(cfg.pt_max * cfg.pt_max * u01f(A.x));
+    const float phi = 2.0f * 3.14159265f * u01f(A.y);
+    const float yme = (1.0f - 2.0f * u01f(A.z)) * cfg.yme_range;
+    const float mT = sqrtf(p.m * p.m + pT * pT);
+    float sphi, cphi;
+    sincosf(phi, &sphi, &cphi);
+    const float px = pT * cphi, py = pT * sphi;
+    const float p0 = mT * coshf(yme), p3 = mT * sinhf(yme);
+    const float pdotu = p0 * p.u0 - px * p.u1 - py * p.u2 - p3 * p.u3;
+    const float f0 = 1.0f / (expf((pdotu - p.mu) / p.T) + p.sign);
+    const float pdsig = p0 * p.da0 + px * p.da1 + py * p.da2 + p3 * p.da3 / p.tau;
+    const float one_m = 1.0f - p.sign * f0;
+    float df = 0.0f;
+    if (cfg.include_shear) {
+        const float W = p0 * p0 * p.pi00 - 2.f * p0 * px * p.pi01 - 2.f * p0 * py * p.pi02 -
+                        2.f * p0 * p3 * p.pi03 + px * px * p.pi11 + 2.f * px * py * p.pi12 +
+                        2.f * px * p3 * p.pi13 + py * py * p.pi22 + 2.f * py * p3 * p.pi23 +
+                        p3 * p3 * p.pi33;
+        df += one_m * W * p.shear_pref;
+    }
+    if (cfg.include_bulk) {
+        const float EoT = pdotu / p.T, moT = p.m / p.T;
+        df += -one_m * p.bulk_c0 * (moT * moT / (3.0f * EoT) - p.bulk_c1 * EoT) * p.bulkPi;
+    }
+    if (cfg.include_diff) {
+        const float qf = p0 * p.q0 - px * p.q1 - py * p.q2 - p3 * p.q3;
+        df += one_m * (p.qpref - p.baryon / pdotu) * qf * p.ikappa;
+    }
+    float resize = 1.0f;
+    if (cfg.restrict_df) resize = fminf(1.0f, cfg.df_max_ratio / (fabsf(df) + 1e-10f));
+    const float result = f0 * pdsig * p.tau * (1.0f + df * resize);
+    const float acc = result / p.bmax;
+    if (acc > 1.0f) violations++;
+    if (!(u01f(A.w) < acc)) return false;
+    pl = make_float4(pT, phi, yme, 0.0f);
+    u_rap = 0.0f;
+    if (cfg.hydro_mode != 2) {
+        const uint4 B = block(u.t, u.i, u.eg, static_cast<uint32_t>(u.s) | (kTagEfaRap << 16),
+                              cfg.key0, cfg.key1);
+        u_rap = u01f(B.x);
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // Learned proposal.  The target density of a (cell, species) pair in the
 // rest frame, per dK dOmega with K = (E - m)/T, is P(K, n) a(K, n): P is the
 // plain proposal above (Gamma mixture in K, flux-linear direction) and a its
@@ -907,6 +1084,55 @@ __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& 
                  pos.x * sinhf(eta_s));
 }
 
+// add_one_sampled_particle of the EmissionFunctionArray path
+// (src/emissionfunction.cpp:4423-4475): rapidity y = (y - eta_s) + eta_s,
+// eta_s the cell's (3+1D) or drawn from a uniform rapidity (boost invariant)
+__device__ void emit_efa(const DevConfig& cfg, const CellArrays& cells, const PropEfa& p, int l,
+                         int pid, float4 pl, float u_rap, HadronRec* out, int64_t slot) {
+    const float4 pos = __ldg(cells.rec + 8 * static_cast<int64_t>(l));
+    const float pT = pl.x, yme = pl.z;
+    float eta_s = pos.w;
+    if (cfg.hydro_mode != 2) eta_s = cfg.y_lb + (cfg.y_rb - cfg.y_lb) * u_rap - yme;
+    const float y = yme + eta_s;
+    float sphi, cphi;
+    sincosf(pl.y, &sphi, &cphi);
+    const float mT = sqrtf(p.m * p.m + pT * pT);
+    write_hadron(out, slot, pid, p.m, mT * coshf(y), pT * cphi, pT * sphi, mT * sinhf(y),
+                 pos.x * coshf(eta_s), pos.y, pos.z, pos.x * sinhf(eta_s));
+}
+
+// the two samplers behind one work loop: FSSW (Prop) and the lab-frame
+// EmissionFunctionArray sampler (PropEfa)
+template <int kAlg> struct PropOf { using type = Prop; };
+template <> struct PropOf<2> { using type = PropEfa; };
+
+__device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
+                                          const SpeciesDev& sp, int l, Prop& p, bool) {
+    return setup_prop(cfg, cells, sp, l, p);
+}
+__device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
+                                          const SpeciesDev& sp, int l, PropEfa& p, bool keep_max) {
+    return setup_efa(cfg, cells, sp, l, p, keep_max);
+}
+__device__ __forceinline__ bool try_any(const DevConfig& cfg, const Prop& p, const Unit& u, float4& pl,
+                                        float& u_rap, unsigned& viol) {
+    return try_once(cfg, p, u, pl, u_rap, viol);
+}
+__device__ __forceinline__ bool try_any(const DevConfig& cfg, const PropEfa& p, const Unit& u,
+                                        float4& pl, float& u_rap, unsigned& viol) {
+    return try_efa(cfg, p, u, pl, u_rap, viol);
+}
+__device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells, const Prop& p,
+                                         int l, int pid, float4 pl, float u_rap, HadronRec* out,
+                                         int64_t slot) {
+    emit(cfg, cells, p, l, pid, pl, u_rap, out, slot);
+}
+__device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells,
+                                         const PropEfa& p, int l, int pid, float4 pl, float u_rap,
+                                         HadronRec* out, int64_t slot) {
+    emit_efa(cfg, cells, p, l, pid, pl, u_rap, out, slot);
+}
+
 // Cell of every hadron's first draw (redraw 0), one warp per work item in
 // species-major order.  Each lane runs independent searches, so the latency
 // of the guide and CDF reads overlaps across many warps; the sampler then
@@ -995,7 +1221,7 @@ constexpr int kSampleThreads = 256;
 
 // kLcc: local_charge_conservation pairs (a separate instantiation, so the
 // common case carries none of the pair state)
-template <bool kLcc, bool kLearned>
+template <bool kLcc, bool kLearned, int kAlg>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
@@ -1016,7 +1242,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
     bool exhausted = false;
     bool active = false;
     Unit u;
-    Prop p;
+    typename PropOf<kAlg>::type p;
     int pid = 0;
     unsigned long long n_tries = 0, n_redraws = 0, n_fail = 0;
     unsigned n_viol = 0;
@@ -1113,7 +1339,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
                                    : nullptr;
                 }
-                if (!setup_prop(cfg, cells, species[u.s], l, p)) {
+                if (!setup_any(cfg, cells, species[u.s], l, p, false)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     for (int q = 0; q < (kLcc ? u.mult : 1); q++)
@@ -1126,12 +1352,16 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
             float4 pl;
             float u_rap;
             bool ok;
-            if (kLearned && u.lp) {
-                ok = try_learned(cfg, p, u, u.lp, pl, u_rap, n_lviol);
-                n_ltries++;
-                n_lhad += ok;
+            if constexpr (kLearned) {
+                if (u.lp) {
+                    ok = try_learned(cfg, p, u, u.lp, pl, u_rap, n_lviol);
+                    n_ltries++;
+                    n_lhad += ok;
+                } else {
+                    ok = try_once(cfg, p, u, pl, u_rap, n_viol);
+                }
             } else {
-                ok = try_once(cfg, p, u, pl, u_rap, n_viol);
+                ok = try_any(cfg, p, u, pl, u_rap, n_viol);
             }
             u.t++;
             u.tries_cell++;
@@ -1141,9 +1371,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                 // hadron's cell: the training rows of the learned proposal)
                 if (u.redraw > 0 && u.phase == 0) cell_of[u.slot] = u.cell;
                 if (kLcc)
-                    emit(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out, u.slot + u.phase);
+                    emit_any(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out,
+                             u.slot + u.phase);
                 else
-                    emit(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
+                    emit_any(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
                 if (kLcc && u.mult == 2 && u.phase == 0) {
                     // the partner: same cell and mass, opposite B, S, Q
                     SpeciesDev sp2 = species[u.s];
@@ -1153,7 +1384,9 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.phase = 1;
                     u.tries_cell = 0;
                     u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
-                    if (!setup_prop(cfg, cells, sp2, u.cell, p)) {
+                    // (the lab-frame sampler keeps the hadron's maximum for
+                    // its partner, src/emissionfunction.cpp:3503-3509)
+                    if (!setup_any(cfg, cells, sp2, u.cell, p, true)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
                         write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
@@ -1448,8 +1681,11 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    auto kernel = cfg.lpairs ? (cfg.lcc ? sampler_kernel<true, true> : sampler_kernel<false, true>)
-                             : (cfg.lcc ? sampler_kernel<true, false> : sampler_kernel<false, false>);
+    auto kernel = cfg.mc_sampling == 2
+                      ? (cfg.lcc ? sampler_kernel<true, false, 2> : sampler_kernel<false, false, 2>)
+                  : cfg.lpairs
+                      ? (cfg.lcc ? sampler_kernel<true, true, 4> : sampler_kernel<false, true, 4>)
+                      : (cfg.lcc ? sampler_kernel<true, false, 4> : sampler_kernel<false, false, 4>);
     kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters, k_end_dev);

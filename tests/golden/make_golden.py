@@ -173,6 +173,28 @@ def decays_case(visc_params, work_root):
                      randomSeed=15), work_root)
 
 
+# keys the reference's EmissionFunctionArray path (MC_sampling = 2) reads,
+# with the values of its own iSS_parameters.dat
+EFA_KEYS = dict(MC_sampling=2, restrict_deltaf=1, deltaf_max_ratio=1.0, sample_pT_up_to=-1,
+                sample_y_minus_eta_s_range=3, use_historic_flow_output_format=0, use_pos_dN_only=0,
+                minimum_emission_function_val=1e-30, calculate_vn_to_order=9, output_dN_dxtdy_4all=0,
+                calculate_dN_deta=0, calculate_dN_dphi=0, calculate_dN_dtau=0, calculate_dN_dx=0,
+                calculate_dN_dxt=0, bin_dtau=0.2, bin_dx=0.5, bin_tau0=0.6, bin_tau_max=17.0,
+                bin_x_max=10.0, bin_x_min=-10.0)
+
+
+def efa_cases(work_root, events_visc=20000, events_ideal=400):
+    """MC_sampling = 2 (EmissionFunctionArray::sample_using_dN_dxtdy_4all_particles_
+    conventional): lab-frame rejection with the estimated maximum."""
+    sample_case("efa_viscous_rta", S.viscous_3d(256, seed=2),
+                dict(EFA_KEYS, hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
+                     include_deltaf_bulk=1, bulk_deltaf_kind=1, turn_on_bulk=1,
+                     number_of_repeated_sampling=events_visc, randomSeed=16), work_root)
+    sample_case("efa_ideal_boost_invariant", S.ideal_boost_invariant(),
+                dict(EFA_KEYS, hydro_mode=1, afterburner_type=0, include_deltaf_shear=1,
+                     number_of_repeated_sampling=events_ideal, randomSeed=17), work_root)
+
+
 def main():
     import argparse
     ap = argparse.ArgumentParser()
@@ -182,6 +204,12 @@ def main():
     work_root = tempfile.mkdtemp(prefix="iss_golden_")
     visc_params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
                        include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1)
+    if only == "samples_efa":
+        try:
+            efa_cases(work_root)
+        finally:
+            shutil.rmtree(work_root, ignore_errors=True)
+        return
     if only in ("samples_viscous_lcc", "samples_viscous_decays"):
         try:
             (lcc_case if only == "samples_viscous_lcc" else decays_case)(visc_params, work_root)
@@ -220,6 +248,7 @@ def main():
                          number_of_repeated_sampling=1000, randomSeed=13), work_root)
         lcc_case(visc_params, work_root)
         decays_case(visc_params, work_root)
+        efa_cases(work_root)
     finally:
         shutil.rmtree(work_root, ignore_errors=True)
 

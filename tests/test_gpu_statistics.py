@@ -2,6 +2,8 @@
 
 * spectra (pT, y, phi, v2 in pT bins) and mean multiplicities per species
   against hadrons sampled by the reference itself (tests/golden/samples_*),
+  for the FSSW sampler (MC_sampling = 4) and the lab-frame sampler
+  (MC_sampling = 2, samples_efa_*),
   with the reference's fermion |p| proposal reproduced
   (gpu_compat_fermion_cdf2 = 1); family-wise level 0.01 (Bonferroni);
 * |p| of a static ideal cell against the analytic p^2 f(E) spectrum;
@@ -69,7 +71,10 @@ def observables(h):
 
 @pytest.mark.parametrize("name,events", [("static_viscous", 40000), ("viscous_14moment", 100000),
                                          ("ideal_boost_invariant", 1000), ("viscous_lcc", 30000),
-                                         ("viscous_decays", 20000)])
+                                         ("viscous_decays", 20000),
+                                         # MC_sampling = 2, the lab-frame sampler
+                                         ("efa_viscous_rta", 40000),
+                                         ("efa_ideal_boost_invariant", 1000)])
 def test_spectra_match_reference_samples(name, events):
     g, s = sample_case(name, events, seed=4242)
     had, off = s.all_hadrons()

@@ -109,7 +109,7 @@ def test_unsupported_options_are_reported():
     s = iSS(".")
     s.set_params(**S.DEFAULT_PARAMETERS)
     s.set_surface(surf.fo_surf())
-    s.setVal("MC_sampling", 2)
+    s.setVal("MC_sampling", 3)
     with pytest.raises(IssError) as e:
         s.generate_samples()
     assert e.value.status in (4, 5)   # unsupported (or no CUDA device here)
