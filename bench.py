@@ -418,6 +418,12 @@ def run_gpu(args, ws, rank, local):
         params["perform_decays"] = 1
     if args.graph:
         params["gpu_graph"] = 1
+    if args.mc_sampling == 2:
+        # the lab-frame sampler with the reference's own defaults
+        # (iSS_parameters.dat: bulk_deltaf_kind 1, restrict_deltaf 1,
+        # sample_pT_up_to -1, sample_y_minus_eta_s_range 3)
+        params.update(MC_sampling=2, bulk_deltaf_kind=1, restrict_deltaf=1, deltaf_max_ratio=1.0,
+                      sample_pT_up_to=-1, sample_y_minus_eta_s_range=3)
     s = iSS(".", inputfile="")
     s.set_params(**params)
     if batch is not None:
@@ -589,7 +595,7 @@ def run_gpu(args, ws, rank, local):
                     "kernel_ms_per_launch": 1e3 * samp_sec / args.steps,
                     "yields_kernel_ms_per_launch": 1e3 * local_stats[3] / args.steps}
         cpu = None
-        if not args.no_cpu_baseline and args.workload == "viscous":
+        if not args.no_cpu_baseline and args.workload == "viscous" and args.mc_sampling == 4:
             h_cpu, t_cpu = cpu_baseline(1, args.cpu_cells, N_EVENTS, seed=7)
             cpu = {"value": h_cpu / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
                    "sample": f"viscous 3+1D surface, every {N_CELLS // args.cpu_cells}th cell "
@@ -601,7 +607,9 @@ def run_gpu(args, ws, rank, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": wl["data"],
                 "config": {"workload": (f"viscous_3d_{args.cells // 1000}k_cells_s95p_"
-                                        f"{n_events}_events" if args.workload == "viscous" else
+                                        f"{n_events}_events" + ("_mc2_kind1_bulk" if
+                                                                args.mc_sampling == 2 else "")
+                                        if args.workload == "viscous" else
                                         f"{args.workload}_{total_cells}_cells_"
                                         f"{n_events}_events" + (f"_{args.surfaces}_surfaces"
                                                                 if batch is not None else "")),
@@ -610,6 +618,7 @@ def run_gpu(args, ws, rank, local):
                            "delta_f": {k: v for k, v in wl["params"].items()
                                        if k.startswith("include_") or k == "bulk_deltaf_kind"},
                            "sampler": args.sampler, "decays": bool(args.decays),
+                           "MC_sampling": args.mc_sampling,
                            "graph_replay": bool(args.graph), "launch_shape": tuning,
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
@@ -675,6 +684,9 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="default launch shape (default: the library's autotuner picks it on "
                          "the workload before the warm-up)")
+    ap.add_argument("--mc-sampling", type=int, choices=[2, 4], default=4,
+                    help="4: the FSSW sampler; 2: the lab-frame EmissionFunctionArray sampler "
+                         "(bulk delta f kind 1)")
     ap.add_argument("--sampler", choices=["plain", "learned"], default="plain",
                     help="learned: train the proposal network first, then sample with it")
     ap.add_argument("--train-momenta", type=int, default=50_000_000)
