@@ -367,6 +367,10 @@ iss_status prepare(iss_handle* h) {
         c.yme_range = static_cast<float>(range);
         c.restrict_df = static_cast<int>(h->params.get_or("restrict_deltaf", 1)) == 1;
         c.df_max_ratio = static_cast<float>(h->params.get_or("deltaf_max_ratio", 1.0));
+        // the reference gives a cell 4,999 proposals before drawing another
+        // (tries = 1 .. maximum_impatience - 1, src/emissionfunction.cpp:4205-4300);
+        // at this sampler's acceptance the cap shapes which cells are sampled
+        if (!h->params.has("gpu_max_tries")) c.max_tries = 4999;
     }
     c.item_size = h->tune.item_size;
     c.yield_groups = h->tune.yield_groups;

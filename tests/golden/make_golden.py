@@ -193,6 +193,11 @@ def efa_cases(work_root, events_visc=20000, events_ideal=400):
     sample_case("efa_ideal_boost_invariant", S.ideal_boost_invariant(),
                 dict(EFA_KEYS, hydro_mode=1, afterburner_type=0, include_deltaf_shear=1,
                      number_of_repeated_sampling=events_ideal, randomSeed=17), work_root)
+    sample_case("efa_viscous_lcc", S.viscous_3d(256, seed=2),
+                dict(EFA_KEYS, hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
+                     include_deltaf_bulk=1, bulk_deltaf_kind=1, turn_on_bulk=1,
+                     local_charge_conservation=1, number_of_repeated_sampling=events_visc,
+                     randomSeed=18), work_root)
 
 
 def main():
@@ -204,9 +209,16 @@ def main():
     work_root = tempfile.mkdtemp(prefix="iss_golden_")
     visc_params = dict(hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
                        include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1)
-    if only == "samples_efa":
+    if only in ("samples_efa", "samples_efa_viscous_lcc"):
         try:
-            efa_cases(work_root)
+            if only == "samples_efa":
+                efa_cases(work_root)
+            else:
+                sample_case("efa_viscous_lcc", S.viscous_3d(256, seed=2),
+                            dict(EFA_KEYS, hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
+                                 include_deltaf_bulk=1, bulk_deltaf_kind=1, turn_on_bulk=1,
+                                 local_charge_conservation=1, number_of_repeated_sampling=20000,
+                                 randomSeed=18), work_root)
         finally:
             shutil.rmtree(work_root, ignore_errors=True)
         return

@@ -74,7 +74,8 @@ def observables(h):
                                          ("viscous_decays", 20000),
                                          # MC_sampling = 2, the lab-frame sampler
                                          ("efa_viscous_rta", 40000),
-                                         ("efa_ideal_boost_invariant", 1000)])
+                                         ("efa_ideal_boost_invariant", 1000),
+                                         ("efa_viscous_lcc", 30000)])
 def test_spectra_match_reference_samples(name, events):
     g, s = sample_case(name, events, seed=4242)
     had, off = s.all_hadrons()
