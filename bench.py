@@ -326,6 +326,26 @@ def surface_spread(s, batch, b_cells, b_events, params, iSS):
     return out
 
 
+def yields_vs_oracle(s, run_params):
+    """Per-species yields of the timed surface (FP32 arithmetic with an FP64
+    reduction on the GPU, read from the handle) against the FP64 CPU oracle
+    (oracle/, the reference's yields restated, pinned bit-exact to the
+    reference's own values): every cell, every species."""
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib as O
+    from iss_gb300 import surfaces as S
+    fo = S.viscous_3d(N_CELLS, seed=SEED_SURFACE).fo_surf()
+    lrf, keep = O.lrf_cells(fo)
+    sp = O.chosen_species(S.TABLE_DIR, 0)
+    oc = O.OracleConfig(dict(run_params), S.TABLE_DIR, n_events=1, seed=1)
+    ref = O.yields(oc, sp, lrf, keep).sum(1)
+    gpu = s.species_yields()
+    rel = np.abs(gpu - ref) / np.maximum(np.abs(ref), 1e-300)
+    return {"cells": int(fo.shape[0]), "species": int(len(sp)), "max_rel_err": float(rel.max()),
+            "median_rel_err": float(np.median(rel)), "bar": 1e-6,
+            "worst_species_pid": int(sp["pid"][int(rel.argmax())])}
+
+
 def learned_report(s, timings, args):
     """Acceptance of the learned proposal against the plain sampler's on the
     same species (alpha -> 0 with the envelope at 1), the plain sampler's step
@@ -557,6 +577,11 @@ def run_gpu(args, ws, rank, local):
 
     if learned is not None:
         learned.update(learned_report(s, timings, args))
+    yields_check = None
+    if rank == 0 and args.workload == "viscous" and args.cells == N_CELLS and not args.no_oracle_check:
+        s.set_params(gpu_sampler=0)
+        s.generate_samples()
+        yields_check = yields_vs_oracle(s, params)
     per_surface = None
     if batch is not None and rank == 0:
         per_surface = surface_spread(s, batch, b_cells, b_events, params, iSS)
@@ -636,6 +661,8 @@ def run_gpu(args, ws, rank, local):
                 "tries_per_hadron": timings["n_tries"] / max(timings["n_hadrons"], 1)}
         if per_surface is not None:
             line["per_surface"] = per_surface
+        if yields_check is not None:
+            line["yields_vs_fp64_oracle"] = yields_check
         if learned is not None:
             peak_tf = 1922.0
             try:
@@ -674,6 +701,8 @@ def main():
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true",
+                    help="skip the per-species yields against the FP64 CPU oracle")
     ap.add_argument("--decays", action="store_true",
                     help="perform_decays = 1 (resonance decays after sampling, timed apart)")
     ap.add_argument("--oscar", action="store_true",
