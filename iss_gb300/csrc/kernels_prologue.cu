@@ -9,10 +9,15 @@
 // through the (t, z) frame, where terms of size cosh(eta)^2 u^t cancel down
 // to O(1), so the result is only reproducible by rounding at the same points
 // as the reference (float storage of u^t, dsigma^mu, pi^{mu nu}_{tz}; double
-// boost matrix and products).
+// boost matrix and products).  The double temporaries are float-float pairs
+// (ffloat.cuh, about 48 bits): each rounds to the same float as the
+// reference's double unless it lies within about 2^-46 of a float rounding
+// boundary, and the FP64 pipe, a small fraction of the FP32 rate on GB300,
+// is left to cosh/sinh of eta and the delta-f coefficient lookups.
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
+#include "ffloat.cuh"
 #include "kernels.h"
 
 namespace iss {
@@ -122,58 +127,81 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
     float pi[10];
     for (int k = 0; k < 10; k++) pi[k] = s[19 + k];
 
-    // regulate_surface_cells
-    const float u0 = static_cast<float>(sqrt(1. + u1 * u1 + u2 * u2 + u3 * u3));
+    // regulate_surface_cells.  Each double temporary of the reference is a
+    // float-float value here; float operations stay float, in the
+    // reference's order (C++ promotes a float product to double only after
+    // rounding it to float).
+    const float u0 = ff_to_float(ff_sqrt(
+        ff_add(ff_add(ff_two_sum(1.0f, u1 * u1), ff_of(u2 * u2)), ff_of(u3 * u3))));
     const float q0 = ((u1 * q1 + u2 * q2 + u3 * q3) / u0);
     {
-        const double g[4] = {-1., 1., 1., 1.};
-        const double u[4] = {u0, u1, u2, u3};
-        double W[4][4] = {{pi[0], pi[1], pi[2], pi[3]},
-                          {pi[1], pi[4], pi[5], pi[6]},
-                          {pi[2], pi[5], pi[7], pi[8]},
-                          {pi[3], pi[6], pi[8], pi[9]}};
-        double udp[4], umu[4];
+        const float g[4] = {-1.f, 1.f, 1.f, 1.f};
+        const float u[4] = {u0, u1, u2, u3};
+        const float W[4][4] = {{pi[0], pi[1], pi[2], pi[3]},
+                               {pi[1], pi[4], pi[5], pi[6]},
+                               {pi[2], pi[5], pi[7], pi[8]},
+                               {pi[3], pi[6], pi[8], pi[9]}};
+        ff udp[4];
         for (int i = 0; i < 4; i++) {
-            udp[i] = (-u[0] * W[0][i] + u[1] * W[1][i] + u[2] * W[2][i] + u[3] * W[3][i]);
-            umu[i] = g[i] * u[i];
+            ff t = ff_two_prod(-u[0], W[0][i]);
+            t = ff_add(t, ff_two_prod(u[1], W[1][i]));
+            t = ff_add(t, ff_two_prod(u[2], W[2][i]));
+            udp[i] = ff_add(t, ff_two_prod(u[3], W[3][i]));
         }
-        const double tr = -W[0][0] + W[1][1] + W[2][2] + W[3][3];
-        double udpdu = 0.0;
+        const ff tr = ff_add(ff_add(ff_two_sum(-W[0][0], W[1][1]), ff_of(W[2][2])), ff_of(W[3][3]));
+        ff udpdu = ff_of(0.0f);
         for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) udpdu += umu[i] * W[i][j] * umu[j];
+            for (int j = 0; j < 4; j++)
+                udpdu = ff_add(udpdu, ff_mul_f(ff_two_prod(g[i] * u[i], W[i][j]), g[j] * u[j]));
+        const ff third = ff{0.333333343f, -9.93410746e-9f};   // 1/3 as a float pair
+        const ff trsum = ff_add(tr, udpdu);
         const int ii[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
         const int jj[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
         for (int k = 0; k < 10; k++) {
             const int i = ii[k], j = jj[k];
-            const double gij = (i == j) ? g[i] : 0.0;
-            pi[k] = static_cast<float>(W[i][j] + u[i] * udp[j] + u[j] * udp[i] +
-                                       u[i] * u[j] * udpdu -
-                                       1. / 3. * (gij + u[i] * u[j]) * (tr + udpdu));
+            const float gij = (i == j) ? g[i] : 0.0f;
+            const ff uu = ff_two_prod(u[i], u[j]);
+            ff v = ff_add(ff_of(W[i][j]), ff_mul_f(udp[j], u[i]));
+            v = ff_add(v, ff_mul_f(udp[i], u[j]));
+            v = ff_add(v, ff_mul(uu, udpdu));
+            v = ff_sub(v, ff_mul(ff_mul(third, ff_add(ff_of(gij), uu)), trsum));
+            pi[k] = ff_to_float(v);
         }
     }
 
-    // transform_to_local_rest_frame
+    // transform_to_local_rest_frame (cosh and sinh of the double eta, rounded
+    // to float, stay in FP64: every later rounding point depends on them)
     const float ch = static_cast<float>(cosh(static_cast<double>(eta)));
     const float sh = static_cast<float>(sinh(static_cast<double>(eta)));
     const float ut = u0 * ch + u3 * sh;
     const float uz = u3 * ch + u0 * sh;
     const float ux = u1, uy = u2;
-    const double L[4][4] = {
-        {ut, -ux, -uy, -uz},
-        {-ux, 1. + ux * ux / (ut + 1.), ux * uy / (ut + 1.), ux * uz / (ut + 1.)},
-        {-uy, ux * uy / (ut + 1.), 1. + uy * uy / (ut + 1.), uy * uz / (ut + 1.)},
-        {-uz, ux * uz / (ut + 1.), uy * uz / (ut + 1.), 1. + uz * uz / (ut + 1.)}};
+    const ff den = ff_two_sum(ut, 1.0f);
+    const ff Lxx = ff_add(ff_of(1.0f), ff_div(ff_of(ux * ux), den));
+    const ff Lyy = ff_add(ff_of(1.0f), ff_div(ff_of(uy * uy), den));
+    const ff Lzz = ff_add(ff_of(1.0f), ff_div(ff_of(uz * uz), den));
+    const ff Lxy = ff_div(ff_of(ux * uy), den);
+    const ff Lxz = ff_div(ff_of(ux * uz), den);
+    const ff Lyz = ff_div(ff_of(uy * uz), den);
+    const ff L[4][4] = {{ff_of(ut), ff_of(-ux), ff_of(-uy), ff_of(-uz)},
+                        {ff_of(-ux), Lxx, Lxy, Lxz},
+                        {ff_of(-uy), Lxy, Lyy, Lyz},
+                        {ff_of(-uz), Lxz, Lyz, Lzz}};
     const float da_up[4] = {tau * da0 * ch - da3 * sh, -tau * da1, -tau * da2,
                             -da3 * ch + tau * da0 * sh};
     float dl[4] = {0.f, 0.f, 0.f, 0.f};
     for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) dl[i] += L[i][j] * da_up[j];
+        for (int j = 0; j < 4; j++) dl[i] = ff_to_float(ff_add(ff_of(dl[i]), ff_mul_f(L[i][j], da_up[j])));
     const float qt[4] = {q0 * ch + q3 * sh, q1, q2, q3 * ch + q0 * sh};
     float ql[4] = {0.f, 0.f, 0.f, 0.f};
     for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) ql[i] += L[i][j] * qt[j];
+        for (int j = 0; j < 4; j++) ql[i] = ff_to_float(ff_add(ff_of(ql[i]), ff_mul_f(L[i][j], qt[j])));
     float pt[4][4];
-    pt[0][0] = (pi[0] * ch * ch + 2. * pi[3] * ch * sh + pi[9] * sh * sh);
+    // 2. * pi * ch * sh is a double product in the reference; the float terms
+    // around it are rounded to float first
+    pt[0][0] = ff_to_float(ff_add(ff_add(ff_of(pi[0] * ch * ch),
+                                         ff_mul_f(ff_two_prod(2.0f * pi[3], ch), sh)),
+                                  ff_of(pi[9] * sh * sh)));
     pt[0][1] = pi[1] * ch + pi[6] * sh;
     pt[0][2] = pi[2] * ch + pi[8] * sh;
     pt[0][3] = (pi[0] * ch * sh + pi[3] * (ch * ch + sh * sh) + pi[9] * sh * ch);
@@ -188,7 +216,9 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
     pt[3][0] = pt[0][3];
     pt[3][1] = pt[1][3];
     pt[3][2] = pt[2][3];
-    pt[3][3] = (pi[0] * sh * sh + 2. * pi[3] * sh * ch + pi[9] * ch * ch);
+    pt[3][3] = ff_to_float(ff_add(ff_add(ff_of(pi[0] * sh * sh),
+                                         ff_mul_f(ff_two_prod(2.0f * pi[3], sh), ch)),
+                                  ff_of(pi[9] * ch * ch)));
     const int pi_i[5] = {1, 1, 1, 2, 2};
     const int pi_j[5] = {1, 2, 3, 2, 3};
     float pl[5];
@@ -196,7 +226,8 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
         const int i = pi_i[k], j = pi_j[k];
         float acc = 0.f;
         for (int a = 0; a < 4; a++)
-            for (int b = 0; b < 4; b++) acc += (L[i][a] * pt[a][b] * L[b][j]);
+            for (int b = 0; b < 4; b++)
+                acc = ff_to_float(ff_add(ff_of(acc), ff_mul(ff_mul_f(L[i][a], pt[a][b]), L[b][j])));
         pl[k] = acc;
     }
 
