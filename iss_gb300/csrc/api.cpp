@@ -1340,7 +1340,7 @@ iss_status autotune(iss_handle* h, double* ms_before, double* ms_after) {
     }
     // the sample phase: re-measure the incumbent with the chosen groups
     if ((st = measure(best, &by, &bs, &bt)) != ISS_OK) return st;
-    const int items[] = {32, 64, 128, 256};
+    const int items[] = {32, 64, 128, 256, 512};
     for (int it : items) {
         if (it == best.item_size) continue;
         iss_tuning_t t = best;

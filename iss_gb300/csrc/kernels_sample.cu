@@ -407,14 +407,28 @@ off_tile_scan_kernel(const int32_t* __restrict__ counts, int64_t n,
 struct Prop {
     float T, m, a, mt, Kmax, W, w32, w3, qa;
     float mut, cpoly, rmax;
-    int boson, compat, sign;
-    // flux geometry in the LRF: dsigma_mu = (d0, D n), e1 _|_ n
-    float d0, D, nx, ny, nz, e1x, e1y, e1z;
+    int compat, sign;
+    // flux geometry in the LRF: dsigma_mu = (d0, D n); e1 _|_ n is rebuilt
+    // from n and its norm einv by e1() (three registers fewer per lane)
+    float d0, D, nx, ny, nz, einv;
     float pxx, pxy, pxz, pyy, pyz, shear_c;
-    int shear_over_p0T;
     float bi0, b0, b1, b2;
     float qx, qy, qz, pq, Bq;
 };
+
+// e1 = normalised (t x n), t the coordinate axis least parallel to n: z when
+// |n_z| < 0.9, else x
+__device__ __forceinline__ void prop_e1(const Prop& p, float& ex, float& ey, float& ez) {
+    if (fabsf(p.nz) < 0.9f) {
+        ex = -p.ny * p.einv;
+        ey = p.nx * p.einv;
+        ez = 0.0f;
+    } else {
+        ex = 0.0f;
+        ey = -p.nz * p.einv;
+        ez = p.ny * p.einv;
+    }
+}
 
 struct Unit {
     int64_t slot;
@@ -449,7 +463,10 @@ __device__ __forceinline__ int cell_search(const unsigned long long* __restrict_
     return lo;
 }
 
-// returns false when m/T - mu/T is outside the reference's momentum tables
+// returns false when m/T - mu/T is outside the reference's momentum tables.
+// kLean: the configuration has neither diffusion nor the compat-fermion
+// correction (both then compile out, which frees registers in the sampler)
+template <bool kLean = false>
 __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
                            int l, Prop& p) {
     const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
@@ -471,11 +488,10 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
     p.mt = m * beta;
     p.mut = mu * beta;
     p.a = (m - mu) * beta;
-    p.boson = (sp.sign == -1);
     const int sampler = p.a < 30.0f ? 0 : (p.a < 50.0f ? 1 : 2);
     float e0, de;
     int npts;
-    if (p.boson) {
+    if (p.sign == -1) {
         e0 = (sampler == 0 ? 0.05f : (sampler == 1 ? 30.0f : 50.0f)) + 0.05f;
         de = 0.05f;
         npts = 1001;
@@ -491,12 +507,12 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
     p.w32 = 2.0f + 2.0f * p.mt;
     p.W = p.w32 + 0.5f * p.mt * p.mt;
     p.qa = -expm1f(-p.a);
-    p.compat = (cfg.compat_fermion && sampler == 0) ? 1 : 0;
+    p.compat = (!kLean && cfg.compat_fermion && sampler == 0) ? 1 : 0;
     p.cpoly = p.mut * p.mut - 0.5f * p.mt * p.mt;
     p.rmax = 1.0f;
     if (p.compat) {
         const float amu = fabsf(p.mut);
-        if (p.boson) {
+        if (p.sign == -1) {
             p.rmax = 1.0f + (p.mut < 0.0f ? 2.0f * amu * kTwoOverE10 / (p.mt * p.mt) : 0.0f);
         } else {
             const float r = 1.0f - p.mut / p.mt;
@@ -524,27 +540,18 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
         p.ny = 0.0f;
         p.nz = 1.0f;
     }
-    // e1 = normalised (t x n) with t the coordinate axis least parallel to n
-    {
-        float tx = 0.f, ty = 0.f, tz = 0.f;
-        if (fabsf(p.nz) < 0.9f) tz = 1.f; else tx = 1.f;
-        float ex = ty * p.nz - tz * p.ny, ey = tz * p.nx - tx * p.nz, ez = tx * p.ny - ty * p.nx;
-        const float inv = rsqrtf(ex * ex + ey * ey + ez * ez);
-        p.e1x = ex * inv;
-        p.e1y = ey * inv;
-        p.e1z = ez * inv;
-    }
+    // 1/|t x n| for e1 (prop_e1)
+    p.einv = fabsf(p.nz) < 0.9f ? rsqrtf(p.ny * p.ny + p.nx * p.nx) : rsqrtf(p.nz * p.nz + p.ny * p.ny);
     p.pxx = pi1.x;
     p.pxy = pi1.y;
     p.pxz = pi1.z;
     p.pyy = pi1.w;
     p.pyz = pi2.x;
     p.shear_c = 0.0f;
-    p.shear_over_p0T = 0;
     if (cfg.include_shear) {
         if (cfg.neos_kind == 1) {
+            // divided by p0 in the acceptance (try_once)
             p.shear_c = 1.0f / (2.0f * cf.z * T);
-            p.shear_over_p0T = 1;
         } else if (cfg.neos_kind == 0) {
             p.shear_c = cf.x;
         } else {
@@ -565,7 +572,7 @@ __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const 
         }
     }
     p.qx = p.qy = p.qz = p.pq = p.Bq = 0.0f;
-    if (cfg.include_diff) {
+    if (!kLean && cfg.include_diff) {
         const float ik = 1.0f / cf.w;
         p.qx = pi2.y * ik;
         p.qy = pi2.z * ik;
@@ -583,9 +590,9 @@ __device__ float compat_ratio(const Prop& p, float Et) {
     for (int n = 1; n <= 10; n++) {
         e *= q;
         S2 += e;
-        S1 += (p.boson || (n & 1)) ? e : -e;
+        S1 += ((p.sign == -1) || (n & 1)) ? e : -e;
     }
-    const float finf = p.boson ? q / (-expm1f(-Et)) : q / (1.0f + q);
+    const float finf = (p.sign == -1) ? q / (-expm1f(-Et)) : q / (1.0f + q);
     const float num = Et * Et * S2 + 2.0f * p.mut * Et * S1 + p.cpoly * finf;
     const float den = (Et * Et + 2.0f * p.mut * Et + p.cpoly) * finf;
     return num / den;
@@ -593,6 +600,7 @@ __device__ float compat_ratio(const Prop& p, float Et) {
 
 // One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
 // the uniform used for the rapidity of boost-invariant surfaces.
+template <bool kLean = false>
 __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, const Unit& u,
                                          float4& pl, float& u_rap, unsigned& violations) {
     const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagTry << 16);
@@ -610,9 +618,9 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
     const float Etil = p.a + K;
     const float em = expf(-Etil);
-    const float a_q = p.boson ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
+    const float a_q = (p.sign == -1) ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
     float a_c = 1.0f;
-    if (p.compat) {
+    if (!kLean && p.compat) {
         a_c = compat_ratio(p, Etil) / p.rmax;
         if (a_c > 1.0f) {
             violations++;
@@ -639,15 +647,17 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
     float sphi, cphi;
     sincospif(2.0f * u01f(B.y), &sphi, &cphi);
-    const float e2x = p.ny * p.e1z - p.nz * p.e1y;
-    const float e2y = p.nz * p.e1x - p.nx * p.e1z;
-    const float e2z = p.nx * p.e1y - p.ny * p.e1x;
+    float e1x, e1y, e1z;
+    prop_e1(p, e1x, e1y, e1z);
+    const float e2x = p.ny * e1z - p.nz * e1y;
+    const float e2y = p.nz * e1x - p.nx * e1z;
+    const float e2z = p.nx * e1y - p.ny * e1x;
     const float T = p.T;
     const float pm = T * ptil;
     const float p0 = T * Et;
-    const float px = pm * (cth * p.nx + sth * (cphi * p.e1x + sphi * e2x));
-    const float py = pm * (cth * p.ny + sth * (cphi * p.e1y + sphi * e2y));
-    const float pz = pm * (cth * p.nz + sth * (cphi * p.e1z + sphi * e2z));
+    const float px = pm * (cth * p.nx + sth * (cphi * e1x + sphi * e2x));
+    const float py = pm * (cth * p.ny + sth * (cphi * e1y + sphi * e2y));
+    const float pz = pm * (cth * p.nz + sth * (cphi * e1z + sphi * e2z));
     const float sgn = static_cast<float>(p.sign);
     const float f0 = em / (1.0f + sgn * em);
     const float one_m = 1.0f - sgn * f0;
@@ -656,13 +666,13 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
         const float Wf = px * px * p.pxx + 2.0f * px * py * p.pxy + 2.0f * px * pz * p.pxz +
                          py * py * p.pyy + 2.0f * py * pz * p.pyz + pz * pz * (-p.pxx - p.pyy);
         float ds = one_m * Wf * p.shear_c;
-        if (p.shear_over_p0T) ds /= p0;
+        if (cfg.neos_kind == 1) ds /= p0;
         df += ds;
     }
     if (cfg.include_bulk) {
         df += one_m * (p.bi0 / p0 + p.b0 + p.b1 * p0 + p.b2 * p0 * p0);
     }
-    if (cfg.include_diff) {
+    if (!kLean && cfg.include_diff) {
         const float qf = -(px * p.qx + py * p.qy + pz * p.qz);
         df += one_m * (p.pq - p.Bq / p0) * qf;
     }
@@ -894,7 +904,7 @@ __device__ __forceinline__ bool plain_target(const DevConfig& cfg, const Prop& p
     const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
     const float Etil = p.a + K;
     const float em = expf(-Etil);
-    const float a_q = p.boson ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
+    const float a_q = (p.sign == -1) ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
     const float a_c = p.compat ? fminf(compat_ratio(p, Etil) / p.rmax, 1.0f) : 1.0f;
     const float T = p.T;
     const float pm = T * ptil;
@@ -908,7 +918,7 @@ __device__ __forceinline__ bool plain_target(const DevConfig& cfg, const Prop& p
         const float Wf = px * px * p.pxx + 2.0f * px * py * p.pxy + 2.0f * px * pz * p.pxz +
                          py * py * p.pyy + 2.0f * py * pz * p.pyz + pz * pz * (-p.pxx - p.pyy);
         float ds = one_m * Wf * p.shear_c;
-        if (p.shear_over_p0T) ds /= p0;
+        if (cfg.neos_kind == 1) ds /= p0;
         df += ds;
     }
     if (cfg.include_bulk) df += one_m * (p.bi0 / p0 + p.b0 + p.b1 * p0 + p.b2 * p0 * p0);
@@ -1106,18 +1116,22 @@ __device__ void emit_efa(const DevConfig& cfg, const CellArrays& cells, const Pr
 template <int kAlg> struct PropOf { using type = Prop; };
 template <> struct PropOf<2> { using type = PropEfa; };
 
+template <bool kLean>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
                                           const SpeciesDev& sp, int l, Prop& p, bool) {
-    return setup_prop(cfg, cells, sp, l, p);
+    return setup_prop<kLean>(cfg, cells, sp, l, p);
 }
+template <bool kLean>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
                                           const SpeciesDev& sp, int l, PropEfa& p, bool keep_max) {
     return setup_efa(cfg, cells, sp, l, p, keep_max);
 }
+template <bool kLean>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const Prop& p, const Unit& u, float4& pl,
                                         float& u_rap, unsigned& viol) {
-    return try_once(cfg, p, u, pl, u_rap, viol);
+    return try_once<kLean>(cfg, p, u, pl, u_rap, viol);
 }
+template <bool kLean>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const PropEfa& p, const Unit& u,
                                         float4& pl, float& u_rap, unsigned& viol) {
     return try_efa(cfg, p, u, pl, u_rap, viol);
@@ -1220,8 +1234,9 @@ cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
 constexpr int kSampleThreads = 256;
 
 // kLcc: local_charge_conservation pairs (a separate instantiation, so the
-// common case carries none of the pair state)
-template <bool kLcc, bool kLearned, int kAlg>
+// common case carries none of the pair state); kLean: FSSW without diffusion
+// and without the compat-fermion correction (setup_prop)
+template <bool kLcc, bool kLearned, int kAlg, bool kLean>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
@@ -1237,14 +1252,17 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // the warp's current work item: units [next, end) of species cur_s in event cur_e
-    int64_t next = 0, end = 0, seg_base = 0;     // draws [next, end); records from seg_base
+    // draws [next, end), records from seg_base; a segment's draws are
+    // counted by an int32, so draw indices fit in an int
+    int next = 0, end = 0;
+    int64_t seg_base = 0;
     int cur_s = 0, cur_e = 0, cur_mult = 1;
     bool exhausted = false;
     bool active = false;
     Unit u;
     typename PropOf<kAlg>::type p;
-    int pid = 0;
-    unsigned long long n_tries = 0, n_redraws = 0, n_fail = 0;
+    // per-thread counts (a thread makes far fewer than 2^32 tries in a launch)
+    unsigned n_tries = 0, n_redraws = 0, n_fail = 0;
     unsigned n_viol = 0;
     unsigned n_ltries = 0, n_lviol = 0, n_lhad = 0;
 
@@ -1267,10 +1285,11 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                 const int64_t seg = static_cast<int64_t>(cur_e) * cfg.n_species + cur_s;
                 seg_base = offsets[seg];
                 cur_mult = kLcc ? records_per_draw(cfg, species[cur_s]) : 1;
-                next = j * cfg.item_size;
-                end = min(next + cfg.item_size, (offsets[seg + 1] - seg_base) / cur_mult);
+                const int64_t first = j * cfg.item_size;
+                next = static_cast<int>(first);
+                end = static_cast<int>(min(first + cfg.item_size, (offsets[seg + 1] - seg_base) / cur_mult));
             }
-            const int64_t avail = end - next;
+            const int avail = end - next;
             const int rank = __popc(need & ((1u << lane) - 1u));
             if (!active && rank < avail) {
                 const int64_t d = next + rank;
@@ -1285,10 +1304,9 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                 u.tries_cell = 0;
                 u.cell = -1;
                 u.lp = nullptr;
-                pid = pids[u.s];
                 active = true;
             }
-            next += min(static_cast<int64_t>(__popc(need)), avail);
+            next += min(__popc(need), avail);
         }
         if (__ballot_sync(FULL, active) == 0) break;
         if (active) {
@@ -1339,7 +1357,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
                                    : nullptr;
                 }
-                if (!setup_any(cfg, cells, species[u.s], l, p, false)) {
+                if (!setup_any<kLean>(cfg, cells, species[u.s], l, p, false)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     for (int q = 0; q < (kLcc ? u.mult : 1); q++)
@@ -1361,12 +1379,13 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     ok = try_once(cfg, p, u, pl, u_rap, n_viol);
                 }
             } else {
-                ok = try_any(cfg, p, u, pl, u_rap, n_viol);
+                ok = try_any<kLean>(cfg, p, u, pl, u_rap, n_viol);
             }
             u.t++;
             u.tries_cell++;
             n_tries++;
             if (ok) {
+                const int pid = pids[u.s];
                 // the final cell of a redrawn hadron (cell_of then holds every
                 // hadron's cell: the training rows of the learned proposal)
                 if (u.redraw > 0 && u.phase == 0) cell_of[u.slot] = u.cell;
@@ -1386,7 +1405,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
                     // (the lab-frame sampler keeps the hadron's maximum for
                     // its partner, src/emissionfunction.cpp:3503-3509)
-                    if (!setup_any(cfg, cells, sp2, u.cell, p, true)) {
+                    if (!setup_any<kLean>(cfg, cells, sp2, u.cell, p, true)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
                         write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
@@ -1400,9 +1419,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
         }
     }
     // warp-aggregated counters
+    unsigned long long w_tries = n_tries;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        n_tries += __shfl_down_sync(FULL, n_tries, o);
+        w_tries += __shfl_down_sync(FULL, w_tries, o);
         n_redraws += __shfl_down_sync(FULL, n_redraws, o);
         n_fail += __shfl_down_sync(FULL, n_fail, o);
         n_viol += __shfl_down_sync(FULL, n_viol, o);
@@ -1413,9 +1433,9 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
         }
     }
     if (lane == 0) {
-        atomicAdd(&ctrs->tries, n_tries);
-        if (n_redraws) atomicAdd(&ctrs->redraws, n_redraws);
-        if (n_fail) atomicAdd(&ctrs->failures, n_fail);
+        atomicAdd(&ctrs->tries, w_tries);
+        if (n_redraws) atomicAdd(&ctrs->redraws, static_cast<unsigned long long>(n_redraws));
+        if (n_fail) atomicAdd(&ctrs->failures, static_cast<unsigned long long>(n_fail));
         if (n_viol) atomicAdd(&ctrs->bound_violations, static_cast<unsigned long long>(n_viol));
         if (kLearned) {
             if (n_ltries) atomicAdd(&ctrs->learned_tries, static_cast<unsigned long long>(n_ltries));
@@ -1681,11 +1701,14 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    auto kernel = cfg.mc_sampling == 2
-                      ? (cfg.lcc ? sampler_kernel<true, false, 2> : sampler_kernel<false, false, 2>)
-                  : cfg.lpairs
-                      ? (cfg.lcc ? sampler_kernel<true, true, 4> : sampler_kernel<false, true, 4>)
-                      : (cfg.lcc ? sampler_kernel<true, false, 4> : sampler_kernel<false, false, 4>);
+    const bool lean = !cfg.include_diff && !cfg.compat_fermion;
+    auto kernel =
+        cfg.mc_sampling == 2
+            ? (cfg.lcc ? sampler_kernel<true, false, 2, false> : sampler_kernel<false, false, 2, false>)
+        : cfg.lpairs
+            ? (cfg.lcc ? sampler_kernel<true, true, 4, false> : sampler_kernel<false, true, 4, false>)
+        : lean ? (cfg.lcc ? sampler_kernel<true, false, 4, true> : sampler_kernel<false, false, 4, true>)
+               : (cfg.lcc ? sampler_kernel<true, false, 4, false> : sampler_kernel<false, false, 4, false>);
     kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters, k_end_dev);
