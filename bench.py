@@ -21,7 +21,10 @@ warm-up) and each generate of the device leg replays one captured CUDA graph
 same metric through the C ABI with the surface copied from pinned host
 memory and all hadrons read back to pinned host memory every step
 (iss_gpu_set_surface + iss_gpu_generate_into, whose device->host copies of
-finished events overlap the sampling of later ones).
+finished events overlap the sampling of later ones).  By default the e2e
+steps run on two handles from two host threads, so that one step's device
+work overlaps the other's record copy; e2e.single_handle is the same with
+one handle (--e2e-handles 1 makes it the headline).
 
 --impl reference times the CPU implementation of the path (the oracle port
 of the reference's algorithm, oracle/) on the host cores with one process per
@@ -409,6 +412,53 @@ def learned_report(s, timings, args):
     return out
 
 
+def e2e_handles(s, make_handle, n_handles, fo_pinned, out_t, steps, step_s, local):
+    """End-to-end steps through the C ABI on n_handles handles, each driven by
+    its own host thread with its own page-locked output buffer.  A handle's
+    generate_into returns once its last records are on the host; while one
+    handle's records cross the device-to-host link, another handle's surface
+    upload, yields, counts and first sampling chunk run on the device.  Thread
+    j starts j/n_handles of a step late so that the pipelines stay out of
+    phase.  Every step still uploads its surface and copies all of its
+    records to host memory inside the timed region.
+    Returns (hadrons, seconds, steps per handle)."""
+    import torch
+    from iss_gb300 import HADRON_DTYPE
+    handles = [s] + [make_handle() for _ in range(n_handles - 1)]
+    bufs = [out_t.numpy().view(HADRON_DTYPE)]
+    for h in handles[1:]:
+        b = torch.empty(out_t.numel(), dtype=torch.uint8, pin_memory=True).numpy().view(HADRON_DTYPE)
+        h.generate_into(b)      # untimed: the handle's buffers and first launches
+        bufs.append(b)
+    per = [steps // n_handles + (1 if j < steps % n_handles else 0) for j in range(n_handles)]
+    counts = [0] * n_handles
+    errors = []
+
+    def work(j):
+        try:
+            torch.cuda.set_device(local)
+            time.sleep(j * step_s / n_handles)
+            for _ in range(per[j]):
+                handles[j].set_surface(fo_pinned)
+                h, _ = handles[j].generate_into(bufs[j])
+                counts[j] += len(h)
+        except Exception as e:  # re-raised on the main thread
+            errors.append(e)
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=work, args=(j,)) for j in range(n_handles)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    if errors:
+        raise errors[0]
+    return sum(counts), sec, per
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -573,7 +623,19 @@ def run_gpu(args, ws, rank, local):
             link.append(nbytes / (ev0.elapsed_time(ev1) * 1e-3) / 1e9)
         del dev_buf
         e2e = [e_had, e_sec, e_bytes_in // args.steps, e_bytes_out // args.steps,
-               [1e3 * x / args.steps for x in parts], max(link)]
+               [1e3 * x / args.steps for x in parts], max(link), None]
+        if args.e2e_handles > 1 and learned is None:
+            def make_handle():
+                h2 = iSS(".", inputfile="")
+                h2.set_params(**params)
+                h2.set_tuning(**s.get_tuning())
+                h2.set_surface(fo_pinned)
+                h2.set_random_seed(20261204)
+                return h2
+            barrier()
+            e2e[6] = e2e_handles(s, make_handle, args.e2e_handles, fo_pinned, out_t, args.steps,
+                                 e_sec / args.steps, local)
+            barrier()
 
     if learned is not None:
         learned.update(learned_report(s, timings, args))
@@ -588,7 +650,8 @@ def run_gpu(args, ws, rank, local):
     sec = sum(dev_ms) / 1e3
     local_stats = [sum(hadrons), sec, sum(t_sample) / 1e3, sum(t_yields) / 1e3]
     if e2e:
-        local_stats += [e2e[0], e2e[1]]
+        # the headline e2e: two handles when that leg ran, else the single handle
+        local_stats += [e2e[6][0], e2e[6][1]] if e2e[6] else [e2e[0], e2e[1]]
     if ws > 1:
         import torch.distributed as dist
         v = torch.tensor(local_stats, dtype=torch.float64, device="cuda")
@@ -600,7 +663,7 @@ def run_gpu(args, ws, rank, local):
         e2e_h, e2e_sec = (tot[4].item(), mx[5].item()) if e2e else (0, 1)
     else:
         all_h, max_sec = local_stats[0], local_stats[1]
-        e2e_h, e2e_sec = (e2e[0], e2e[1]) if e2e else (0, 1)
+        e2e_h, e2e_sec = (local_stats[4], local_stats[5]) if e2e else (0, 1)
 
     if rank == 0:
         value = all_h / max_sec
@@ -651,8 +714,12 @@ def run_gpu(args, ws, rank, local):
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": ({"value": e2e_h / e2e_sec, "unit": UNIT,
                          "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3],
-                         "host_ms_per_step": {"set_surface": e2e[4][0],
-                                              "generate_into": e2e[4][1]},
+                         "handles": args.e2e_handles if e2e[6] else 1,
+                         "ms_per_step": 1e3 * e2e_sec / args.steps,
+                         "single_handle": {"value": e2e[0] / e2e[1],
+                                           "ms_per_step": 1e3 * e2e[1] / args.steps,
+                                           "host_ms_per_step": {"set_surface": e2e[4][0],
+                                                                "generate_into": e2e[4][1]}},
                          "d2h_link_gbs": e2e[5]}
                         if e2e else None),
                 "gpu_launches": launches, "clocks": clk,
@@ -701,6 +768,9 @@ def main():
     ap.add_argument("--cpu-cells", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-handles", type=int, choices=[1, 2, 3, 4], default=2,
+                    help="handles of the end-to-end leg, each driven by its own host thread, so "
+                         "that one step's device work overlaps another's record copy")
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the per-species yields against the FP64 CPU oracle")
     ap.add_argument("--decays", action="store_true",
