@@ -109,6 +109,7 @@ struct iss_handle {
     DevBuf<float4> d_milne;          // MC_sampling = 2: regulated Milne cells, 6 float4 each
     DevBuf<SpeciesDev> d_species;
     DevBuf<int32_t> d_pids;
+    DevBuf<int32_t> d_yorder;        // yields kernel: species grouped by identical series
     DevBuf<float> d_yields;
     DevBuf<unsigned long long> d_cdf, d_tile_sum, d_tile_off, d_qtot;
     DevBuf<double> d_totals;
@@ -167,6 +168,7 @@ struct iss_handle {
             d_milne.release();
             d_species.release();
             d_pids.release();
+            d_yorder.release();
             DevBuf<double>* db[] = {&d_totals, &d_b14c0, &d_b14c1, &d_b14c2, &d_ce, &d_qmu,
                                     &d_logfact, &d_pois};
             for (auto* b : db) b->release();
@@ -230,6 +232,45 @@ iss_status fail(iss_handle* h, iss_status st, const char* fmt, ...) {
         if (_e != cudaSuccess)                                                              \
             return fail((h), ISS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(_e)); \
     } while (0)
+
+// Species groups of the yields kernel.  The thermal series of
+// calculate_dN_analytic (src/FSSW.cpp:719-848) depends on a species only
+// through its mass, statistics, number of terms and chemical potential, so
+// species that agree in the first three share one series per cell (isospin
+// partners, particles and antiparticles).  Layout: G + 1 group starts into
+// the member list, then the members (species indices, each species once).
+// Groups are ordered by decreasing work (series terms, then members), so
+// that the kernel's interleaving of groups over grid rows stays balanced.
+std::vector<int32_t> yield_group_order(const std::vector<SpeciesDev>& sd) {
+    std::vector<std::vector<int32_t>> groups;
+    for (size_t k = 0; k < sd.size(); k++) {
+        const SpeciesDev& a = sd[k];
+        bool placed = false;
+        for (auto& g : groups) {
+            const SpeciesDev& b = sd[g[0]];
+            if (a.m_hi == b.m_hi && a.m_lo == b.m_lo && a.sign == b.sign && a.light == b.light) {
+                g.push_back(static_cast<int32_t>(k));
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) groups.push_back({static_cast<int32_t>(k)});
+    }
+    auto cost = [&](const std::vector<int32_t>& g) {
+        return (sd[g[0]].light ? 20 : 2) + static_cast<int>(g.size());
+    };
+    std::stable_sort(groups.begin(), groups.end(),
+                     [&](const auto& x, const auto& y) { return cost(x) > cost(y); });
+    std::vector<int32_t> out;
+    int32_t start = 0;
+    for (const auto& g : groups) {
+        out.push_back(start);
+        start += static_cast<int32_t>(g.size());
+    }
+    out.push_back(start);
+    for (const auto& g : groups) out.insert(out.end(), g.begin(), g.end());
+    return out;
+}
 
 iss_status ensure_cuda(iss_handle* h) {
     if (h->cuda_ready) return ISS_OK;
@@ -513,12 +554,22 @@ iss_status prepare(iss_handle* h) {
         sd[k].sign = s.sign;
         pids[k] = s.pid;
     }
+    // species whose thermal series are the same function of the cell
+    // (same float-float mass, statistics and number of terms) form one group
+    // of the yields kernel; the series runs once per group and cell whenever
+    // the members' chemical potentials agree in that cell
+    const std::vector<int32_t> yorder = yield_group_order(sd);
+    c.n_ygroups = static_cast<int>(yorder.size() - sd.size()) - 1;
     CUDA_TRY(h, h->d_species.reserve(sd.size()));
     CUDA_TRY(h, h->d_pids.reserve(sd.size()));
+    CUDA_TRY(h, h->d_yorder.reserve(yorder.size()));
+    c.yorder = h->d_yorder.ptr;
     if (!sd.empty()) {
         CUDA_TRY(h, cudaMemcpyAsync(h->d_species.ptr, sd.data(), sizeof(SpeciesDev) * sd.size(),
                                     cudaMemcpyHostToDevice, h->stream));
         CUDA_TRY(h, cudaMemcpyAsync(h->d_pids.ptr, pids.data(), 4 * pids.size(),
+                                    cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_yorder.ptr, yorder.data(), 4 * yorder.size(),
                                     cudaMemcpyHostToDevice, h->stream));
     }
     h->cfg = c;

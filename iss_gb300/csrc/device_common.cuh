@@ -70,6 +70,10 @@ struct DevConfig {
     // launch shape (results do not depend on it; the autotuner picks it)
     int item_size;       // draws per sampler work item (multiple of 32, <= 1024)
     int yield_groups;    // species groups per cell in the yields kernel (grid y)
+    // yields kernel: n_ygroups + 1 group starts, then the species of each
+    // group (species with the same thermal series, yield_group_order)
+    const int32_t* yorder;
+    int n_ygroups;
     int sampler_ctas;    // sampler CTAs per SM (1..3)
     int assign_bps;      // cell-assignment blocks per SM
     // graph replays: (key0, key1, event_offset) of the call in device memory,

@@ -95,14 +95,177 @@ __device__ __forceinline__ GridPos grid_pos(float xh, float xl) {
 constexpr int kYieldThreads = 128;
 constexpr int kYieldGroups = 4;   // species groups per cell (grid y)
 
-// Yields of species k0, k0 + kstep, ... in cell l (not dropped: u.dsigma >= 0).
+// Per-cell quantities shared by every species' yield in cell l.
+struct CellYieldIn {
+    float T, b_hi, b_lo;
+    bool warm, with_bulk, kind_ce, kind_14;
+    int bulk_kind;
+    float bulkPi, dsq, pref_q, inv_kappa, unit_pref;
+    float4 th, th2, cf;
+};
+
+// Sums of the thermal series (calculate_dN_analytic, src/FSSW.cpp:719-848) of
+// one species in one cell: they depend on the species only through its
+// float-float mass, statistics, number of terms and chemical potential mu.
+struct SeriesSums {
+    float Neq, b1, b2, b3, q1, q2;
+};
+
+__device__ __forceinline__ float species_mu(const SpeciesDev& sp, const float4& th) {
+    return static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
+           static_cast<float>(sp.charge) * th.w;
+}
+
+template <bool kDiff>
+__device__ __forceinline__ SeriesSums thermal_series(const DevConfig& cfg, const CellYieldIn& c,
+                                                     const SpeciesDev& sp, float mu) {
+    const float b_hi = c.b_hi, b_lo = c.b_lo;
+    const bool warm = c.warm, with_bulk = c.with_bulk;
+    constexpr bool with_diff = kDiff;
+    const bool kind_ce = c.kind_ce, kind_14 = c.kind_14;
+    // beta*mu and m*beta as float-float numbers
+    float bm_h, bm_e;
+    two_prod(mu, b_hi, bm_h, bm_e);
+    const float bm_l = fmaf(mu, b_lo, bm_e);
+    float x1_h, x1_e;
+    two_prod(sp.m_hi, b_hi, x1_h, x1_e);
+    const float x1_l = x1_e + fmaf(sp.m_hi, b_lo, sp.m_lo * b_hi);
+    const int nmax = (sp.light && warm) ? 10 : 1;
+    float Neq = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f, q1 = 0.f, q2 = 0.f;
+    const float mbeta = x1_h + x1_l;
+    for (int nn = 1; nn <= nmax; nn++) {
+        const float fn = static_cast<float>(nn);
+        float theta = 1.0f;
+        if (sp.sign == 1 && (nn % 2 == 0)) theta = -1.0f;
+        if (sp.sign == 0 && nn > 1) theta = 0.0f;
+        // x_n = n m beta
+        float xh, xe;
+        two_prod(fn, x1_h, xh, xe);
+        const float xl = fmaf(fn, x1_l, xe);
+        // lambda^n = exp(n beta mu)
+        float ah, ae;
+        two_prod(fn, bm_h, ah, ae);
+        const float al = fmaf(fn, bm_l, ae);
+        const float fug = expf(ah) * (1.0f + al);
+        const GridPos g = grid_pos(xh, xl);
+        float K1, K2, K3;
+        if (g.on_table) {
+            const float4 ka = __ldg(cfg.tab.sfK + g.idx);
+            const float4 kb = __ldg(cfg.tab.sfK + g.idx + 1);
+            K1 = fmaf(g.frac, kb.x - ka.x, ka.x);
+            K2 = fmaf(g.frac, kb.y - ka.y, ka.y);
+            K3 = fmaf(g.frac, kb.z - ka.z, ka.z);
+        } else {
+            const double xd = static_cast<double>(xh) + static_cast<double>(xl);
+            K2 = static_cast<float>(bessel_k_direct(2, xd));
+            K1 = with_bulk ? static_cast<float>(bessel_k_direct(1, xd)) : 0.0f;
+            K3 = (with_bulk && kind_14) ? static_cast<float>(bessel_k_direct(3, xd)) : 0.0f;
+        }
+        const float tf = theta * fug;
+        Neq = fmaf(tf / fn, K2, Neq);
+        if (with_bulk) {
+            if (kind_ce) {
+                b1 = fmaf(tf, fmaf(mbeta, K1, 3.0f * K2 / fn), b1);
+                b2 = fmaf(tf, K1, b2);
+            } else if (kind_14) {
+                b1 = fmaf(tf, K2, b1);
+                b2 = fmaf(tf, fmaf(mbeta, K1, 3.0f * K2 / fn), b2);
+                b3 = fmaf(tf, fmaf(mbeta, K2, 3.0f * K3 / fn), b3);
+            }
+        }
+        if (with_diff) {
+            q1 = fmaf(tf / fn, K2, q1);
+            float En[9];
+            if (g.on_table) {
+                const float* ea = cfg.tab.sfE + 9 * g.idx;
+#pragma unroll
+                for (int i = 0; i < 9; i++) {
+                    const float a = __ldg(ea + i), b = __ldg(ea + 9 + i);
+                    En[i] = fmaf(g.frac, b - a, a);
+                }
+            } else {
+                const double xd = static_cast<double>(xh) + static_cast<double>(xl);
+                En[0] = static_cast<float>(expint_direct(2, xd));
+                for (int i = 1; i < 9; i++) En[i] = static_cast<float>(expint_direct(2 * i + 2, xd));
+            }
+            const float arg = xh;
+            const float em = expf(-xh) * (1.0f - xl);
+            float I = em / arg * (2.0f / (arg * arg) + 2.0f / arg - 0.5f) + 0.375f * En[0];
+            // 3 (2k-5)!! / (2^k k!) for k = 3..10
+            const float ck[8] = {0.0625f, 0.0234375f, 0.01171875f, 0.0068359375f,
+                                 0.00439453125f, 0.0030212402343750f,
+                                 0.0021820068359375f, 0.0016365051269531f};
+#pragma unroll
+            for (int k2 = 0; k2 < 8; k2++) I = fmaf(ck[k2], En[k2 + 1], I);
+            I = -(mbeta * mbeta * mbeta) * I;
+            q2 = fmaf(fn * tf, I, q2);
+        }
+    }
+    return SeriesSums{Neq, b1, b2, b3, q1, q2};
+}
+
+// The yield of species sp in cell l from its series sums: the prefactor,
+// the bulk and diffusion terms and the clip at zero of
+// calculate_dN_dxtdy_for_one_particle_species (src/FSSW.cpp:565-715).
+template <bool kDiff>
+__device__ __forceinline__ float assemble_yield(const CellYieldIn& c, const SpeciesDev& sp,
+                                                const SeriesSums& ss, float4 da) {
+    const float T = c.T;
+    const float4 cf = c.cf;
+    const bool with_bulk = c.with_bulk, kind_ce = c.kind_ce;
+    constexpr bool with_diff = kDiff;
+    const int bulk_kind = c.bulk_kind;
+    const float bulkPi = c.bulkPi, dsq = c.dsq, pref_q = c.pref_q, inv_kappa = c.inv_kappa;
+    const float unit_pref = c.unit_pref;
+    const float mass = sp.m_hi + sp.m_lo;
+    const float Neq = ss.Neq, b1 = ss.b1, b2 = ss.b2, b3 = ss.b3, q1 = ss.q1, q2 = ss.q2;
+    const float m2 = mass * mass;
+    const float ug = unit_pref * sp.degen;
+    const float pref = ug * da.x;
+    float total = pref * (m2 * T * Neq);
+    if (with_bulk) {
+        if (kind_ce) {
+            // Chapman-Enskog form, bulk_deltaf_kind 1 and 21
+            const float r1 = m2 * T * b1;
+            const float r2 = m2 * mass / 3.0f * b2;
+            total += pref * (-bulkPi * cf.x) * (-cf.y * r1 + r2);
+        } else if (bulk_kind == 11) {
+            const float r1 = m2 * T * b1;
+            const float r2 = m2 * T * T * b2;
+            const float r3 = m2 * mass * T * T * b3;
+            total += pref * bulkPi *
+                     (r1 * m2 * cf.x + r2 * static_cast<float>(sp.baryon) * cf.y + r3 * cf.z);
+        }
+    }
+    if (with_diff) {
+        const float r4 = m2 * T * T * q1;
+        const float r5 = (T * T * T / 3.0f) * q2;
+        total += ug * dsq * inv_kappa * (-pref_q * r4 - static_cast<float>(sp.baryon) * r5);
+    }
+    // negative -> 0 (FSSW::calculate_dN_dxtdy_for_one_particle_species,
+    // src/FSSW.cpp:707); NaN -> 0; +inf -> FLT_MAX so the cell CDF stays
+    // finite; -0 -> +0 so the bits order as the values
+    const float yv = __uint_as_float(
+        __float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
+    return yv;
+}
+
+// Yields of the species groups k0, k0 + kstep, ... in cell l (not dropped:
+// u.dsigma >= 0).  A group's series runs for its first member and is reused
+// by the next members while their chemical potential in this cell has the
+// same bits (the same inputs, so the same sums); a member with another mu
+// gets its own series.
+template <bool kDiff>
 __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArrays& cells,
-                                            const SpeciesDev* s_sp, int nsp, int k0, int kstep,
+                                            const SpeciesDev* s_sp, const int32_t* s_gst,
+                                            const int32_t* s_mem, int n_groups, int k0, int kstep,
                                             int64_t n, int64_t l, float4 da,
                                             float* __restrict__ yields) {
-    const float4 th = cells.th[l];
-    const float4 th2 = cells.th2[l];
-    const float4 cf = cells.coef[l];
+    CellYieldIn c;
+    c.th = cells.th[l];
+    c.th2 = cells.th2[l];
+    c.cf = cells.coef[l];
+    const float4 th = c.th, th2 = c.th2, cf = c.cf;
     const float T = th.x;
     const double beta_d = 1.0 / static_cast<double>(T);
     const float b_hi = static_cast<float>(beta_d);
@@ -110,7 +273,7 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
     const bool warm = static_cast<double>(T) > 0.05;
     const int bulk_kind = cfg.bulk_kind;
     const bool with_bulk = cfg.include_bulk != 0;
-    const bool with_diff = cfg.include_diff != 0;
+    constexpr bool with_diff = kDiff;
     const bool kind_ce = (bulk_kind == 1 || bulk_kind == 21);
     const bool kind_14 = (bulk_kind == 11 || bulk_kind == 20);
     float bulkPi = 0.0f;
@@ -127,140 +290,64 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
     const float unit_pref = (1.0f / (0.197327053f * 0.197327053f * 0.197327053f)) /
                             (2.0f * 9.8696044010893586f);
 
-    for (int k = k0; k < nsp; k += kstep) {
-        const SpeciesDev sp = s_sp[k];
-        const float mass = sp.m_hi + sp.m_lo;
-        const float mu = static_cast<float>(sp.baryon) * th.y + static_cast<float>(sp.strange) * th.z +
-                         static_cast<float>(sp.charge) * th.w;
-        // beta*mu and m*beta as float-float numbers
-        float bm_h, bm_e;
-        two_prod(mu, b_hi, bm_h, bm_e);
-        const float bm_l = fmaf(mu, b_lo, bm_e);
-        float x1_h, x1_e;
-        two_prod(sp.m_hi, b_hi, x1_h, x1_e);
-        const float x1_l = x1_e + fmaf(sp.m_hi, b_lo, sp.m_lo * b_hi);
-        const int nmax = (sp.light && warm) ? 10 : 1;
-        float Neq = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f, q1 = 0.f, q2 = 0.f;
-        const float mbeta = x1_h + x1_l;
-        for (int nn = 1; nn <= nmax; nn++) {
-            const float fn = static_cast<float>(nn);
-            float theta = 1.0f;
-            if (sp.sign == 1 && (nn % 2 == 0)) theta = -1.0f;
-            if (sp.sign == 0 && nn > 1) theta = 0.0f;
-            // x_n = n m beta
-            float xh, xe;
-            two_prod(fn, x1_h, xh, xe);
-            const float xl = fmaf(fn, x1_l, xe);
-            // lambda^n = exp(n beta mu)
-            float ah, ae;
-            two_prod(fn, bm_h, ah, ae);
-            const float al = fmaf(fn, bm_l, ae);
-            const float fug = expf(ah) * (1.0f + al);
-            const GridPos g = grid_pos(xh, xl);
-            float K1, K2, K3;
-            if (g.on_table) {
-                const float4 ka = __ldg(cfg.tab.sfK + g.idx);
-                const float4 kb = __ldg(cfg.tab.sfK + g.idx + 1);
-                K1 = fmaf(g.frac, kb.x - ka.x, ka.x);
-                K2 = fmaf(g.frac, kb.y - ka.y, ka.y);
-                K3 = fmaf(g.frac, kb.z - ka.z, ka.z);
-            } else {
-                const double xd = static_cast<double>(xh) + static_cast<double>(xl);
-                K2 = static_cast<float>(bessel_k_direct(2, xd));
-                K1 = with_bulk ? static_cast<float>(bessel_k_direct(1, xd)) : 0.0f;
-                K3 = (with_bulk && kind_14) ? static_cast<float>(bessel_k_direct(3, xd)) : 0.0f;
+    c.T = T;
+    c.b_hi = b_hi;
+    c.b_lo = b_lo;
+    c.warm = warm;
+    c.with_bulk = with_bulk;
+    c.kind_ce = kind_ce;
+    c.kind_14 = kind_14;
+    c.bulk_kind = bulk_kind;
+    c.bulkPi = bulkPi;
+    c.dsq = dsq;
+    c.pref_q = pref_q;
+    c.inv_kappa = inv_kappa;
+    c.unit_pref = unit_pref;
+    for (int j = k0; j < n_groups; j += kstep) {
+        const int a = s_gst[j], b = s_gst[j + 1];
+        SeriesSums ss{};
+        uint32_t mu_bits = 0;
+        for (int t = a; t < b; t++) {
+            const int k = s_mem[t];
+            const SpeciesDev sp = s_sp[k];
+            const float mu = species_mu(sp, th);
+            if (t == a || __float_as_uint(mu) != mu_bits) {
+                ss = thermal_series<kDiff>(cfg, c, sp, mu);
+                mu_bits = __float_as_uint(mu);
             }
-            const float tf = theta * fug;
-            Neq = fmaf(tf / fn, K2, Neq);
-            if (with_bulk) {
-                if (kind_ce) {
-                    b1 = fmaf(tf, fmaf(mbeta, K1, 3.0f * K2 / fn), b1);
-                    b2 = fmaf(tf, K1, b2);
-                } else if (kind_14) {
-                    b1 = fmaf(tf, K2, b1);
-                    b2 = fmaf(tf, fmaf(mbeta, K1, 3.0f * K2 / fn), b2);
-                    b3 = fmaf(tf, fmaf(mbeta, K2, 3.0f * K3 / fn), b3);
-                }
-            }
-            if (with_diff) {
-                q1 = fmaf(tf / fn, K2, q1);
-                float En[9];
-                if (g.on_table) {
-                    const float* ea = cfg.tab.sfE + 9 * g.idx;
-#pragma unroll
-                    for (int i = 0; i < 9; i++) {
-                        const float a = __ldg(ea + i), b = __ldg(ea + 9 + i);
-                        En[i] = fmaf(g.frac, b - a, a);
-                    }
-                } else {
-                    const double xd = static_cast<double>(xh) + static_cast<double>(xl);
-                    En[0] = static_cast<float>(expint_direct(2, xd));
-                    for (int i = 1; i < 9; i++) En[i] = static_cast<float>(expint_direct(2 * i + 2, xd));
-                }
-                const float arg = xh;
-                const float em = expf(-xh) * (1.0f - xl);
-                float I = em / arg * (2.0f / (arg * arg) + 2.0f / arg - 0.5f) + 0.375f * En[0];
-                // 3 (2k-5)!! / (2^k k!) for k = 3..10
-                const float ck[8] = {0.0625f, 0.0234375f, 0.01171875f, 0.0068359375f,
-                                     0.00439453125f, 0.0030212402343750f,
-                                     0.0021820068359375f, 0.0016365051269531f};
-#pragma unroll
-                for (int k2 = 0; k2 < 8; k2++) I = fmaf(ck[k2], En[k2 + 1], I);
-                I = -(mbeta * mbeta * mbeta) * I;
-                q2 = fmaf(fn * tf, I, q2);
-            }
+            yields[static_cast<int64_t>(k) * n + l] = assemble_yield<kDiff>(c, sp, ss, da);
         }
-        const float m2 = mass * mass;
-        const float ug = unit_pref * sp.degen;
-        const float pref = ug * da.x;
-        float total = pref * (m2 * T * Neq);
-        if (with_bulk) {
-            if (kind_ce) {
-                // Chapman-Enskog form, bulk_deltaf_kind 1 and 21
-                const float r1 = m2 * T * b1;
-                const float r2 = m2 * mass / 3.0f * b2;
-                total += pref * (-bulkPi * cf.x) * (-cf.y * r1 + r2);
-            } else if (bulk_kind == 11) {
-                const float r1 = m2 * T * b1;
-                const float r2 = m2 * T * T * b2;
-                const float r3 = m2 * mass * T * T * b3;
-                total += pref * bulkPi *
-                         (r1 * m2 * cf.x + r2 * static_cast<float>(sp.baryon) * cf.y + r3 * cf.z);
-            }
-        }
-        if (with_diff) {
-            const float r4 = m2 * T * T * q1;
-            const float r5 = (T * T * T / 3.0f) * q2;
-            total += ug * dsq * inv_kappa * (-pref_q * r4 - static_cast<float>(sp.baryon) * r5);
-        }
-        // negative -> 0 (FSSW::calculate_dN_dxtdy_for_one_particle_species,
-        // src/FSSW.cpp:707); NaN -> 0; +inf -> FLT_MAX so the cell CDF stays
-        // finite; -0 -> +0 so the bits order as the values
-        const float yv = __uint_as_float(
-            __float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
-        yields[static_cast<int64_t>(k) * n + l] = yv;
     }
 }
 
+// kDiff: include_deltaf_diffusion (a separate instantiation, so the common
+// case carries none of the diffusion series' registers)
+template <bool kDiff>
 __global__ void __launch_bounds__(kYieldThreads)
 yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
               float* __restrict__ yields) {
     extern __shared__ SpeciesDev s_sp[];
     const int nsp = cfg.n_species;
+    const int G = cfg.n_ygroups;
+    int32_t* s_gst = reinterpret_cast<int32_t*>(s_sp + nsp);
+    int32_t* s_mem = s_gst + G + 1;
     for (int k = threadIdx.x; k < nsp; k += blockDim.x) s_sp[k] = species[k];
+    for (int k = threadIdx.x; k < G + 1 + nsp; k += blockDim.x) s_gst[k] = cfg.yorder[k];
     __syncthreads();
     const int64_t n = cfg.n_cells;
     const int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    // blockIdx.y picks every gridDim.y-th species: the light species (ten
-    // series terms each) come first in mass order, so interleaving keeps the
-    // groups' work equal, and the grid has several waves of blocks
+    // blockIdx.y picks every gridDim.y-th species group: the groups come in
+    // decreasing order of work, so interleaving keeps the rows' work equal,
+    // and the grid has several waves of blocks
     const int k0 = blockIdx.y, kstep = gridDim.y;
     if (l < n) {
         const float4 da = cells.da[l];
         if (da.x < 0.0f) {
-            for (int k = k0; k < nsp; k += kstep) yields[static_cast<int64_t>(k) * n + l] = 0.0f;
+            for (int j = k0; j < G; j += kstep)
+                for (int t = s_gst[j]; t < s_gst[j + 1]; t++)
+                    yields[static_cast<int64_t>(s_mem[t]) * n + l] = 0.0f;
         } else {
-            cell_yields(cfg, cells, s_sp, nsp, k0, kstep, n, l, da, yields);
+            cell_yields<kDiff>(cfg, cells, s_sp, s_gst, s_mem, G, k0, kstep, n, l, da, yields);
         }
     }
 }
@@ -521,16 +608,17 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
                           float* yields, cudaStream_t stream) {
     if (cfg.n_cells <= 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>((cfg.n_cells + kYieldThreads - 1) / kYieldThreads);
-    const size_t smem = sizeof(SpeciesDev) * static_cast<size_t>(cfg.n_species);
+    const size_t smem = sizeof(SpeciesDev) * static_cast<size_t>(cfg.n_species) +
+                        sizeof(int32_t) * static_cast<size_t>(cfg.n_ygroups + 1 + cfg.n_species);
+    auto kernel = cfg.include_diff ? yields_kernel<true> : yields_kernel<false>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(yields_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
     const int want = cfg.yield_groups > 0 ? cfg.yield_groups : kYieldGroups;
-    const unsigned groups = static_cast<unsigned>(std::max(1, std::min(want, cfg.n_species)));
-    yields_kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
+    const unsigned groups = static_cast<unsigned>(std::max(1, std::min(want, cfg.n_ygroups)));
+    kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
     return cudaGetLastError();
 }
 

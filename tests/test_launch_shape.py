@@ -119,3 +119,46 @@ def test_graph_replay_matches_eager():
     assert len(a[0]) > 1.5 * len(run(handle(surf, number_of_repeated_sampling=80), 9)[0])
     assert a[0].tobytes() == b[0].tobytes()
     assert np.array_equal(a[2], b[2])
+
+
+@pytest.mark.gpu
+def test_two_handles_on_two_threads_match_sequential_runs():
+    """Two handles driven concurrently from two host threads (each with its
+    own output buffer, both calling generate_into in turn, as bench.py's
+    e2e leg does) give every step's hadrons bit for bit as one handle
+    sampling the same seeds alone."""
+    import threading
+
+    import torch
+    surf = S.viscous_3d(30000, seed=2)
+    seeds = [[21, 23, 25], [22, 24, 26]]
+    ref = {}
+    solo = handle(surf)
+    for sd in sum(seeds, []):
+        had, off, _ = run(solo, sd)
+        ref[sd] = (had, off)
+    cap = max(len(h) for h, _ in ref.values()) + 1000
+    handles = [handle(surf), handle(surf)]
+    got = {}
+    errors = []
+
+    def work(j):
+        try:
+            torch.cuda.set_device(0)
+            out = np.zeros(cap, dtype=ref[21][0].dtype)
+            for sd in seeds[j]:
+                handles[j].set_random_seed(sd)
+                h, off = handles[j].generate_into(out)
+                got[sd] = (h.copy(), off.copy())
+        except Exception as e:
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(j,)) for j in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for sd, (had, off) in ref.items():
+        assert got[sd][0].tobytes() == had.tobytes(), sd
+        assert np.array_equal(got[sd][1], off), sd
