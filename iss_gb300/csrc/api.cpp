@@ -621,7 +621,7 @@ iss_status run_cells(iss_handle* h) {
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvStart], st));
     CUDA_TRY(h, launch_cell_prologue(c, h->d_fo34.ptr, n, cells, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvPrologue], st));
-    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, st));
+    CUDA_TRY(h, launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, h->d_ymax.ptr, st));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvYields], st));
     CUDA_TRY(h, launch_cdf(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S,
                            h->d_ymax.ptr, h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr,
@@ -944,7 +944,7 @@ cudaError_t enqueue_generate(iss_handle* h, const DevConfig& c) {
     record(h, kEvStart, true);
     GTRY(launch_cell_prologue(c, h->d_fo34.ptr, n, cells, s));
     record(h, kEvPrologue, true);
-    GTRY(launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, s));
+    GTRY(launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, h->d_ymax.ptr, s));
     record(h, kEvYields, true);
     GTRY(launch_cdf(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S, h->d_ymax.ptr,
                     h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,

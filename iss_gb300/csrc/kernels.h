@@ -11,12 +11,15 @@ namespace iss {
 // kernels_cells.cu
 cudaError_t launch_cell_prologue(const DevConfig& cfg, const float* fo34, int64_t n,
                                  const CellArrays& cells, cudaStream_t stream);
+// per-cell yields [species][cell] and, in ymax (n_surf * S rows, zeroed
+// here first), the largest yield of every (surface, species) row as float bits
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, cudaStream_t stream);
+                          float* yields, uint32_t* ymax, cudaStream_t stream);
 int cdf_num_tiles(int64_t n);
 // Fixed-point cell CDF (cdf_quantize) of every (surface, species) row of a
-// batch; four launches over n_tiles = sum over surfaces of S * nt tiles
-// (row maxima, tile sums, tile offsets, scan).  Row (b, k) of the CDF holds
+// batch from the yields and their row maxima (launch_yields); three launches
+// over n_tiles = sum over surfaces of S * nt tiles (tile sums, tile offsets,
+// scan).  Row (b, k) of the CDF holds
 // n_b + 1 entries C[0..n_b] at surf[b].cdf_base + k (n_b + 1); its guide
 // table 2^g_b + 1 entries at surf[b].guide_base + k (2^g_b + 1).  ymax,
 // qtot and totals hold n_surf * S rows.  surf is a device array.

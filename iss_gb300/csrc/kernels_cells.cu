@@ -95,6 +95,16 @@ __device__ __forceinline__ GridPos grid_pos(float xh, float xl) {
 constexpr int kYieldThreads = 128;
 constexpr int kYieldGroups = 4;   // species groups per cell (grid y)
 
+// Surface of cell l in a batch: the last b with surf[b].c0 <= l.
+__device__ __forceinline__ int surface_of(const SurfSeg* __restrict__ surf, int n_surf, int64_t l) {
+    int lo = 0, hi = n_surf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (surf[mid].c0 <= l) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Per-cell quantities shared by every species' yield in cell l.
 struct CellYieldIn {
     float T, b_hi, b_lo;
@@ -259,12 +269,14 @@ template <bool kDiff>
 __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArrays& cells,
                                             const SpeciesDev* s_sp, const int32_t* s_gst,
                                             const int32_t* s_mem, int n_groups, int k0, int kstep,
-                                            int64_t n, int64_t l, float4 da,
+                                            int64_t n, int64_t l, float4 da, bool valid, bool live,
+                                            uint32_t* s_max, uint32_t* __restrict__ ymax_row,
                                             float* __restrict__ yields) {
     CellYieldIn c;
-    c.th = cells.th[l];
-    c.th2 = cells.th2[l];
-    c.cf = cells.coef[l];
+    const int64_t lc = valid ? l : 0;   // lanes past the last cell read cell 0 and store nothing
+    c.th = cells.th[lc];
+    c.th2 = cells.th2[lc];
+    c.cf = cells.coef[lc];
     const float4 th = c.th, th2 = c.th2, cf = c.cf;
     const float T = th.x;
     const double beta_d = 1.0 / static_cast<double>(T);
@@ -281,7 +293,7 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
                                 ? th2.w : th2.w / kHbarCf;
     float dsq = 0.0f, pref_q = 0.0f, inv_kappa = 0.0f;
     if (with_diff) {
-        const float4 p2 = cells.pi2[l];
+        const float4 p2 = cells.pi2[lc];
         dsq = p2.y * da.y + p2.z * da.z + p2.w * da.w;
         pref_q = th2.z / (th2.x + th2.y);
         inv_kappa = 1.0f / cf.w;
@@ -310,45 +322,73 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
         for (int t = a; t < b; t++) {
             const int k = s_mem[t];
             const SpeciesDev sp = s_sp[k];
-            const float mu = species_mu(sp, th);
-            if (t == a || __float_as_uint(mu) != mu_bits) {
-                ss = thermal_series<kDiff>(cfg, c, sp, mu);
-                mu_bits = __float_as_uint(mu);
+            float yv = 0.0f;
+            if (live) {
+                const float mu = species_mu(sp, th);
+                if (t == a || __float_as_uint(mu) != mu_bits) {
+                    ss = thermal_series<kDiff>(cfg, c, sp, mu);
+                    mu_bits = __float_as_uint(mu);
+                }
+                yv = assemble_yield<kDiff>(c, sp, ss, da);
             }
-            yields[static_cast<int64_t>(k) * n + l] = assemble_yield<kDiff>(c, sp, ss, da);
+            if (valid) yields[static_cast<int64_t>(k) * n + l] = yv;
+            // the species' largest yield (its float bits: yields are >= +0,
+            // so the unsigned order of the bits is the order of the values)
+            const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(yv));
+            if ((threadIdx.x & 31) == 0 && m) {
+                if (s_max) atomicMax(s_max + k, m);
+                else atomicMax(ymax_row + k, m);
+            }
         }
     }
 }
 
 // kDiff: include_deltaf_diffusion (a separate instantiation, so the common
-// case carries none of the diffusion series' registers)
+// case carries none of the diffusion series' registers).  Besides the
+// yields, the kernel raises ymax[b S + k] to the largest yield of species k
+// on surface b (as float bits; ymax starts at 0): through a per-block
+// maximum in shared memory when the block's cells lie on one surface, else
+// lane by lane.
 template <bool kDiff>
 __global__ void __launch_bounds__(kYieldThreads)
 yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
-              float* __restrict__ yields) {
+              float* __restrict__ yields, uint32_t* __restrict__ ymax) {
     extern __shared__ SpeciesDev s_sp[];
+    __shared__ int s_b[2];
     const int nsp = cfg.n_species;
     const int G = cfg.n_ygroups;
     int32_t* s_gst = reinterpret_cast<int32_t*>(s_sp + nsp);
     int32_t* s_mem = s_gst + G + 1;
-    for (int k = threadIdx.x; k < nsp; k += blockDim.x) s_sp[k] = species[k];
-    for (int k = threadIdx.x; k < G + 1 + nsp; k += blockDim.x) s_gst[k] = cfg.yorder[k];
-    __syncthreads();
+    uint32_t* s_max = reinterpret_cast<uint32_t*>(s_mem + nsp);
     const int64_t n = cfg.n_cells;
-    const int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t first = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+    for (int k = threadIdx.x; k < nsp; k += blockDim.x) {
+        s_sp[k] = species[k];
+        s_max[k] = 0u;
+    }
+    for (int k = threadIdx.x; k < G + 1 + nsp; k += blockDim.x) s_gst[k] = cfg.yorder[k];
+    if (threadIdx.x < 2) {
+        const int64_t lb = threadIdx.x == 0 ? first : min(first + blockDim.x, n) - 1;
+        s_b[threadIdx.x] = surface_of(cfg.surf, cfg.n_surfaces, lb);
+    }
+    __syncthreads();
+    const int64_t l = first + threadIdx.x;
+    const bool valid = l < n;
+    const bool one_surface = s_b[0] == s_b[1];
+    const int b = one_surface ? s_b[0] : surface_of(cfg.surf, cfg.n_surfaces, valid ? l : n - 1);
     // blockIdx.y picks every gridDim.y-th species group: the groups come in
     // decreasing order of work, so interleaving keeps the rows' work equal,
     // and the grid has several waves of blocks
     const int k0 = blockIdx.y, kstep = gridDim.y;
-    if (l < n) {
-        const float4 da = cells.da[l];
-        if (da.x < 0.0f) {
-            for (int j = k0; j < G; j += kstep)
-                for (int t = s_gst[j]; t < s_gst[j + 1]; t++)
-                    yields[static_cast<int64_t>(s_mem[t]) * n + l] = 0.0f;
-        } else {
-            cell_yields<kDiff>(cfg, cells, s_sp, s_gst, s_mem, G, k0, kstep, n, l, da, yields);
-        }
+    const float4 da = cells.da[valid ? l : 0];
+    const bool live = valid && !(da.x < 0.0f);
+    cell_yields<kDiff>(cfg, cells, s_sp, s_gst, s_mem, G, k0, kstep, n, l, da, valid, live,
+                       one_surface ? s_max : nullptr, ymax + static_cast<int64_t>(b) * nsp,
+                       yields);
+    if (one_surface) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < nsp; k += blockDim.x)
+            if (s_max[k]) atomicMax(ymax + static_cast<int64_t>(s_b[0]) * nsp + k, s_max[k]);
     }
 }
 
@@ -415,29 +455,6 @@ __device__ __forceinline__ TileRef tile_ref(const SurfSeg* __restrict__ surf, in
     r.tile = local - static_cast<int64_t>(r.k) * r.sg->nt;
     if (r.k >= S) r.k = S - 1;   // not reached: the grid has exactly the batch's tiles
     return r;
-}
-
-// maximum yield of every row, as float bits (the yields are >= +0, so the
-// unsigned order of the bits is the order of the values); ymax starts at 0
-__global__ void __launch_bounds__(kScanThreads)
-cdf_tile_max_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg* __restrict__ surf,
-                    int n_surf, int S, uint32_t* __restrict__ ymax) {
-    const TileRef tr = tile_ref(surf, n_surf, S, blockIdx.x);
-    const int64_t n = tr.sg->n;
-    const int64_t t0 = tr.tile * kScanTile;
-    const uint32_t* row =
-        reinterpret_cast<const uint32_t*>(yields + static_cast<int64_t>(tr.k) * N + tr.sg->c0);
-    uint32_t v[kScanPer];
-#pragma unroll
-    for (int k = 0; k < kScanPer; k++) {
-        const int64_t i = t0 + k * kScanThreads + threadIdx.x;
-        v[k] = i < n ? __ldg(row + i) : 0u;
-    }
-    uint32_t m = 0u;
-#pragma unroll
-    for (int k = 0; k < kScanPer; k++) m = max(m, v[k]);
-    m = __reduce_max_sync(0xffffffffu, m);
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(ymax + tr.b * S + tr.k, m);
 }
 
 __global__ void __launch_bounds__(kScanThreads)
@@ -605,11 +622,15 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg*
 // launch wrappers
 
 cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev* sp,
-                          float* yields, cudaStream_t stream) {
+                          float* yields, uint32_t* ymax, cudaStream_t stream) {
+    cudaError_t e0 = cudaMemsetAsync(
+        ymax, 0, sizeof(uint32_t) * static_cast<size_t>(cfg.n_surfaces) * cfg.n_species, stream);
+    if (e0 != cudaSuccess) return e0;
     if (cfg.n_cells <= 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>((cfg.n_cells + kYieldThreads - 1) / kYieldThreads);
+    // species, group starts and members, per-block species maxima
     const size_t smem = sizeof(SpeciesDev) * static_cast<size_t>(cfg.n_species) +
-                        sizeof(int32_t) * static_cast<size_t>(cfg.n_ygroups + 1 + cfg.n_species);
+                        sizeof(int32_t) * static_cast<size_t>(cfg.n_ygroups + 1 + 2 * cfg.n_species);
     auto kernel = cfg.include_diff ? yields_kernel<true> : yields_kernel<false>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -618,7 +639,7 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
     }
     const int want = cfg.yield_groups > 0 ? cfg.yield_groups : kYieldGroups;
     const unsigned groups = static_cast<unsigned>(std::max(1, std::min(want, cfg.n_ygroups)));
-    kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields);
+    kernel<<<dim3(blocks, groups), kYieldThreads, smem, stream>>>(cfg, cells, sp, yields, ymax);
     return cudaGetLastError();
 }
 
@@ -630,10 +651,7 @@ cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int 
                        unsigned long long* cdf, int32_t* guide, cudaStream_t stream) {
     if (n_tiles <= 0 || S <= 0 || n_surf <= 0) return cudaSuccess;
     const int rows = n_surf * S;
-    cudaError_t e = cudaMemsetAsync(ymax, 0, sizeof(uint32_t) * rows, stream);
-    if (e != cudaSuccess) return e;
     const unsigned grid = static_cast<unsigned>(n_tiles);
-    cdf_tile_max_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax);
     cdf_tile_sum_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax,
                                                           tile_sum);
     cdf_tile_offset_kernel<<<rows, kScanThreads, 0, stream>>>(surf, S, tile_sum, ymax, tile_off,
