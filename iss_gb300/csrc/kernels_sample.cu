@@ -63,11 +63,20 @@ static_assert(sizeof(PoissonC) == kPoissonConsts * sizeof(double), "PoissonC lay
 // Inversion CDF of one species, cdf[0..len) as the inversion loop forms it,
 // stopped where adding the next term no longer changes it (then every later
 // term is smaller still); len = 0 when kInvTable entries do not reach that.
+// Each entry is held as floor(cdf 2^53): the draw's uniform is an integer
+// U times 2^-53 (u53), and u > cdf exactly when U > floor(cdf 2^53), so the
+// search compares 64-bit integers (ALU) instead of doubles (FP64 pipe) and
+// finds the same k.
 struct PoissonInv {
-    double cdf[kInvTable];
+    unsigned long long icdf[kInvTable];
     int len;
 };
 static_assert(sizeof(PoissonInv) == (kInvTable + 1) * sizeof(double), "PoissonInv layout");
+
+__device__ __forceinline__ unsigned long long floor_2p53(double x) {
+    // x in [0, 1]: x 2^53 is exact and below 2^53 + 1, truncation is floor
+    return static_cast<unsigned long long>(x * 9007199254740992.0);
+}
 
 __device__ PoissonC poisson_consts(double mu) {
     PoissonC c{};
@@ -103,7 +112,7 @@ __device__ void poisson_inv_table(const PoissonC& c, PoissonInv& t) {
     t.len = 0;
     if (!(c.mu < 12.0)) return;
     double p = c.emu, cdf = p;
-    t.cdf[0] = cdf;
+    t.icdf[0] = floor_2p53(cdf);
     for (int k = 1; k < kInvTable; k++) {
         p = __dmul_rn(p, c.mu / static_cast<double>(k));
         const double next = __dadd_rn(cdf, p);
@@ -112,7 +121,7 @@ __device__ void poisson_inv_table(const PoissonC& c, PoissonInv& t) {
             return;
         }
         cdf = next;
-        t.cdf[k] = cdf;
+        t.icdf[k] = floor_2p53(cdf);
     }
 }
 
@@ -122,17 +131,19 @@ __device__ int64_t poisson_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t 
     const double mu = c.mu;
     if (mu < 12.0) {
         const uint4 w = block(iter0, 0u, c2, c3, k0, k1);
-        const double u = u53(w.x, w.y);
         if (inv && inv->len > 0) {
-            // first k with u <= cdf[k]; past the saturated end the loop below
-            // would run to its cap
+            // first k with u <= cdf[k], u = U 2^-53; past the saturated end
+            // the loop below would run to its cap
+            const unsigned long long U = (static_cast<unsigned long long>(w.x >> 5) << 26) |
+                                         static_cast<unsigned long long>(w.y >> 6);
             int lo = 0, hi = inv->len;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (u > inv->cdf[mid]) lo = mid + 1; else hi = mid;
+                if (U > inv->icdf[mid]) lo = mid + 1; else hi = mid;
             }
             return lo < inv->len ? lo : 1000;
         }
+        const double u = u53(w.x, w.y);
         double p = c.emu;
         double cdf = p;
         int64_t k = 0;
@@ -242,8 +253,12 @@ __global__ void counts_kernel(DevConfig cfg_in, const SpeciesDev* __restrict__ s
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = static_cast<int64_t>(cfg.n_events) * cfg.n_species;
     if (idx >= total) return;
-    const int e = static_cast<int>(idx / cfg.n_species);
-    const int s = static_cast<int>(idx % cfg.n_species);
+    // species-major threads: a warp draws one species in consecutive events,
+    // so its lanes take the same branch (inversion table or PTRS) and read
+    // the same constants; every draw is keyed by (event, species)
+    const int s = static_cast<int>(idx / cfg.n_events);
+    const int e = static_cast<int>(idx % cfg.n_events);
+    const int64_t seg = static_cast<int64_t>(e) * cfg.n_species + s;
     const uint32_t c2 = cfg.event_offset + static_cast<uint32_t>(e);
     const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCount << 16);
     const int row = cfg.ev_surf[e] * cfg.n_species + s;    // (surface, species)
@@ -279,7 +294,7 @@ __global__ void counts_kernel(DevConfig cfg_in, const SpeciesDev* __restrict__ s
         if (nsamp < 0) atomicCAS(error, 0, 3);
     }
     const int32_t c = static_cast<int32_t>(nsamp < 0 ? 0 : nsamp);
-    counts[idx] = c * records_per_draw(cfg, sp);       // records of the segment
+    counts[seg] = c * records_per_draw(cfg, sp);       // records of the segment
     items[item_index(cfg, e, s)] = (c + cfg.item_size - 1) / cfg.item_size;
 }
 
