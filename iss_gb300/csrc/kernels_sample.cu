@@ -200,6 +200,9 @@ __device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
 // a work item is cfg.item_size consecutive draws of one (event, species)
 // segment; the cell assignment takes them 64 at a time (two per lane)
 constexpr int kAssignSub = 64;
+// guide buckets spanning at most this many cells past their first are
+// resolved with one batch of CDF reads (cell_assign_kernel)
+constexpr int kAssignSpan = 3;
 
 // Work items are ordered by event chunk (cfg.chunk_events consecutive events),
 // then species, then event: warps that run at the same time mostly sample one
@@ -1229,6 +1232,33 @@ cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
         hi0 = min(max(hi0, lo0), last);
         lo1 = min(max(lo1, 0), last);
         hi1 = min(max(hi1, lo1), last);
+        // buckets of up to kAssignSpan cells: the candidates' CDF entries are
+        // read at once and counted (C is nondecreasing and C[lo] <= v, so the
+        // cell is lo + #{i in 1..w : C[lo + i] <= v}, what the binary search
+        // below finds): one dependent read instead of a chain of them
+        {
+            const int w0 = hi0 - lo0, w1 = hi1 - lo1;
+            unsigned long long a0[kAssignSpan], a1[kAssignSpan];
+#pragma unroll
+            for (int i = 0; i < kAssignSpan; i++) {
+                a0[i] = (w0 <= kAssignSpan && i < w0) ? __ldg(row + lo0 + 1 + i) : ~0ull;
+                a1[i] = (w1 <= kAssignSpan && i < w1) ? __ldg(row + lo1 + 1 + i) : ~0ull;
+            }
+            int k0 = 0, k1 = 0;
+#pragma unroll
+            for (int i = 0; i < kAssignSpan; i++) {
+                k0 += a0[i] <= q0;
+                k1 += a1[i] <= q1;
+            }
+            if (w0 <= kAssignSpan) {
+                lo0 += k0;
+                hi0 = lo0;
+            }
+            if (w1 <= kAssignSpan) {
+                lo1 += k1;
+                hi1 = lo1;
+            }
+        }
         while (lo0 < hi0 || lo1 < hi1) {
             const int m0 = (lo0 + hi0 + 1) >> 1, m1 = (lo1 + hi1 + 1) >> 1;
             const unsigned long long c0 = lo0 < hi0 ? __ldg(row + m0) : 0ull;
