@@ -336,3 +336,42 @@ def test_edge_case_surfaces():
     s.generate_samples()
     h0, off0 = s.all_hadrons()
     assert len(h0) == 0 and s.get_number_of_sampled_events() == 0 and off0.tolist() == [0]
+
+
+@pytest.mark.parametrize("diffusion", [0, 1])
+def test_grouped_yields_with_strange_and_charge_potentials(diffusion):
+    """The yields kernel evaluates one thermal series per group of species
+    with the same mass and statistics and reuses it for every member whose
+    chemical potential in the cell has the same bits.  With mu_S and mu_Q
+    nonzero in most cells (isospin partners and particle/antiparticle pairs
+    then differ) and zero in every seventh cell (they share), the per-cell
+    yields still match the FP64 oracle."""
+    surf = S.finite_density_3d(3000, seed=5)
+    fo = surf.fo_surf().copy()
+    rng = np.random.default_rng(3)
+    fo[:, 17] = rng.uniform(-0.1, 0.1, len(fo)).astype(np.float32)     # mu_S, GeV
+    fo[:, 18] = rng.uniform(-0.05, 0.05, len(fo)).astype(np.float32)   # mu_Q, GeV
+    fo[::7, 17:19] = 0.0
+    params = dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=2, include_deltaf_shear=1,
+                  include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1, turn_on_rhob=1,
+                  include_deltaf_diffusion=diffusion, turn_on_diff=diffusion,
+                  number_of_repeated_sampling=2)
+    s = iSS(".", inputfile="")
+    s.set_params(**params)
+    s.set_surface(fo)
+    s.set_random_seed(1)
+    s.generate_samples()
+    lrf = s.lrf_cells()
+    keep = (lrf[:, 4] >= 0).astype(np.int32)
+    assert np.abs(lrf[:, 17]).max() > 0.05 and np.abs(lrf[:, 18]).max() > 0.02   # mu_S, mu_Q reach the cells
+    sp = O.chosen_species(S.TABLE_DIR, 2)
+    oc = O.OracleConfig(params, S.TABLE_DIR, n_events=2, seed=1)
+    ref = O.yields(oc, sp, lrf, keep)
+    y = s.cell_yields().astype(np.float64)
+    big = ref > 1e-30 * ref.max()
+    rel = np.abs(y[big] - ref[big]) / ref[big]
+    assert rel.max() < CELL_RTOL, f"per-cell yields differ by {rel.max():.2e}"
+    tot = s.species_yields()
+    rt = ref.sum(1)
+    m = rt > 0
+    assert (np.abs(tot[m] - rt[m]) / rt[m]).max() < TOTAL_RTOL
