@@ -214,50 +214,53 @@ __device__ __forceinline__ SeriesSums thermal_series(const DevConfig& cfg, const
     return SeriesSums{Neq, b1, b2, b3, q1, q2};
 }
 
-// The yield of species sp in cell l from its series sums: the prefactor,
-// the bulk and diffusion terms and the clip at zero of
-// calculate_dN_dxtdy_for_one_particle_species (src/FSSW.cpp:565-715).
+// The yield of calculate_dN_dxtdy_for_one_particle_species
+// (src/FSSW.cpp:565-715) is, for a species of degeneracy g and baryon number
+// B, g (X + B Y): X and Y hold the prefactor, the equilibrium sum and the
+// bulk and diffusion terms, and depend on the species only through the
+// quantities its group shares (mass and the series sums).  They are formed
+// once per series; each member then costs one multiply-add.
 template <bool kDiff>
-__device__ __forceinline__ float assemble_yield(const CellYieldIn& c, const SpeciesDev& sp,
-                                                const SeriesSums& ss, float4 da) {
+__device__ __forceinline__ float2 yield_coefs(const CellYieldIn& c, const SpeciesDev& sp,
+                                              const SeriesSums& ss, float4 da) {
     const float T = c.T;
     const float4 cf = c.cf;
-    const bool with_bulk = c.with_bulk, kind_ce = c.kind_ce;
-    constexpr bool with_diff = kDiff;
-    const int bulk_kind = c.bulk_kind;
-    const float bulkPi = c.bulkPi, dsq = c.dsq, pref_q = c.pref_q, inv_kappa = c.inv_kappa;
-    const float unit_pref = c.unit_pref;
     const float mass = sp.m_hi + sp.m_lo;
-    const float Neq = ss.Neq, b1 = ss.b1, b2 = ss.b2, b3 = ss.b3, q1 = ss.q1, q2 = ss.q2;
     const float m2 = mass * mass;
-    const float ug = unit_pref * sp.degen;
-    const float pref = ug * da.x;
-    float total = pref * (m2 * T * Neq);
-    if (with_bulk) {
-        if (kind_ce) {
+    float x = m2 * T * ss.Neq;
+    float y = 0.0f;
+    if (c.with_bulk) {
+        if (c.kind_ce) {
             // Chapman-Enskog form, bulk_deltaf_kind 1 and 21
-            const float r1 = m2 * T * b1;
-            const float r2 = m2 * mass / 3.0f * b2;
-            total += pref * (-bulkPi * cf.x) * (-cf.y * r1 + r2);
-        } else if (bulk_kind == 11) {
-            const float r1 = m2 * T * b1;
-            const float r2 = m2 * T * T * b2;
-            const float r3 = m2 * mass * T * T * b3;
-            total += pref * bulkPi *
-                     (r1 * m2 * cf.x + r2 * static_cast<float>(sp.baryon) * cf.y + r3 * cf.z);
+            const float r1 = m2 * T * ss.b1;
+            const float r2 = m2 * mass / 3.0f * ss.b2;
+            x += (-c.bulkPi * cf.x) * (-cf.y * r1 + r2);
+        } else if (c.bulk_kind == 11) {
+            const float r1 = m2 * T * ss.b1;
+            const float r2 = m2 * T * T * ss.b2;
+            const float r3 = m2 * mass * T * T * ss.b3;
+            x += c.bulkPi * (r1 * m2 * cf.x + r3 * cf.z);
+            y += c.bulkPi * r2 * cf.y;
         }
     }
-    if (with_diff) {
-        const float r4 = m2 * T * T * q1;
-        const float r5 = (T * T * T / 3.0f) * q2;
-        total += ug * dsq * inv_kappa * (-pref_q * r4 - static_cast<float>(sp.baryon) * r5);
+    x *= da.x;
+    y *= da.x;
+    if (kDiff) {
+        const float r4 = m2 * T * T * ss.q1;
+        const float r5 = (T * T * T / 3.0f) * ss.q2;
+        const float dq = c.dsq * c.inv_kappa;
+        x -= dq * c.pref_q * r4;
+        y -= dq * r5;
     }
-    // negative -> 0 (FSSW::calculate_dN_dxtdy_for_one_particle_species,
-    // src/FSSW.cpp:707); NaN -> 0; +inf -> FLT_MAX so the cell CDF stays
-    // finite; -0 -> +0 so the bits order as the values
-    const float yv = __uint_as_float(
-        __float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
-    return yv;
+    return make_float2(c.unit_pref * x, c.unit_pref * y);
+}
+
+// negative -> 0 (FSSW::calculate_dN_dxtdy_for_one_particle_species,
+// src/FSSW.cpp:707); NaN -> 0; +inf -> FLT_MAX so the cell CDF stays
+// finite; -0 -> +0 so the bits order as the values
+__device__ __forceinline__ float member_yield(const SpeciesDev& sp, float2 xy) {
+    const float total = sp.degen * fmaf(static_cast<float>(sp.baryon), xy.y, xy.x);
+    return __uint_as_float(__float_as_uint(fminf(fmaxf(total, 0.0f), 3.40282347e38f)) & 0x7FFFFFFFu);
 }
 
 // Yields of the species groups k0, k0 + kstep, ... in cell l (not dropped:
@@ -317,7 +320,7 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
     c.unit_pref = unit_pref;
     for (int j = k0; j < n_groups; j += kstep) {
         const int a = s_gst[j], b = s_gst[j + 1];
-        SeriesSums ss{};
+        float2 xy = make_float2(0.0f, 0.0f);
         uint32_t mu_bits = 0;
         for (int t = a; t < b; t++) {
             const int k = s_mem[t];
@@ -326,10 +329,10 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
             if (live) {
                 const float mu = species_mu(sp, th);
                 if (t == a || __float_as_uint(mu) != mu_bits) {
-                    ss = thermal_series<kDiff>(cfg, c, sp, mu);
+                    xy = yield_coefs<kDiff>(c, sp, thermal_series<kDiff>(cfg, c, sp, mu), da);
                     mu_bits = __float_as_uint(mu);
                 }
-                yv = assemble_yield<kDiff>(c, sp, ss, da);
+                yv = member_yield(sp, xy);
             }
             if (valid) yields[static_cast<int64_t>(k) * n + l] = yv;
             // the species' largest yield (its float bits: yields are >= +0,
