@@ -45,17 +45,22 @@ bool load_zlib(ZlibApi* z) {
     return z->gzopen && z->gzwrite && z->gzclose;
 }
 
-uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
-    static uint32_t table[256];
-    static bool init = false;
-    if (!init) {
+struct Crc32Table {
+    uint32_t v[256];
+    Crc32Table() {
         for (uint32_t i = 0; i < 256; i++) {
             uint32_t c = i;
             for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            table[i] = c;
+            v[i] = c;
         }
-        init = true;
     }
+};
+
+uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
+    // built once; the initialisation of a function-local static is thread-safe,
+    // so handles on several threads may write gzip output at the same time
+    static const Crc32Table tab;
+    const uint32_t* table = tab.v;
     crc = ~crc;
     for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
     return ~crc;
