@@ -598,8 +598,12 @@ cdf_tile_scan_kernel(const float* __restrict__ yields, int64_t N, const SurfSeg*
     // with Q = qd G + qr; f is stepped exactly: f(j+1) = f(j) + qd + carry.
     // First bucket at or after this thread's first cell: a float estimate of
     // ceil(start G / Q), then exact steps.
-    int64_t j = static_cast<int64_t>(static_cast<float>(start) *
-                                     (static_cast<float>(G) / static_cast<float>(Q)));
+    // (the top 24 significant bits of Q and start, converted exactly from
+    // 32-bit integers: within a bucket of the answer for g <= 22)
+    const int qsh = max(0, 40 - __clzll(static_cast<long long>(Q)));
+    int64_t j = static_cast<int64_t>(
+        static_cast<float>(static_cast<uint32_t>(start >> qsh)) *
+        __fdividef(static_cast<float>(G), static_cast<float>(static_cast<uint32_t>(Q >> qsh))));
     j = j < 0 ? 0 : (j > G ? G : j);
     while (j > 0 && bucket_start(static_cast<unsigned long long>(j - 1), g, Q) >= start) --j;
     while (j < G && bucket_start(static_cast<unsigned long long>(j), g, Q) < start) ++j;
