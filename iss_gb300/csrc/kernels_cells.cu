@@ -347,13 +347,14 @@ __device__ __forceinline__ void cell_yields(const DevConfig& cfg, const CellArra
 }
 
 // kDiff: include_deltaf_diffusion (a separate instantiation, so the common
-// case carries none of the diffusion series' registers).  Besides the
+// case carries none of the diffusion series' registers; it is held to 6
+// blocks per SM, whose few spills cost less than the warps they add).  Besides the
 // yields, the kernel raises ymax[b S + k] to the largest yield of species k
 // on surface b (as float bits; ymax starts at 0): through a per-block
 // maximum in shared memory when the block's cells lie on one surface, else
 // lane by lane.
 template <bool kDiff>
-__global__ void __launch_bounds__(kYieldThreads)
+__global__ void __launch_bounds__(kYieldThreads, kDiff ? 4 : 6)
 yields_kernel(DevConfig cfg, CellArrays cells, const SpeciesDev* __restrict__ species,
               float* __restrict__ yields, uint32_t* __restrict__ ymax) {
     extern __shared__ SpeciesDev s_sp[];
