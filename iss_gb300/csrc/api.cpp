@@ -589,6 +589,7 @@ CellArrays cell_arrays(iss_handle* h) {
     a.pi2 = b + 6 * n;
     a.coef = b + 7 * n;
     a.rec = b + 8 * n;   // 128-byte records, 128-byte aligned
+    a.srec = b + 16 * n;  // the lean sampler's 128-byte records
     a.milne = h->cfg.mc_sampling == 2 ? h->d_milne.ptr : nullptr;
     return a;
 }
@@ -606,7 +607,8 @@ iss_status run_cells(iss_handle* h) {
                                     cudaMemcpyHostToDevice, st));
         h->surface_on_device = true;
     }
-    CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 16));   // 8 SoA arrays + the records
+    // 8 SoA arrays, the records and the lean sampler's records
+    CUDA_TRY(h, h->d_cells.reserve(static_cast<size_t>(n) * 24));
     if (c.mc_sampling == 2) CUDA_TRY(h, h->d_milne.reserve(static_cast<size_t>(n) * 6));
     CUDA_TRY(h, h->d_yields.reserve(static_cast<size_t>(n) * S));
     const size_t rows = static_cast<size_t>(c.n_surfaces) * S;

@@ -115,6 +115,15 @@ struct CellArrays {
     // th2, pi1, pi2, coef): the sampler reads a random cell's record as one
     // cache line instead of eight
     float4* rec;
+    // the lean FSSW sampler's constants of each cell, eight float4 (128
+    // bytes) computed once by the prologue from the record above:
+    // (t, x, y, z) for 3+1D surfaces, else (tau, x, y, eta); u^mu;
+    // (d0, D, einv, T) and (n_x, n_y, n_z, 1/T) of the flux frame
+    // dsigma_LRF = (d0, D n) with einv = 1/|t x n| (prop_e1);
+    // (mu_B, mu_S, mu_Q, 0); pi_xx, pi_xy, pi_xz, pi_yy times the shear
+    // prefactor; (pi_yz times it, bulk b0 / m^2, b1 (/ B for kind 11), b2);
+    // (bulk bi0 / m^2, 0, 0, 0)
+    float4* srec;
     // MC_sampling = 2 only (else null): the regulated Milne-frame cell, six
     // float4 per cell: (da0..da3), (u0..u3), (pi00 pi01 pi02 pi03),
     // (pi11 pi12 pi13 pi22), (pi23 pi33 q0 q1), (q2 q3 bulkPi 0)

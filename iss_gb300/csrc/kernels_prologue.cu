@@ -262,6 +262,60 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
     if (cfg.include_diff) kappa = qmu_coeff(cfg.tab.qmu, Tdec, s[16]);
     rec[7] = cells.coef[l] = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]),
                                          static_cast<float>(c[2]), static_cast<float>(kappa));
+    if (cells.srec) {
+        // the lean sampler's per-cell constants, from the record's floats
+        const float4 da = make_float4(dl[0], -dl[1], -dl[2], -dl[3]);
+        const float4 th = make_float4(Tdec, s[16], s[17], s[18]);
+        const float4 th2 = make_float4(Edec, Pdec, Bn, s[29]);
+        const float4 p1 = make_float4(pl[0], pl[1], pl[2], pl[3]);
+        const float4 p2 = make_float4(pl[4], ql[1], ql[2], ql[3]);
+        const float4 cf = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]),
+                                      static_cast<float>(c[2]), static_cast<float>(kappa));
+        const float T = th.x;
+        const float d0 = fabsf(da.x);
+        float D = sqrtf(da.y * da.y + da.z * da.z + da.w * da.w);
+        float nx = 0.0f, ny = 0.0f, nz = 1.0f;
+        if (D > 1e-30f) {
+            const float inv = 1.0f / D;
+            nx = da.y * inv;
+            ny = da.z * inv;
+            nz = da.w * inv;
+        } else {
+            D = 0.0f;
+        }
+        const float einv = fabsf(nz) < 0.9f ? 1.0f / sqrtf(ny * ny + nx * nx)
+                                            : 1.0f / sqrtf(nz * nz + ny * ny);
+        // shear prefactor (the sampler divides by p0 for the CE form, neos_kind 1)
+        float sc = 0.0f;
+        if (cfg.include_shear) {
+            if (cfg.neos_kind == 1) sc = 1.0f / (2.0f * cf.z * T);
+            else if (cfg.neos_kind == 0) sc = cf.x;
+            else sc = 1.0f / (2.0f * T * T * (th2.x + th2.y));
+        }
+        float cb0 = 0.0f, cb1 = 0.0f, cb2 = 0.0f, cbi0 = 0.0f;
+        if (cfg.include_bulk) {
+            if (cfg.bulk_kind == 11) {
+                const float Pi = th2.w;
+                cb0 = Pi * cf.x;
+                cb1 = Pi * cf.y;
+                cb2 = Pi * cf.z;
+            } else if (cfg.bulk_kind == 21 || cfg.bulk_kind == 1) {
+                const float Pi = (cfg.bulk_kind == 1) ? th2.w / 0.197327053f : th2.w;
+                cbi0 = -cf.x * Pi / (3.0f * T);
+                cb1 = cf.x * Pi * cf.y / T;
+            }
+        }
+        float4* sr = cells.srec + 8 * l;
+        sr[0] = cfg.hydro_mode == 2 ? make_float4(tau * coshf(eta), xpt, ypt, tau * sinhf(eta))
+                                    : make_float4(tau, xpt, ypt, eta);
+        sr[1] = make_float4(ut, ux, uy, uz);
+        sr[2] = make_float4(d0, D, einv, T);
+        sr[3] = make_float4(nx, ny, nz, 1.0f / T);
+        sr[4] = make_float4(th.y, th.z, th.w, 0.0f);
+        sr[5] = make_float4(p1.x * sc, p1.y * sc, p1.z * sc, p1.w * sc);
+        sr[6] = make_float4(p2.x * sc, cb0, cb1, cb2);
+        sr[7] = make_float4(cbi0, 0.0f, 0.0f, 0.0f);
+    }
 }
 
 }  // namespace

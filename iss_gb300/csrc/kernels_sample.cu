@@ -484,9 +484,82 @@ __device__ __forceinline__ int cell_search(const unsigned long long* __restrict_
 // returns false when m/T - mu/T is outside the reference's momentum tables.
 // kLean: the configuration has neither diffusion nor the compat-fermion
 // correction (both then compile out, which frees registers in the sampler)
+// the lean instantiation: the cell-only constants come precomputed from the
+// prologue (CellArrays::srec); the rest is setup_prop's own arithmetic
+__device__ bool setup_prop_lean(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
+                                int l, Prop& p) {
+    const float4* sr = cells.srec + 8 * static_cast<int64_t>(l);
+    const float4 fr = __ldg(sr + 2);   // d0, D, einv, T
+    const float4 nb = __ldg(sr + 3);   // n, 1/T
+    const float4 mu4 = __ldg(sr + 4);
+    const float4 sh1 = __ldg(sr + 5);
+    const float4 sh2 = __ldg(sr + 6);
+    const float T = fr.w;
+    const float beta = nb.w;
+    const float m = sp.m_hi + sp.m_lo;
+    const float mu_raw = static_cast<float>(sp.baryon) * mu4.x + static_cast<float>(sp.strange) * mu4.y +
+                         static_cast<float>(sp.charge) * mu4.z;
+    const float mu = fminf(m, mu_raw);
+    p.T = T;
+    p.m = m;
+    p.sign = sp.sign;
+    p.mt = m * beta;
+    p.mut = mu * beta;
+    p.a = (m - mu) * beta;
+    const int sampler = p.a < 30.0f ? 0 : (p.a < 50.0f ? 1 : 2);
+    float e0, de;
+    int npts;
+    if (p.sign == -1) {
+        e0 = (sampler == 0 ? 0.05f : (sampler == 1 ? 30.0f : 50.0f)) + 0.05f;
+        de = 0.05f;
+        npts = 1001;
+    } else {
+        e0 = (sampler == 0 ? 0.0f : (sampler == 1 ? 30.0f : 50.0f));
+        de = 0.02f;
+        npts = 2001;
+    }
+    const int idx_min = static_cast<int>((p.a - e0) / de);
+    if (idx_min < 0 || idx_min >= npts - 1) return false;
+    p.Kmax = e0 + (npts - 1) * de - p.a;
+    p.w3 = 2.0f;
+    p.w32 = 2.0f + 2.0f * p.mt;
+    p.W = p.w32 + 0.5f * p.mt * p.mt;
+    p.qa = -expm1f(-p.a);
+    p.compat = 0;
+    p.cpoly = p.mut * p.mut - 0.5f * p.mt * p.mt;
+    p.rmax = 1.0f;
+    p.d0 = fr.x;
+    p.D = fr.y;
+    p.einv = fr.z;
+    p.nx = nb.x;
+    p.ny = nb.y;
+    p.nz = nb.z;
+    // shear tensor already times its prefactor
+    p.pxx = sh1.x;
+    p.pxy = sh1.y;
+    p.pxz = sh1.z;
+    p.pyy = sh1.w;
+    p.pyz = sh2.x;
+    p.shear_c = 1.0f;
+    p.bi0 = p.b0 = p.b1 = p.b2 = 0.0f;
+    if (cfg.include_bulk) {
+        if (cfg.bulk_kind == 11) {
+            p.b0 = sh2.y * (m * m);
+            p.b1 = sh2.z * static_cast<float>(sp.baryon);
+            p.b2 = sh2.w;
+        } else if (cfg.bulk_kind == 21 || cfg.bulk_kind == 1) {
+            p.bi0 = __ldg(sr + 7).x * (m * m);
+            p.b1 = sh2.z;
+        }
+    }
+    p.qx = p.qy = p.qz = p.pq = p.Bq = 0.0f;
+    return true;
+}
+
 template <bool kLean = false>
 __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
                            int l, Prop& p) {
+    if (kLean) return setup_prop_lean(cfg, cells, sp, l, p);
     const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
     const float4 da = __ldg(rec + 1);
     const float4 th = __ldg(rec + 3);
@@ -1081,10 +1154,13 @@ __device__ __forceinline__ void write_hadron(HadronRec* out, int64_t slot, int p
     o[4] = make_float2(y, z);
 }
 
+// kLean: u and the position come from the lean sampler's record, whose
+// position of a 3+1D cell is already (t, x, y, z)
+template <bool kLean = false>
 __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& p, int l, int pid,
                      float4 pl, float u_rap, HadronRec* out, int64_t slot) {
-    const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
-    const float4 u = __ldg(rec + 2);
+    const float4* rec = (kLean ? cells.srec : cells.rec) + 8 * static_cast<int64_t>(l);
+    const float4 u = __ldg(rec + (kLean ? 1 : 2));
     const float4 pos = __ldg(rec);
     const float pdu = pl.y * u.y + pl.z * u.z + pl.w * u.w;
     const float c = pdu / (u.x + 1.0f) + pl.x;
@@ -1097,6 +1173,10 @@ __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& 
         eta_s = pos.w;
         pz = lz;
         E = sqrtf(mT2 + lz * lz);
+        if (kLean) {
+            write_hadron(out, slot, pid, p.m, E, lx, ly, pz, pos.x, pos.y, pos.z, pos.w);
+            return;
+        }
     } else {
         const float mT = sqrtf(mT2);
         const float rap = cfg.y_lb + (cfg.y_rb - cfg.y_lb) * u_rap;
@@ -1154,11 +1234,13 @@ __device__ __forceinline__ bool try_any(const DevConfig& cfg, const PropEfa& p, 
                                         float4& pl, float& u_rap, unsigned& viol) {
     return try_efa(cfg, p, u, pl, u_rap, viol);
 }
+template <bool kLean>
 __device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells, const Prop& p,
                                          int l, int pid, float4 pl, float u_rap, HadronRec* out,
                                          int64_t slot) {
-    emit(cfg, cells, p, l, pid, pl, u_rap, out, slot);
+    emit<kLean>(cfg, cells, p, l, pid, pl, u_rap, out, slot);
 }
+template <bool kLean>
 __device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells,
                                          const PropEfa& p, int l, int pid, float4 pl, float u_rap,
                                          HadronRec* out, int64_t slot) {
@@ -1435,10 +1517,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                 // hadron's cell: the training rows of the learned proposal)
                 if (u.redraw > 0 && u.phase == 0) cell_of[u.slot] = u.cell;
                 if (kLcc)
-                    emit_any(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out,
-                             u.slot + u.phase);
+                    emit_any<kLean>(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out,
+                                    u.slot + u.phase);
                 else
-                    emit_any(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
+                    emit_any<kLean>(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
                 if (kLcc && u.mult == 2 && u.phase == 0) {
                     // the partner: same cell and mass, opposite B, S, Q
                     SpeciesDev sp2 = species[u.s];
