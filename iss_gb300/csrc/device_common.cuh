@@ -120,9 +120,9 @@ struct CellArrays {
     // (t, x, y, z) for 3+1D surfaces, else (tau, x, y, eta); u^mu;
     // (d0, D, einv, T) and (n_x, n_y, n_z, 1/T) of the flux frame
     // dsigma_LRF = (d0, D n) with einv = 1/|t x n| (prop_e1);
-    // (mu_B, mu_S, mu_Q, 0); pi_xx, pi_xy, pi_xz, pi_yy times the shear
-    // prefactor; (pi_yz times it, bulk b0 / m^2, b1 (/ B for kind 11), b2);
-    // (bulk bi0 / m^2, 0, 0, 0)
+    // (mu_B, mu_S, mu_Q, n_B/(e+P)); pi_xx, pi_xy, pi_xz, pi_yy times the
+    // shear prefactor; (pi_yz times it, bulk b0 / m^2, b1 (/ B for kind 11),
+    // b2); (bulk bi0 / m^2, q_x, q_y, q_z over kappa_B)
     float4* srec;
     // MC_sampling = 2 only (else null): the regulated Milne-frame cell, six
     // float4 per cell: (da0..da3), (u0..u3), (pi00 pi01 pi02 pi03),

@@ -311,10 +311,19 @@ cell_prologue_kernel(DevConfig cfg, const float* __restrict__ fo34, int64_t n, C
         sr[1] = make_float4(ut, ux, uy, uz);
         sr[2] = make_float4(d0, D, einv, T);
         sr[3] = make_float4(nx, ny, nz, 1.0f / T);
-        sr[4] = make_float4(th.y, th.z, th.w, 0.0f);
+        // diffusion: n_B / (e + P) and q^mu / kappa_B (the sampler's pq and q)
+        float pq = 0.0f, qkx = 0.0f, qky = 0.0f, qkz = 0.0f;
+        if (cfg.include_diff) {
+            const float ik = 1.0f / cf.w;
+            qkx = p2.y * ik;
+            qky = p2.z * ik;
+            qkz = p2.w * ik;
+            pq = th2.z / (th2.x + th2.y);
+        }
+        sr[4] = make_float4(th.y, th.z, th.w, pq);
         sr[5] = make_float4(p1.x * sc, p1.y * sc, p1.z * sc, p1.w * sc);
         sr[6] = make_float4(p2.x * sc, cb0, cb1, cb2);
-        sr[7] = make_float4(cbi0, 0.0f, 0.0f, 0.0f);
+        sr[7] = make_float4(cbi0, qkx, qky, qkz);
     }
 }
 

@@ -482,10 +482,10 @@ __device__ __forceinline__ int cell_search(const unsigned long long* __restrict_
 }
 
 // returns false when m/T - mu/T is outside the reference's momentum tables.
-// kLean: the configuration has neither diffusion nor the compat-fermion
-// correction (both then compile out, which frees registers in the sampler)
-// the lean instantiation: the cell-only constants come precomputed from the
-// prologue (CellArrays::srec); the rest is setup_prop's own arithmetic
+// The lean instantiations (no compat-fermion correction, with or without
+// diffusion, kDiff) take the cell-only constants precomputed by the prologue
+// (CellArrays::srec); the rest is setup_prop's own arithmetic
+template <bool kDiff>
 __device__ bool setup_prop_lean(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
                                 int l, Prop& p) {
     const float4* sr = cells.srec + 8 * static_cast<int64_t>(l);
@@ -553,13 +553,25 @@ __device__ bool setup_prop_lean(const DevConfig& cfg, const CellArrays& cells, c
         }
     }
     p.qx = p.qy = p.qz = p.pq = p.Bq = 0.0f;
+    if (kDiff && cfg.include_diff) {
+        const float4 dq = __ldg(sr + 7);   // q / kappa_B in its yzw
+        p.qx = dq.y;
+        p.qy = dq.z;
+        p.qz = dq.w;
+        p.pq = mu4.w;                      // n_B / (e + P)
+        p.Bq = static_cast<float>(sp.baryon);
+    }
     return true;
 }
 
-template <bool kLean = false>
+// kMode 0: every configuration, from the cell record; 1: lean (no diffusion,
+// no compat-fermion factor), from the prologue's lean record; 2: the same
+// with diffusion
+template <int kMode = 0>
 __device__ bool setup_prop(const DevConfig& cfg, const CellArrays& cells, const SpeciesDev& sp,
                            int l, Prop& p) {
-    if (kLean) return setup_prop_lean(cfg, cells, sp, l, p);
+    if (kMode != 0) return setup_prop_lean<kMode == 2>(cfg, cells, sp, l, p);
+    constexpr bool kLean = false;
     const float4* rec = cells.rec + 8 * static_cast<int64_t>(l);
     const float4 da = __ldg(rec + 1);
     const float4 th = __ldg(rec + 3);
@@ -691,7 +703,7 @@ __device__ float compat_ratio(const Prop& p, float Et) {
 
 // One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
 // the uniform used for the rapidity of boost-invariant surfaces.
-template <bool kLean = false>
+template <int kMode = 0>
 __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, const Unit& u,
                                          float4& pl, float& u_rap, unsigned& violations) {
     const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagTry << 16);
@@ -711,7 +723,7 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float em = expf(-Etil);
     const float a_q = (p.sign == -1) ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
     float a_c = 1.0f;
-    if (!kLean && p.compat) {
+    if (kMode == 0 && p.compat) {
         a_c = compat_ratio(p, Etil) / p.rmax;
         if (a_c > 1.0f) {
             violations++;
@@ -763,7 +775,7 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     if (cfg.include_bulk) {
         df += one_m * (p.bi0 / p0 + p.b0 + p.b1 * p0 + p.b2 * p0 * p0);
     }
-    if (!kLean && cfg.include_diff) {
+    if (kMode != 1 && cfg.include_diff) {
         const float qf = -(px * p.qx + py * p.qy + pz * p.qz);
         df += one_m * (p.pq - p.Bq / p0) * qf;
     }
@@ -1154,11 +1166,12 @@ __device__ __forceinline__ void write_hadron(HadronRec* out, int64_t slot, int p
     o[4] = make_float2(y, z);
 }
 
-// kLean: u and the position come from the lean sampler's record, whose
-// position of a 3+1D cell is already (t, x, y, z)
-template <bool kLean = false>
+// kMode 1, 2 (lean): u and the position come from the lean sampler's record,
+// whose position of a 3+1D cell is already (t, x, y, z)
+template <int kMode = 0>
 __device__ void emit(const DevConfig& cfg, const CellArrays& cells, const Prop& p, int l, int pid,
                      float4 pl, float u_rap, HadronRec* out, int64_t slot) {
+    constexpr bool kLean = kMode != 0;
     const float4* rec = (kLean ? cells.srec : cells.rec) + 8 * static_cast<int64_t>(l);
     const float4 u = __ldg(rec + (kLean ? 1 : 2));
     const float4 pos = __ldg(rec);
@@ -1214,33 +1227,33 @@ __device__ void emit_efa(const DevConfig& cfg, const CellArrays& cells, const Pr
 template <int kAlg> struct PropOf { using type = Prop; };
 template <> struct PropOf<2> { using type = PropEfa; };
 
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
                                           const SpeciesDev& sp, int l, Prop& p, bool) {
-    return setup_prop<kLean>(cfg, cells, sp, l, p);
+    return setup_prop<kMode>(cfg, cells, sp, l, p);
 }
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
                                           const SpeciesDev& sp, int l, PropEfa& p, bool keep_max) {
     return setup_efa(cfg, cells, sp, l, p, keep_max);
 }
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const Prop& p, const Unit& u, float4& pl,
                                         float& u_rap, unsigned& viol) {
-    return try_once<kLean>(cfg, p, u, pl, u_rap, viol);
+    return try_once<kMode>(cfg, p, u, pl, u_rap, viol);
 }
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const PropEfa& p, const Unit& u,
                                         float4& pl, float& u_rap, unsigned& viol) {
     return try_efa(cfg, p, u, pl, u_rap, viol);
 }
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells, const Prop& p,
                                          int l, int pid, float4 pl, float u_rap, HadronRec* out,
                                          int64_t slot) {
-    emit<kLean>(cfg, cells, p, l, pid, pl, u_rap, out, slot);
+    emit<kMode>(cfg, cells, p, l, pid, pl, u_rap, out, slot);
 }
-template <bool kLean>
+template <int kMode>
 __device__ __forceinline__ void emit_any(const DevConfig& cfg, const CellArrays& cells,
                                          const PropEfa& p, int l, int pid, float4 pl, float u_rap,
                                          HadronRec* out, int64_t slot) {
@@ -1361,9 +1374,11 @@ cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
 constexpr int kSampleThreads = 256;
 
 // kLcc: local_charge_conservation pairs (a separate instantiation, so the
-// common case carries none of the pair state); kLean: FSSW without diffusion
-// and without the compat-fermion correction (setup_prop)
-template <bool kLcc, bool kLearned, int kAlg, bool kLean>
+// common case carries none of the pair state); kMode (setup_prop): 0 every
+// configuration, 1 FSSW without diffusion and without the compat-fermion
+// correction (both compile out, which frees registers), 2 the same with
+// diffusion; 1 and 2 read the prologue's lean cell records
+template <bool kLcc, bool kLearned, int kAlg, int kMode>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict__ species,
                const int32_t* __restrict__ pids, const unsigned long long* __restrict__ cdf,
@@ -1484,7 +1499,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
                                    : nullptr;
                 }
-                if (!setup_any<kLean>(cfg, cells, species[u.s], l, p, false)) {
+                if (!setup_any<kMode>(cfg, cells, species[u.s], l, p, false)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     for (int q = 0; q < (kLcc ? u.mult : 1); q++)
@@ -1506,7 +1521,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     ok = try_once(cfg, p, u, pl, u_rap, n_viol);
                 }
             } else {
-                ok = try_any<kLean>(cfg, p, u, pl, u_rap, n_viol);
+                ok = try_any<kMode>(cfg, p, u, pl, u_rap, n_viol);
             }
             u.t++;
             u.tries_cell++;
@@ -1517,10 +1532,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                 // hadron's cell: the training rows of the learned proposal)
                 if (u.redraw > 0 && u.phase == 0) cell_of[u.slot] = u.cell;
                 if (kLcc)
-                    emit_any<kLean>(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out,
+                    emit_any<kMode>(cfg, cells, p, u.cell, u.phase ? -pid : pid, pl, u_rap, out,
                                     u.slot + u.phase);
                 else
-                    emit_any<kLean>(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
+                    emit_any<kMode>(cfg, cells, p, u.cell, pid, pl, u_rap, out, u.slot);
                 if (kLcc && u.mult == 2 && u.phase == 0) {
                     // the partner: same cell and mass, opposite B, S, Q
                     SpeciesDev sp2 = species[u.s];
@@ -1532,7 +1547,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
                     // (the lab-frame sampler keeps the hadron's maximum for
                     // its partner, src/emissionfunction.cpp:3503-3509)
-                    if (!setup_any<kLean>(cfg, cells, sp2, u.cell, p, true)) {
+                    if (!setup_any<kMode>(cfg, cells, sp2, u.cell, p, true)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
                         write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
@@ -1828,14 +1843,15 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
     const int64_t max_blocks = (n_items + (kSampleThreads / 32) - 1) / (kSampleThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    const bool lean = !cfg.include_diff && !cfg.compat_fermion;
+    const int mode = cfg.compat_fermion ? 0 : (cfg.include_diff ? 2 : 1);
     auto kernel =
         cfg.mc_sampling == 2
-            ? (cfg.lcc ? sampler_kernel<true, false, 2, false> : sampler_kernel<false, false, 2, false>)
+            ? (cfg.lcc ? sampler_kernel<true, false, 2, 0> : sampler_kernel<false, false, 2, 0>)
         : cfg.lpairs
-            ? (cfg.lcc ? sampler_kernel<true, true, 4, false> : sampler_kernel<false, true, 4, false>)
-        : lean ? (cfg.lcc ? sampler_kernel<true, false, 4, true> : sampler_kernel<false, false, 4, true>)
-               : (cfg.lcc ? sampler_kernel<true, false, 4, false> : sampler_kernel<false, false, 4, false>);
+            ? (cfg.lcc ? sampler_kernel<true, true, 4, 0> : sampler_kernel<false, true, 4, 0>)
+        : mode == 1 ? (cfg.lcc ? sampler_kernel<true, false, 4, 1> : sampler_kernel<false, false, 4, 1>)
+        : mode == 2 ? (cfg.lcc ? sampler_kernel<true, false, 4, 2> : sampler_kernel<false, false, 4, 2>)
+                    : (cfg.lcc ? sampler_kernel<true, false, 4, 0> : sampler_kernel<false, false, 4, 0>);
     kernel<<<static_cast<unsigned>(blocks), kSampleThreads, 0, stream>>>(
         cfg, cells, sp, pids, cdf, guide, qtot, offsets, item_off, item_seg, k_begin,
         k_end, cell_of, out, work_counter, counters, k_end_dev);
