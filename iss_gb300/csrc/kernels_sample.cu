@@ -1377,7 +1377,8 @@ constexpr int kSampleThreads = 256;
 // common case carries none of the pair state); kMode (setup_prop): 0 every
 // configuration, 1 FSSW without diffusion and without the compat-fermion
 // correction (both compile out, which frees registers), 2 the same with
-// diffusion; 1 and 2 read the prologue's lean cell records
+// diffusion; 1 and 2 read the prologue's lean cell records (the learned
+// proposal's plain component uses the same Prop fields)
 template <bool kLcc, bool kLearned, int kAlg, int kMode>
 __global__ void __launch_bounds__(kSampleThreads, 3)
 sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict__ species,
@@ -1518,7 +1519,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     n_ltries++;
                     n_lhad += ok;
                 } else {
-                    ok = try_once(cfg, p, u, pl, u_rap, n_viol);
+                    ok = try_once<kMode>(cfg, p, u, pl, u_rap, n_viol);
                 }
             } else {
                 ok = try_any<kMode>(cfg, p, u, pl, u_rap, n_viol);
@@ -1848,7 +1849,9 @@ cudaError_t launch_sampler(const DevConfig& cfg, const CellArrays& cells, const 
         cfg.mc_sampling == 2
             ? (cfg.lcc ? sampler_kernel<true, false, 2, 0> : sampler_kernel<false, false, 2, 0>)
         : cfg.lpairs
-            ? (cfg.lcc ? sampler_kernel<true, true, 4, 0> : sampler_kernel<false, true, 4, 0>)
+            ? (mode == 1 ? (cfg.lcc ? sampler_kernel<true, true, 4, 1> : sampler_kernel<false, true, 4, 1>)
+             : mode == 2 ? (cfg.lcc ? sampler_kernel<true, true, 4, 2> : sampler_kernel<false, true, 4, 2>)
+                         : (cfg.lcc ? sampler_kernel<true, true, 4, 0> : sampler_kernel<false, true, 4, 0>))
         : mode == 1 ? (cfg.lcc ? sampler_kernel<true, false, 4, 1> : sampler_kernel<false, false, 4, 1>)
         : mode == 2 ? (cfg.lcc ? sampler_kernel<true, false, 4, 2> : sampler_kernel<false, false, 4, 2>)
                     : (cfg.lcc ? sampler_kernel<true, false, 4, 0> : sampler_kernel<false, false, 4, 0>);
