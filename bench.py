@@ -30,12 +30,18 @@ one handle (--e2e-handles 1 makes it the headline).
 of the reference's algorithm, oracle/) on the host cores with one process per
 core, each sampling a disjoint share of the events on a 10 % cell sample.
 
---sampler learned first trains the proposal network (5e7 momenta of the
-plain sampler from seeds 10..19, Adam on the tensor cores, reported apart),
-then times the same steps with the learned proposal (gpu_sampler = 1,
-alpha = 0.8) and reports its acceptance against the plain sampler's on the
-same species, the network's tensor-core throughput, and two-sample
-chi-square / KS p-values of pT, y, phi and v2 against the plain sampler.
+The default line also carries the metric's second arm, `learned`: the
+proposal network is trained on the same surface (5e7 momenta of the plain
+sampler from seeds 10..19, Adam on the tensor cores, untimed), then W + K
+generates with the learned proposal (gpu_sampler = 1, alpha = 0.8, exact
+rejection) are timed like the plain steps.  It reports the learned
+hadrons/s and its ratio to the plain arm, proposals per hadron (with and
+without the network, and with the pilot envelope alone), the excess
+branch's share, violations (none by construction), the network's
+tensor-core throughput, and two-sample chi-square / KS p-values of pT, y,
+phi and v2 of the learned species against the plain sampler on 1,000
+events.  --no-learned skips it; --sampler learned makes the learned arm
+the headline `value`.
 """
 from __future__ import annotations
 
@@ -213,6 +219,9 @@ def dist_setup():
 # ---------------------------------------------------------------------------
 # CPU (oracle) leg
 
+_CPU_SURF: dict = {}
+
+
 def cpu_worker(args):
     """One process: the reference's sampling algorithm (oracle part 3:
     per-species yields, Poisson counts, cell draws from the cumulative
@@ -223,9 +232,12 @@ def cpu_worker(args):
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib as O
     from iss_gb300 import surfaces as S
-    surf = S.viscous_3d(N_CELLS, seed=SEED_SURFACE)
-    rec = surf.records[:: max(1, N_CELLS // n_sample)][:n_sample]
-    fo = S.music_to_fo_surf(rec, 2)
+    # the synthetic surface is built once per process (not timed)
+    if _CPU_SURF.get("n") != n_sample:
+        surf = S.viscous_3d(N_CELLS, seed=SEED_SURFACE)
+        rec = surf.records[:: max(1, N_CELLS // n_sample)][:n_sample]
+        _CPU_SURF.update(n=n_sample, fo=S.music_to_fo_surf(rec, 2))
+    fo = _CPU_SURF["fo"]
     params = dict(S.DEFAULT_PARAMETERS, **PARAMS)
     t0 = time.perf_counter()
     lrf, keep = O.lrf_cells(fo)
@@ -235,13 +247,15 @@ def cpu_worker(args):
     return int(n), time.perf_counter() - t0
 
 
-def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int):
+def cpu_baseline(n_procs: int, n_sample: int, n_events: int, seed: int, pool=None):
     import multiprocessing as mp
     per = [n_events // n_procs + (1 if k < n_events % n_procs else 0) for k in range(n_procs)]
     offs = np.concatenate([[0], np.cumsum(per)[:-1]])
     jobs = [(n_sample, per[k], int(offs[k]), seed) for k in range(n_procs) if per[k] > 0]
     if len(jobs) == 1:
         res = [cpu_worker(jobs[0])]
+    elif pool is not None:
+        res = pool.map(cpu_worker, jobs, chunksize=1)
     else:
         with mp.get_context("spawn").Pool(len(jobs)) as pool:
             res = pool.map(cpu_worker, jobs)
@@ -257,25 +271,32 @@ def run_reference(args, ws, rank):
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib
     oracle_lib.lib()
+    import multiprocessing as mp
     n_procs = max(1, os.cpu_count() or 1)
-    n_sample = args.cpu_cells
+    n_sample = args.ref_cells
     rates = []
-    for step in range(args.warmup + args.steps):
-        h, wall = cpu_baseline(n_procs, n_sample, N_EVENTS, seed=1000 + step)
-        if step >= args.warmup:
-            rates.append((h, wall))
+    # one process per core for the whole run; each builds the surface once
+    with mp.get_context("spawn").Pool(n_procs) as pool:
+        for step in range(args.warmup + args.steps):
+            h, wall = cpu_baseline(n_procs, n_sample, N_EVENTS, seed=1000 + step, pool=pool)
+            if step >= args.warmup:
+                rates.append((h, wall))
     had = sum(r[0] for r in rates)
     sec = sum(r[1] for r in rates)
     value = had / sec
-    sample = (f"viscous 3+1D surface, every {N_CELLS // n_sample}th cell ({n_sample} cells), "
-              f"{N_EVENTS} events split over {n_procs} processes")
+    sample = ((f"viscous 3+1D surface, all {N_CELLS} cells" if n_sample >= N_CELLS else
+               f"viscous 3+1D surface, every {N_CELLS // n_sample}th cell ({n_sample} cells)") +
+              f", {N_EVENTS} events split over {n_procs} processes (each process computes the "
+              f"yields of its cells as one reference run does, then samples its events)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "viscous_3d_200k_cells_s95p_1000_events (CPU cell sample)",
+            "config": {"workload": ("viscous_3d_200k_cells_s95p_1000_events" if n_sample >= N_CELLS
+                                    else "viscous_3d_200k_cells_s95p_1000_events (CPU cell sample)"),
                        "cells_sampled": n_sample, "events": N_EVENTS, "species": 319,
-                       "bulk_deltaf_kind": 11, "l2": "n/a (CPU)"},
+                       "bulk_deltaf_kind": 11, "l2": "n/a (CPU)",
+                       "same_config": n_sample >= N_CELLS},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_procs, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -349,47 +370,20 @@ def yields_vs_oracle(s, run_params):
             "worst_species_pid": int(sp["pid"][int(rel.argmax())])}
 
 
-def learned_report(s, timings, args):
-    """Acceptance of the learned proposal against the plain sampler's on the
-    same species (alpha -> 0 with the envelope at 1), the plain sampler's step
-    time, and spectra of the learned species against the plain sampler (100
-    events, same seed, so the counts agree)."""
+def spectra_pvalues(plain, lrn, pids):
+    """Two-sample chi-square / KS p-values of pT, y, phi and v2 (mean cos 2 phi
+    in four pT bins) of each species, learned against plain."""
     from scipy import stats
-    st = s.learned_stats()
-    out = {"species": st["n_species"], "pairs": st["n_pairs"], "ms_network": st["ms_network"],
-           "ms_forward": st["ms_forward"], "tries_per_hadron": st["n_tries"] / max(st["n_hadrons"], 1),
-           "violations_per_try": st["n_violations"] / max(st["n_tries"], 1)}
-    s.set_params(gpu_learned_alpha=1e-4, gpu_learned_safety=1e6)
-    s.generate_samples()
-    st0 = s.learned_stats()
-    out["tries_per_hadron_without_network"] = st0["n_tries"] / max(st0["n_hadrons"], 1)
-    s.set_params(gpu_learned_alpha=0.8, gpu_learned_safety=1.15)
-    s.set_params(gpu_sampler=0)
-    s.generate_samples()
-    out["plain_ms_per_step"] = s.timings()["ms_total"]
-    out["plain_tries_per_hadron_all_species"] = (s.timings()["n_tries"] /
-                                                 max(s.timings()["n_hadrons"], 1))
-    # the same events as the timed steps (so the same species take the
-    # learned proposal); spectra of the first 100 events
-    n_cmp = min(100, int(s.getVal("number_of_repeated_sampling")))
-    s.set_random_seed(99)
-    s.generate_samples()
-    plain, off = s.all_hadrons()
-    plain = plain[:off[n_cmp]]
-    s.set_params(gpu_sampler=1)
-    s.set_random_seed(99)
-    s.generate_samples()
-    lrn, off = s.all_hadrons()
-    lrn = lrn[:off[n_cmp]]
     pv = {}
-    for pid in (211, -211, 111, 321, -321, 2212):
+    for pid in pids:
         a, b = plain[plain["pid"] == pid], lrn[lrn["pid"] == pid]
         if len(a) < 1000:
             continue
         obs = []
         for h in (a, b):
             pt = np.hypot(h["px"], h["py"]).astype(np.float64)
-            y = 0.5 * np.log((h["E"].astype(np.float64) + h["pz"]) / (h["E"].astype(np.float64) - h["pz"]))
+            E, pz = h["E"].astype(np.float64), h["pz"].astype(np.float64)
+            y = 0.5 * np.log((E + pz) / (E - pz))
             ph = np.arctan2(h["py"], h["px"]).astype(np.float64)
             obs.append((pt, y, ph))
         (pa, ya, fa), (pb, yb, fb) = obs
@@ -406,9 +400,110 @@ def learned_report(s, timings, args):
             if len(ca) > 100 and len(cb) > 100:
                 zs.append((ca.mean() - cb.mean()) / np.sqrt(ca.var() / len(ca) + cb.var() / len(cb)))
         pv[f"{pid}_v2_chi2"] = float(stats.chi2.sf(np.sum(np.square(zs)), len(zs))) if zs else 1.0
-    out["spectra_vs_plain"] = {"events": n_cmp, "min_p": min(pv.values()) if pv else None,
-                               "tests": len(pv), "p_values": pv}
+    return pv
+
+
+def learned_train(s, args):
+    """Trains the proposal network on the handle's surface (plain-sampler
+    momenta from seeds 10..19, Adam on the tensor cores); untimed."""
+    t0 = time.perf_counter()
+    curve = s.learned_train(n_momenta=args.train_momenta, first_seed=10, n_seeds=10,
+                            n_steps=args.train_steps, batch=8192, learning_rate=2e-3,
+                            init_seed=1)
+    t_train = time.perf_counter() - t0
+    st = s.learned_stats()
+    return {"train_momenta": st["n_train_rows"], "train_steps": args.train_steps,
+            "train_batch": 8192, "train_s_total": t_train,
+            "train_ms_adam_steps": st["ms_train"],
+            "loss_first": float(curve[:20].mean()), "loss_last": float(curve[-100:].mean()),
+            "nll_plain_proposal": st["train_nll_plain"]}
+
+
+def learned_timed(s, args, flush, plain_value):
+    """The learned arm of the metric on the same surface and events: W + K
+    generates with gpu_sampler = 1 (alpha = 0.8, exact mode), timed like the
+    plain arm (device time, L2 flushed between steps)."""
+    import torch
+    s.set_params(gpu_sampler=1, gpu_learned_alpha=0.8, gpu_learned_exact=1)
+    s.set_random_seed(20261203)
+    for _ in range(args.warmup):
+        s.generate_samples()
+    ms, had, ltries, lhad, viol, exc_t, exc_h, over = [], [], 0, 0, 0, 0, 0, 0
+    net_ms, fwd_ms, samp_ms = 0.0, 0.0, 0.0
+    tries = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s.generate_samples()
+        t, st = s.timings(), s.learned_stats()
+        ms.append(t["ms_total"])
+        had.append(t["n_hadrons"])
+        tries += t["n_tries"]
+        ltries += st["n_tries"]
+        lhad += st["n_hadrons"]
+        viol += st["n_violations"]
+        exc_t += st["n_excess_tries"]
+        exc_h += st["n_excess_hadrons"]
+        over += st["n_over_one"]
+        net_ms += st["ms_network"] / args.steps
+        fwd_ms += st["ms_forward"] / args.steps
+        samp_ms += t["ms_sample"] / args.steps
+    value = sum(had) / (sum(ms) * 1e-3)
+    return {"value": value, "unit": UNIT, "ms_per_step": sum(ms) / args.steps,
+            "learned_over_plain": value / plain_value,
+            "exact": True, "alpha": 0.8,
+            "species": st["n_species"], "pairs": st["n_pairs"],
+            "ms_network": net_ms, "ms_forward": fwd_ms, "ms_sample": samp_ms,
+            "tries_per_hadron_learned_species": ltries / max(lhad, 1),
+            "tries_per_hadron_all_species": tries / max(sum(had), 1),
+            "violations": viol,
+            "excess_branch_share_of_tries": exc_t / max(ltries, 1),
+            "excess_branch_hadrons": exc_h,
+            "mixture_ratios_above_one_per_try": over / max(ltries, 1)}
+
+
+def learned_report(s, args):
+    """What the network changes, on the same species: proposals per hadron
+    without the network (alpha -> 0, every envelope at its cap: the plain
+    sampler's acceptance) and with the pilot envelope alone (gpu_learned_exact
+    = 0, inexact: ratios above 1 counted); then spectra of the learned
+    species against the plain sampler on the same events (same seed, so the
+    counts agree) over n_cmp events."""
+    out = {}
+    s.set_params(gpu_sampler=1, gpu_learned_alpha=1e-4, gpu_learned_safety=1e6, gpu_learned_exact=1)
+    s.generate_samples()
+    st0 = s.learned_stats()
+    out["tries_per_hadron_without_network"] = st0["n_tries"] / max(st0["n_hadrons"], 1)
+    s.set_params(gpu_learned_alpha=0.8, gpu_learned_safety=1.15, gpu_learned_exact=0)
+    s.generate_samples()
+    st1 = s.learned_stats()
+    out["pilot_envelope_only"] = {"tries_per_hadron": st1["n_tries"] / max(st1["n_hadrons"], 1),
+                                  "ratios_above_one_per_try": st1["n_violations"] / max(st1["n_tries"], 1),
+                                  "ms_per_step": s.timings()["ms_total"]}
+    s.set_params(gpu_learned_exact=1, gpu_sampler=0)
+    n_ev = int(s.getVal("number_of_repeated_sampling"))
+    n_cmp = min(args.spectra_events, n_ev)
+    s.set_random_seed(99)
+    s.generate_samples()
+    plain, off = s.all_hadrons()
+    plain = plain[:off[n_cmp]].copy()
     s.set_params(gpu_sampler=1)
+    s.set_random_seed(99)
+    s.generate_samples()
+    st = s.learned_stats()
+    lrn, off = s.all_hadrons()
+    lrn = lrn[:off[n_cmp]]
+    assert len(lrn) == len(plain)
+    # the learned species: the most abundant ones (the pair tables take the
+    # species with enough hadrons per cell)
+    pid_order = s.species()[np.argsort(-s.species_yields())]
+    pv = spectra_pvalues(plain, lrn, [int(q) for q in pid_order[:min(st["n_species"], 6)]])
+    del plain, lrn
+    vals = list(pv.values())
+    out["spectra_vs_plain"] = {"events": n_cmp, "tests": len(pv), "min_p": min(vals) if vals else None,
+                               "below_0.01": int(sum(v < 0.01 for v in vals)),
+                               "expected_below_0.01": 0.01 * len(vals), "p_values": pv}
+    s.set_params(gpu_sampler=0)
     return out
 
 
@@ -505,18 +600,8 @@ def run_gpu(args, ws, rank, local):
     s.set_random_seed(20261203)
     learned = None
     if args.sampler == "learned":
-        t0 = time.perf_counter()
-        curve = s.learned_train(n_momenta=args.train_momenta, first_seed=10, n_seeds=10,
-                                n_steps=args.train_steps, batch=8192, learning_rate=2e-3,
-                                init_seed=1)
-        t_train = time.perf_counter() - t0
-        st = s.learned_stats()
-        learned = {"train_momenta": st["n_train_rows"], "train_steps": args.train_steps,
-                   "train_batch": 8192, "train_s_total": t_train,
-                   "train_ms_adam_steps": st["ms_train"],
-                   "loss_first": float(curve[:20].mean()), "loss_last": float(curve[-100:].mean()),
-                   "nll_plain_proposal": st["train_nll_plain"]}
-        s.set_params(gpu_sampler=1, gpu_learned_alpha=0.8)
+        learned = learned_train(s, args)
+        s.set_params(gpu_sampler=1, gpu_learned_alpha=0.8, gpu_learned_exact=1)
         s.set_random_seed(20261203)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     tuning = None
@@ -549,11 +634,17 @@ def run_gpu(args, ws, rank, local):
     dev_ms, hadrons, t_sample, t_yields = [], [], [], []
     phases = {k: 0.0 for k in ("ms_prologue", "ms_yields", "ms_cdf", "ms_counts", "ms_sample")}
     wall0 = time.perf_counter()
+    step_wall, gen_wall = [], []
     for _ in range(args.steps):
+        ta = time.perf_counter()
         flush.zero_()
         torch.cuda.synchronize()
+        tb = time.perf_counter()
         s.generate_samples()
+        tc = time.perf_counter()
         t = s.timings()
+        step_wall.append(1e3 * (time.perf_counter() - ta))
+        gen_wall.append(1e3 * (tc - tb))
         # with --decays a step also includes the decays (and counts final hadrons)
         dev_ms.append(t["ms_total"] + (t["ms_decays"] if args.decays else 0.0))
         hadrons.append(t["n_hadrons"])
@@ -644,8 +735,31 @@ def run_gpu(args, ws, rank, local):
                 print(e2e_note, file=sys.stderr)
             barrier()
 
+    local_value = sum(hadrons) / (sum(dev_ms) * 1e-3)
     if learned is not None:
-        learned.update(learned_report(s, timings, args))
+        # --sampler learned: the headline was the learned arm; the plain arm
+        # is timed the same way for the ratio
+        s.set_params(gpu_sampler=0)
+        s.set_random_seed(20261203)
+        p_ms, p_had = [], []
+        for _ in range(args.warmup + args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            s.generate_samples()
+            p_ms.append(s.timings()["ms_total"])
+            p_had.append(s.timings()["n_hadrons"])
+        plain_value = sum(p_had[args.warmup:]) / (sum(p_ms[args.warmup:]) * 1e-3)
+        learned.update(learned_timed(s, args, flush, plain_value))
+        learned["plain_value"] = plain_value
+        learned.update(learned_report(s, args))
+    elif (args.learned_arm and args.workload == "viscous" and args.mc_sampling == 4
+          and not args.decays):
+        # the metric's second arm, on the same surface and events
+        learned = learned_train(s, args)
+        learned.update(learned_timed(s, args, flush, local_value))
+        learned["plain_value"] = local_value
+        learned.update(learned_report(s, args))
+        s.set_params(gpu_sampler=0)
     yields_check = None
     if rank == 0 and args.workload == "viscous" and args.cells == N_CELLS and not args.no_oracle_check:
         s.set_params(gpu_sampler=0)
@@ -717,7 +831,15 @@ def run_gpu(args, ws, rank, local):
                            "graph_replay": bool(args.graph), "launch_shape": tuning,
                            "parallelism": f"event shards x{ws}",
                            "l2": "256 MB buffer written between steps; working set > L2",
-                           "wall_s_timed": wall},
+                           "wall_s_timed": wall,
+                           # host clock per step (flush + generate + timings read-out)
+                           # and inside iss_gpu_generate alone, against ms_per_step
+                           "host_ms_per_step": {"min": min(step_wall),
+                                                "median": statistics.median(step_wall),
+                                                "max": max(step_wall)},
+                           "host_ms_generate": {"min": min(gen_wall),
+                                                "median": statistics.median(gen_wall),
+                                                "max": max(gen_wall)}},
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": ({"value": e2e_h / e2e_sec, "unit": UNIT,
                          "h2d_bytes_per_step": e2e[2], "d2h_bytes_per_step": e2e[3],
@@ -773,7 +895,10 @@ def main():
     ap.add_argument("--cells", type=int, default=None,
                     help="surface size (profiling runs use a smaller surface)")
     ap.add_argument("--surfaces", type=int, default=256, help="surfaces of --workload batched")
-    ap.add_argument("--cpu-cells", type=int, default=20_000)
+    ap.add_argument("--cpu-cells", type=int, default=20_000,
+                    help="cells of the one-core cpu_baseline sample in the GPU line")
+    ap.add_argument("--ref-cells", type=int, default=N_CELLS,
+                    help="cells of --impl reference (default: the whole surface)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-handles", type=int, choices=[1, 2, 3, 4], default=2,
@@ -796,6 +921,11 @@ def main():
                          "(bulk delta f kind 1)")
     ap.add_argument("--sampler", choices=["plain", "learned"], default="plain",
                     help="learned: train the proposal network first, then sample with it")
+    ap.add_argument("--no-learned", dest="learned_arm", action="store_false",
+                    help="skip the learned arm of the default line (training, timed steps with "
+                         "gpu_sampler = 1, spectra against the plain sampler)")
+    ap.add_argument("--spectra-events", type=int, default=1000,
+                    help="events of the learned-vs-plain spectra comparison")
     ap.add_argument("--train-momenta", type=int, default=50_000_000)
     ap.add_argument("--train-steps", type=int, default=3000)
     args = ap.parse_args()

@@ -203,6 +203,18 @@ iss_status iss_gpu_copy_all(iss_handle* h, iss_hadron_t* out, int64_t capacity,
  * the current directory: OSCAR.DAT, particle_samples.gz, particle_samples.bin). */
 iss_status iss_gpu_write_output(iss_handle* h, int format, const char* filename);
 
+/* The same writers on a caller's host hadron list (no device work, no
+ * handle): FSSW::combine_samples_to_OSCAR / _gzip_file / _binary_file
+ * (src/FSSW.cpp:365-561) applied to events [event_offsets[i],
+ * event_offsets[i+1]) of `hadrons`, i < n_events.  For example the
+ * concatenated hadrons of event shards sampled on several GPUs.  The OSCAR
+ * header is read from <table_path>/OSCAR_header.txt, as the reference reads
+ * it (src/FSSW.cpp:164); table_path NULL means "iSS_tables".  filename NULL
+ * takes the reference's default name. */
+iss_status iss_gpu_write_hadron_list(int format, const char* filename, const char* table_path,
+                                     const iss_hadron_t* hadrons, const int64_t* event_offsets,
+                                     int32_t n_events);
+
 /* ---- inspection (parity tests, run reports) ---------------------------- */
 
 /* Number of chosen species and their PDG ids in the sampler's mass-sorted
@@ -334,11 +346,20 @@ iss_status iss_gpu_learned_train(iss_handle* h, const iss_learned_train_t* optio
  * expected hadrons per cell over all events reach
  * gpu_learned_min_hadrons_per_cell (default 1) are proposed from
  * gpu_learned_alpha (default 0.8) x network mixture + (1 - alpha) x the
- * plain proposal; the others keep the plain sampler.  The accept step keeps
- * the plain sampler's target: P a / (M q), with M per (species, cell) from
- * gpu_learned_pilot (default 64) pilot proposals times gpu_learned_safety
- * (default 1.15), capped by 1 / (1 - alpha).  A proposal whose ratio exceeds
- * 1 is counted as a violation. */
+ * plain proposal q_P; the others keep the plain sampler.  M per (species,
+ * cell) is gpu_learned_safety (default 1.15) times the largest ratio
+ * P a / q over gpu_learned_pilot (default 64) pilot proposals, capped by
+ * 1 / (1 - alpha).  Target: the plain sampler's P a (a <= 1 its acceptance).
+ *   gpu_learned_exact = 1 (default): exact rejection for every M.  A try is
+ *     the mixture branch with probability M / (M + c): x from q, accepted
+ *     with min(1, P a / (M q)); else the excess branch: x from the plain
+ *     proposal, accepted with (P a - M q) / (c P), c = 1 - M (1 - alpha)
+ *     (plus a rounding margin) >= sup (a - M q / P).  The accepted density
+ *     is min(P a, M q) + (P a - M q)+ = P a whatever M is.  n_violations
+ *     counts excess-branch ratios above 1 (none by construction).
+ *   gpu_learned_exact = 0: the mixture branch alone; ratios above 1 are
+ *     accepted and counted as violations (the output is then the target
+ *     only where M q >= P a). */
 typedef struct iss_learned_stats {
     int32_t n_species;       /* species sampled with the learned proposal   */
     int64_t n_pairs;         /* (species, cell) pairs evaluated by the network */
@@ -352,6 +373,10 @@ typedef struct iss_learned_stats {
     double train_nll_plain;  /* mean -ln P of the training rows under the plain proposal
                                 (same units as the network's loss) */
     double ms_forward;       /* the network's forward pass alone (part of ms_network) */
+    int64_t n_excess_tries;  /* exact mode: proposals of the excess branch (in n_tries) */
+    int64_t n_excess_hadrons;/* exact mode: hadrons accepted by the excess branch      */
+    int64_t n_over_one;      /* exact mode: mixture-branch ratios above 1 (their
+                                missing mass is what the excess branch supplies) */
 } iss_learned_stats_t;
 iss_status iss_gpu_learned_stats(iss_handle* h, iss_learned_stats_t* out);
 /* Training rows first .. first + count - 1 of the last training: features
@@ -385,8 +410,15 @@ iss_status iss_gpu_mma_selftest(const uint16_t* a, const uint16_t* b, int32_t n,
  *   - Nothing has to be zeroed before the call.
  *   - The fixed array is shared by all calls on one device.  Calls on one
  *     device must not overlap in time; issue them on one stream.
- *   - The first call on each device looks up the array's address.  Make that
- *     call before starting any stream capture on that device. */
+ *   - Counts must be >= 0; negative counts give wrong offsets (not checked).
+ *   - The first call on each device looks up the array's address.  With
+ *     CUDA's lazy module loading (the default) that lookup loads the module
+ *     holding the array, which takes its 128 KiB of device memory then.  So
+ *     make the first call on a device before a memory pool claims that
+ *     device's memory, and before starting any stream capture on it.  Later
+ *     calls allocate nothing.
+ *   - A CUDA error that earlier work left pending makes the call return
+ *     ISS_ERR_CUDA without launching anything; that error stays pending. */
 #define ISS_GPU_NOALLOC_SCAN_MAX_SEGMENTS ((int64_t)16384 * 4096)
 iss_status iss_gpu_scan_counts_noalloc(const int32_t* d_counts, int64_t n,
                                        int64_t* d_offsets, void* stream);

@@ -389,6 +389,11 @@ iss_status prepare(iss_handle* h) {
         if (h->use_learned && !(alpha > 0.0 && alpha < 1.0))
             return fail(h, ISS_ERR_INVALID_ARG, "gpu_learned_alpha = %g must lie in (0, 1)", alpha);
         c.lalpha = static_cast<float>(alpha);
+        const int exact = static_cast<int>(h->params.get_or("gpu_learned_exact", 1));
+        if (exact != 0 && exact != 1)
+            return fail(h, ISS_ERR_INVALID_ARG, "gpu_learned_exact = %d (1: exact, 0: pilot envelope)",
+                        exact);
+        c.lexact = exact;
         c.lslot = nullptr;
         c.lpairs = nullptr;
     }
@@ -1317,6 +1322,9 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
         h->lstats.n_tries = static_cast<int64_t>(ctr.learned_tries);
         h->lstats.n_hadrons = static_cast<int64_t>(ctr.learned_hadrons);
         h->lstats.n_violations = static_cast<int64_t>(ctr.learned_violations);
+        h->lstats.n_excess_tries = static_cast<int64_t>(ctr.learned_excess_tries);
+        h->lstats.n_excess_hadrons = static_cast<int64_t>(ctr.learned_excess_hadrons);
+        h->lstats.n_over_one = static_cast<int64_t>(ctr.learned_over_one);
         h->lstats.ms_network = elapsed(h, kEvLearnStart, kEvLearnEnd);
         h->lstats.ms_forward = elapsed(h, kEvFwdStart, kEvFwdEnd);
     }
@@ -1895,6 +1903,31 @@ iss_status iss_gpu_write_output(iss_handle* h, int format, const char* filename)
         return fail(h, ISS_ERR_INVALID_ARG, "unknown output format %d", format);
     }
     return ok ? ISS_OK : fail(h, ISS_ERR_IO, "%s", err.c_str());
+}
+
+iss_status iss_gpu_write_hadron_list(int format, const char* filename, const char* table_path,
+                                     const iss_hadron_t* hadrons, const int64_t* event_offsets,
+                                     int32_t n_events) {
+    if (n_events < 0 || !event_offsets || (event_offsets[n_events] > 0 && !hadrons))
+        return ISS_ERR_INVALID_ARG;
+    for (int32_t e = 0; e < n_events; e++)
+        if (event_offsets[e + 1] < event_offsets[e] || event_offsets[e] < 0) return ISS_ERR_INVALID_ARG;
+    const std::string tables = table_path ? table_path : "iSS_tables";
+    std::string err;
+    bool ok = false;
+    if (format == ISS_OUTPUT_OSCAR) {
+        ok = write_oscar(filename ? filename : "OSCAR.DAT", tables + "/OSCAR_header.txt", hadrons,
+                         event_offsets, n_events, &err);
+    } else if (format == ISS_OUTPUT_GZIP) {
+        ok = write_gzip(filename ? filename : "particle_samples.gz", hadrons, event_offsets, n_events,
+                        &err);
+    } else if (format == ISS_OUTPUT_BINARY) {
+        ok = write_binary(filename ? filename : "particle_samples.bin", hadrons, event_offsets,
+                          n_events, &err);
+    } else {
+        return ISS_ERR_INVALID_ARG;
+    }
+    return ok ? ISS_OK : ISS_ERR_IO;
 }
 
 iss_status iss_gpu_species(iss_handle* h, int32_t* n_species, int32_t* pids, int32_t capacity) {

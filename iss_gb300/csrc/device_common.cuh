@@ -67,6 +67,9 @@ struct DevConfig {
     const int32_t* lslot;
     const float* lpairs;
     float lalpha;
+    // 1: exact rejection (the mixture with an excess branch, try_learned);
+    // 0: the pilot envelope alone, whose ratios above 1 are counted
+    int lexact;
     // launch shape (results do not depend on it; the autotuner picks it)
     int item_size;       // draws per sampler work item (multiple of 32, <= 1024)
     int yield_groups;    // species groups per cell in the yields kernel (grid y)
@@ -160,6 +163,9 @@ struct SampleCounters {
     unsigned long long learned_tries;       // proposals of the learned sampler
     unsigned long long learned_violations;  // of these, ratios above the envelope M
     unsigned long long learned_hadrons;     // hadrons of species in the pair tables
+    unsigned long long learned_excess_tries;    // exact mode: proposals of the excess branch
+    unsigned long long learned_excess_hadrons;  // exact mode: hadrons accepted there
+    unsigned long long learned_over_one;        // exact mode: mixture-branch ratios above 1
     int error_code;          // 1: m/T - mu/T off the momentum tables
     int error_species;
 };

@@ -1080,13 +1080,14 @@ __device__ __forceinline__ void around(float mx, float my, float mz, float c, fl
     nz = c * mz + s * (cphi * ez + sphi * fz);
 }
 
-// one proposal from q = alpha Q + (1 - alpha) P, from the uniforms of A and
-// B (A.x selects the component of q); false when it falls outside the support
+// one proposal from the network's mixture Q (from_q) or from the plain
+// proposal P, from the uniforms A.y .. B.z (A.x and B.w are the caller's);
+// false when it falls outside the support
 template <bool kShared = false>
 __device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __restrict__ lp,
-                                                float alpha, const uint4& A, const uint4& B,
+                                                bool from_q, const uint4& A, const uint4& B,
                                                 float& K, float& nx, float& ny, float& nz) {
-    if (u01f(A.x) < alpha) {
+    if (from_q) {
         const float uc = u01f(A.y);
         int k = 0;
         while (k < 7 && uc >= rec1<kShared>(lp, 8 * k)) k++;
@@ -1130,21 +1131,58 @@ __device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __re
     return true;
 }
 
-// one learned proposal and its accept step
+// excess-branch bound c >= sup (a - M q / P) = 1 - M (1 - alpha), since
+// a <= 1 and q / P >= 1 - alpha; the margin covers the FP32 rounding of a
+constexpr float kExcessMargin = 1e-4f;
+__device__ __forceinline__ float excess_bound(float M, float alpha) {
+    return fmaxf(0.0f, 1.0f + kExcessMargin - M * (1.0f - alpha));
+}
+
+// One learned proposal and its accept step, for the target t = P a of the
+// plain sampler and the envelope E = M q, q = alpha Q + (1 - alpha) P.
+// Exact mode (cfg.lexact): with probability M / (M + c) the mixture branch
+// (x from q, accepted with min(1, t / E)), else the excess branch (x from P,
+// accepted with (t - E) / (c P), c = excess_bound).  Accepted density per
+// try: [min(t, E) + (t - E)+] / (M + c) = t / (M + c), for any M: exact
+// rejection whatever the envelope's quality.  A ratio above 1 in the
+// mixture branch is then not an error: the excess branch supplies the mass
+// min() drops there (counted in over_one); an excess-branch ratio above 1
+// would mean c < sup (a - M q / P), and is counted as a violation.
+// Without lexact: the mixture branch alone, ratios above 1 counted.
+struct LearnedTryStats {
+    unsigned viol = 0, excess_tries = 0, excess_hadrons = 0, over_one = 0;
+};
 __device__ __forceinline__ bool try_learned(const DevConfig& cfg, const Prop& p, const Unit& u,
                                             const float* __restrict__ lp, float4& pl, float& u_rap,
-                                            unsigned& violations) {
+                                            LearnedTryStats& ls) {
     const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagLearn << 16);
     const uint4 A = block(2u * u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
     const uint4 B = block(2u * u.t + 1u, u.i, u.eg, c3, cfg.key0, cfg.key1);
+    const float M = __ldg(lp + 56);
+    const float alpha = cfg.lalpha;
+    const float c = cfg.lexact ? excess_bound(M, alpha) : 0.0f;
+    // one uniform picks the branch and, within the mixture branch, Q or P
+    const float sel = u01f(A.x) * (M + c);
+    const bool excess = sel < c;
+    const bool from_q = !excess && (sel - c) < alpha * M;
+    ls.excess_tries += excess;
     float K, nx, ny, nz, P, a;
-    if (!propose_mixture(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) return false;
+    if (!propose_mixture(p, lp, from_q, A, B, K, nx, ny, nz)) return false;
     if (!plain_target(cfg, p, K, nx, ny, nz, P, a, pl)) return false;
     const float Q = learned_density(lp, K, nx, ny, nz);
-    const float M = __ldg(lp + 56);
-    const float r = P * a / (M * (cfg.lalpha * Q + (1.0f - cfg.lalpha) * P));
-    if (r > 1.0f) violations++;
+    const float E = M * (alpha * Q + (1.0f - alpha) * P);
+    float r;
+    if (excess) {
+        r = (P * a - E) / (c * P);
+        if (r > 1.0f) ls.viol++;
+    } else {
+        r = P * a / E;
+        if (r > 1.0f) {
+            if (cfg.lexact) ls.over_one++; else ls.viol++;
+        }
+    }
     if (!(u01f(B.w) < r)) return false;
+    ls.excess_hadrons += excess;
     u_rap = 0.0f;
     if (cfg.hydro_mode != 2) {
         const uint4 C = block(u.t, u.i, u.eg, static_cast<uint32_t>(u.s) | (kTagLearnRap << 16),
@@ -1407,7 +1445,8 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
     // per-thread counts (a thread makes far fewer than 2^32 tries in a launch)
     unsigned n_tries = 0, n_redraws = 0, n_fail = 0;
     unsigned n_viol = 0;
-    unsigned n_ltries = 0, n_lviol = 0, n_lhad = 0;
+    unsigned n_ltries = 0, n_lhad = 0;
+    LearnedTryStats lts;
 
     for (;;) {
         // hand out units to the lanes that have none
@@ -1515,7 +1554,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
             bool ok;
             if constexpr (kLearned) {
                 if (u.lp) {
-                    ok = try_learned(cfg, p, u, u.lp, pl, u_rap, n_lviol);
+                    ok = try_learned(cfg, p, u, u.lp, pl, u_rap, lts);
                     n_ltries++;
                     n_lhad += ok;
                 } else {
@@ -1571,8 +1610,11 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
         n_viol += __shfl_down_sync(FULL, n_viol, o);
         if (kLearned) {
             n_ltries += __shfl_down_sync(FULL, n_ltries, o);
-            n_lviol += __shfl_down_sync(FULL, n_lviol, o);
             n_lhad += __shfl_down_sync(FULL, n_lhad, o);
+            lts.viol += __shfl_down_sync(FULL, lts.viol, o);
+            lts.excess_tries += __shfl_down_sync(FULL, lts.excess_tries, o);
+            lts.excess_hadrons += __shfl_down_sync(FULL, lts.excess_hadrons, o);
+            lts.over_one += __shfl_down_sync(FULL, lts.over_one, o);
         }
     }
     if (lane == 0) {
@@ -1582,7 +1624,14 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
         if (n_viol) atomicAdd(&ctrs->bound_violations, static_cast<unsigned long long>(n_viol));
         if (kLearned) {
             if (n_ltries) atomicAdd(&ctrs->learned_tries, static_cast<unsigned long long>(n_ltries));
-            if (n_lviol) atomicAdd(&ctrs->learned_violations, static_cast<unsigned long long>(n_lviol));
+            if (lts.viol) atomicAdd(&ctrs->learned_violations, static_cast<unsigned long long>(lts.viol));
+            if (lts.excess_tries)
+                atomicAdd(&ctrs->learned_excess_tries, static_cast<unsigned long long>(lts.excess_tries));
+            if (lts.excess_hadrons)
+                atomicAdd(&ctrs->learned_excess_hadrons,
+                          static_cast<unsigned long long>(lts.excess_hadrons));
+            if (lts.over_one)
+                atomicAdd(&ctrs->learned_over_one, static_cast<unsigned long long>(lts.over_one));
             if (n_lhad) atomicAdd(&ctrs->learned_hadrons, static_cast<unsigned long long>(n_lhad));
         }
     }
@@ -1694,7 +1743,7 @@ __global__ void learned_pair_envelope_kernel(DevConfig cfg, CellArrays cells,
             const uint4 B = block(2u * j + 1u, static_cast<uint32_t>(q), 0u, c3, cfg.key0, cfg.key1);
             float K, nx, ny, nz, P, a;
             float4 pl;
-            if (!propose_mixture<true>(p, lp, cfg.lalpha, A, B, K, nx, ny, nz)) continue;
+            if (!propose_mixture<true>(p, lp, u01f(A.x) < cfg.lalpha, A, B, K, nx, ny, nz)) continue;
             if (!plain_target(cfg, p, K, nx, ny, nz, P, a, pl)) continue;
             const float Q = learned_density<true>(lp, K, nx, ny, nz);
             const float r = P * a / (cfg.lalpha * Q + (1.0f - cfg.lalpha) * P);

@@ -22,8 +22,17 @@
 //     at the same time on one device race on it: calls on one device must be
 //     ordered, for example by issuing them on one stream.
 //   * The scratch address is looked up once per device, on the first call
-//     made on that device.  That first call may load the module.  It must
-//     therefore come before any stream capture on that device.
+//     made on that device.  Under CUDA's lazy module loading (the default)
+//     that first call loads the module holding the array, and loading it
+//     takes the array's 128 KiB of device memory then.  So the first call on
+//     a device must come before a memory pool claims that device's memory,
+//     and before any stream capture on that device.  Later calls allocate
+//     nothing.
+//   * Counts must be >= 0; negative counts give wrong offsets (not checked).
+//   * A CUDA error that earlier work left pending makes the call return
+//     ISS_ERR_CUDA before it launches anything; that error stays pending for
+//     its owner.  An error of this call's own launches is cleared and
+//     reported as ISS_ERR_CUDA.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -66,6 +75,9 @@ extern "C" iss_status iss_gpu_scan_counts_noalloc(const int32_t* d_counts, int64
     if (n < 0 || !d_offsets || (n > 0 && !d_counts)) return ISS_ERR_INVALID_ARG;
     if (n > ISS_GPU_NOALLOC_SCAN_MAX_SEGMENTS || iss::offsets_num_tiles(n) > kScratchTiles)
         return ISS_ERR_CAPACITY;
+    // an error left pending by the caller's earlier work is not ours to
+    // clear, and launching behind it would misreport it as this call's
+    if (cudaPeekAtLastError() != cudaSuccess) return ISS_ERR_CUDA;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();

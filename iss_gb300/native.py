@@ -33,7 +33,8 @@ EXPORTED = [
     "iss_gpu_generate", "iss_gpu_generate_into",
     "iss_gpu_shell",
     "iss_gpu_clear", "iss_gpu_num_events", "iss_gpu_num_particles", "iss_gpu_get_hadron",
-    "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output", "iss_gpu_species",
+    "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output",
+    "iss_gpu_write_hadron_list", "iss_gpu_species",
     "iss_gpu_species_yields", "iss_gpu_num_cells", "iss_gpu_copy_lrf_cells",
     "iss_gpu_copy_cell_yields", "iss_gpu_copy_counts", "iss_gpu_get_timings",
     "iss_gpu_last_error", "iss_gpu_status_string", "iss_gpu_scan_counts_noalloc",
@@ -66,7 +67,8 @@ class LearnedStats(C.Structure):
                 ("n_tries", C.c_int64), ("n_hadrons", C.c_int64), ("n_violations", C.c_int64),
                 ("n_train_rows", C.c_int64), ("ms_train", C.c_double),
                 ("train_events_per_seed", C.c_int32), ("train_nll_plain", C.c_double),
-                ("ms_forward", C.c_double)]
+                ("ms_forward", C.c_double), ("n_excess_tries", C.c_int64),
+                ("n_excess_hadrons", C.c_int64), ("n_over_one", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -119,6 +121,7 @@ def lib():
         L.iss_gpu_copy_event.argtypes = [h, C.c_int32, v, C.c_int64, C.POINTER(C.c_int64)]
         L.iss_gpu_copy_all.argtypes = [h, v, C.c_int64, v, C.POINTER(C.c_int64)]
         L.iss_gpu_write_output.argtypes = [h, C.c_int, C.c_char_p]
+        L.iss_gpu_write_hadron_list.argtypes = [C.c_int, C.c_char_p, C.c_char_p, v, v, C.c_int32]
         L.iss_gpu_species.argtypes = [h, C.POINTER(C.c_int32), v, C.c_int32]
         L.iss_gpu_species_yields.argtypes = [h, v, C.c_int32]
         L.iss_gpu_num_cells.argtypes = [h, C.POINTER(C.c_int64)]
@@ -436,3 +439,16 @@ def mma_selftest(a_bf16, b_bf16):
     if st != ISS_OK:
         raise IssError(st, "tensor-core self-test failed")
     return c
+
+
+def write_hadron_list(fmt, filename, hadrons, event_offsets, table_path=TABLE_DIR):
+    """The reference's output writers (OSCAR / gzip / binary) on a host hadron
+    list: events [event_offsets[i], event_offsets[i+1]) of `hadrons`
+    (HADRON_DTYPE).  No device is needed."""
+    h = np.ascontiguousarray(hadrons, dtype=HADRON_DTYPE)
+    off = np.ascontiguousarray(event_offsets, dtype=np.int64)
+    st = lib().iss_gpu_write_hadron_list(int(fmt), filename.encode(),
+                                         table_path.encode() if table_path else None,
+                                         _ptr(h) if h.size else None, _ptr(off), len(off) - 1)
+    if st != ISS_OK:
+        raise IssError(st, f"iss_gpu_write_hadron_list({fmt}, {filename})")

@@ -7,7 +7,8 @@ species, parameters and number of events, single-threaded on this host.
 
     python oracle/calibrate_cpu_baseline.py [--cells-every 10] [--events 100] [--bulk-kind 1]
 
-Needs the reference tree (ISS_REFERENCE, default /root/reference) for its
+Needs the reference tree (ISS_REFERENCE, default: a directory named
+`reference` beside this repository) for its
 iSS_tables; prints one JSON line."""
 from __future__ import annotations
 

@@ -15,6 +15,14 @@
 //     Runs iSS::shell() (src/iSS.cpp:41-56) and writes every sampled hadron
 //     (iSS_Hadron records, src/data_struct.h:79-84) event by event.
 //
+//   ref_driver write <param_file> <work_dir> <surface_file> <table_path> <in.bin> [key=val ...]
+//     Builds the FSSW sampler as in `yields`, replaces its in-memory hadron
+//     list by the events of <in.bin> (the format `sample` writes) and calls
+//     the reference's three writers on it: FSSW::combine_samples_to_OSCAR,
+//     combine_samples_to_gzip_file and combine_samples_to_binary_file
+//     (src/FSSW.cpp:365-561), which write OSCAR.DAT, particle_samples.gz and
+//     particle_samples.bin into the current directory.
+//
 // The reference keeps the data it computes in private members; this driver
 // reads them by compiling the reference headers with `private` mapped to
 // `public` (the reference sources themselves are compiled unchanged).
@@ -107,6 +115,41 @@ int run_yields(iSS& iss, const std::string& work_dir, const std::string& table_p
     return 0;
 }
 
+int run_write(iSS& iss, const std::string& work_dir, const std::string& table_path,
+              const char* in_name) {
+    iss.read_in_FO_surface();
+    iss.set_random_seed();
+    Table chosen;
+    chosen.loadTableFromFile(table_path + "/chosen_particles_s95p-v1.dat");
+    FSSW sampler(iss.ran_gen_ptr_, &chosen, iss.particle_, iss.FOsurf_LRF_array_,
+                 iss.flag_PCE_, iss.paraRdr_ptr, work_dir, table_path,
+                 iss.afterburner_type_);
+    std::FILE* f = std::fopen(in_name, "rb");
+    if (!f) { std::perror(in_name); return 2; }
+    int32_t magic = 0, nev = 0;
+    if (std::fread(&magic, 4, 1, f) != 1 || magic != 0x48414452 || std::fread(&nev, 4, 1, f) != 1) {
+        std::fprintf(stderr, "ref_driver: %s is not a hadron list\n", in_name);
+        return 2;
+    }
+    for (auto* ev : *sampler.Hadron_list) delete ev;
+    sampler.Hadron_list->clear();
+    for (int iev = 0; iev < nev; iev++) {
+        int32_t n = 0;
+        if (std::fread(&n, 4, 1, f) != 1) return 2;
+        auto* ev = new std::vector<iSS_Hadron>(static_cast<size_t>(n));
+        if (n > 0 && std::fread(ev->data(), sizeof(iSS_Hadron), static_cast<size_t>(n), f) !=
+                         static_cast<size_t>(n))
+            return 2;
+        sampler.Hadron_list->push_back(ev);
+    }
+    std::fclose(f);
+    sampler.flag_store_samples_in_memory = 1;
+    sampler.combine_samples_to_OSCAR();
+    sampler.combine_samples_to_gzip_file();
+    sampler.combine_samples_to_binary_file();
+    return 0;
+}
+
 int run_sample(iSS& iss, const char* out_name) {
     iss.shell();
     std::FILE* f = std::fopen(out_name, "wb");
@@ -128,8 +171,8 @@ int run_sample(iSS& iss, const char* out_name) {
 int main(int argc, char** argv) {
     if (argc < 7) {
         std::fprintf(stderr,
-                     "usage: %s yields|sample <param_file> <work_dir> <surface_file> "
-                     "<table_path> <out.bin> [key=val ...]\n", argv[0]);
+                     "usage: %s yields|sample|write <param_file> <work_dir> <surface_file> "
+                     "<table_path> <out.bin | in.bin> [key=val ...]\n", argv[0]);
         return 1;
     }
     const std::string mode = argv[1];
@@ -142,6 +185,7 @@ int main(int argc, char** argv) {
     iss.paraRdr_ptr->readFromArguments(argc, argv, "#", 7);
     if (mode == "yields") return run_yields(iss, work_dir, table_path, out_name);
     if (mode == "sample") return run_sample(iss, out_name);
+    if (mode == "write") return run_write(iss, work_dir, table_path, out_name);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 1;
 }

@@ -1,7 +1,8 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference tree at /root/reference:
+Run where the reference tree is at $ISS_REFERENCE (default: a directory
+named `reference` beside this repository):
 
     python tests/golden/make_golden.py
 
@@ -13,7 +14,10 @@ It compiles the unmodified reference sources with the recipe in oracle/Makefile
     iSS::read_in_FO_surface and FSSW::calculate_dN_dxtdy_for_one_particle_species,
     and stores species, local-rest-frame cells and per-cell FP64 yields;
   * for the sampling cases, runs ref_driver `sample` (iSS::shell) and stores
-    histograms of the reference's sampled hadrons.
+    histograms of the reference's sampled hadrons;
+  * for the writers, runs ref_driver `write` on a fixed hadron list, which
+    calls the reference's own OSCAR, gzip and binary writers, and stores
+    their files (the gzip file decompressed).
 The GPU tests never read the reference: they only read the .npz files written
 here.
 """
@@ -33,7 +37,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 from iss_gb300 import surfaces as S  # noqa: E402
 
-REF = os.environ.get("ISS_REFERENCE", "/root/reference")
+REF = os.environ.get("ISS_REFERENCE", os.path.normpath(os.path.join(REPO, os.pardir, "reference")))
 REF_TABLES = os.path.join(REF, "iSS_tables")
 DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
 
@@ -173,6 +177,64 @@ def decays_case(visc_params, work_root):
                      randomSeed=15), work_root)
 
 
+def writer_hadrons(seed=31):
+    """A fixed hadron list for the writer fixtures: seven events of 0 to 40
+    hadrons (empty events included) whose fields cover what the formats must
+    carry -- ordinary momenta and positions, signed zeros, denormals, values
+    near the float limits, powers of ten and their neighbours -- and PDG
+    ids of both signs."""
+    rng = np.random.default_rng(seed)
+    counts = [3, 0, 25, 1, 0, 40, 7]
+    dt = np.dtype([("pid", "<i4"), ("mass", "<f4"), ("E", "<f4"), ("px", "<f4"),
+                   ("py", "<f4"), ("pz", "<f4"), ("t", "<f4"), ("x", "<f4"),
+                   ("y", "<f4"), ("z", "<f4")])
+    special = np.array([0.0, -0.0, 1e-40, -3e-42, 3.4028235e38, -1.1754944e-38, 1e-7, 9.999999e-8,
+                        1e16, 9.999999e16, 1e17, 1.0000001e17, 0.1, 1.0 / 3.0, 2.0 ** -149,
+                        123456.79], dtype=np.float32)
+    pids = np.array([211, -211, 111, 321, -321, 2212, -2212, 3122, -3334, 22], dtype=np.int32)
+    events = []
+    k = 0
+    for n in counts:
+        ev = np.zeros(n, dtype=dt)
+        ev["pid"] = pids[rng.integers(0, len(pids), n)]
+        for f in dt.names[1:]:
+            v = (rng.standard_normal(n) * 10.0 ** rng.integers(-3, 4, n)).astype(np.float32)
+            pick = rng.random(n) < 0.25
+            v[pick] = special[(k + np.arange(pick.sum())) % len(special)]
+            k += int(pick.sum())
+            ev[f] = v
+        events.append(ev)
+    return events
+
+
+def writers_case(work_root):
+    """The reference's OSCAR, gzip and binary writers on a fixed hadron list."""
+    import gzip
+    events = writer_hadrons()
+    run = make_run_dir(os.path.join(work_root, "writers"))
+    surf = S.viscous_3d(16, seed=2)
+    S.write_music_binary(os.path.join(run, "work", "surface.dat"), surf.records)
+    S.write_music_input(os.path.join(run, "work"), surf)
+    inp = os.path.join(run, "hadrons_in.bin")
+    with open(inp, "wb") as f:
+        f.write(np.array([0x48414452, len(events)], dtype="<i4").tobytes())
+        for ev in events:
+            f.write(np.array([len(ev)], dtype="<i4").tobytes())
+            f.write(ev.tobytes())
+    run_driver(run, "write", dict(hydro_mode=2, afterburner_type=0), inp)
+    oscar = open(os.path.join(run, "OSCAR.DAT"), "rb").read()
+    gz_text = gzip.open(os.path.join(run, "particle_samples.gz"), "rb").read()
+    binary = open(os.path.join(run, "particle_samples.bin"), "rb").read()
+    off = np.concatenate([[0], np.cumsum([len(e) for e in events])]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "writers_reference.npz"),
+                        hadrons=np.concatenate(events), event_offsets=off,
+                        oscar=np.frombuffer(oscar, dtype=np.uint8),
+                        gzip_text=np.frombuffer(gz_text, dtype=np.uint8),
+                        binary=np.frombuffer(binary, dtype=np.uint8))
+    print(f"writers: {off[-1]} hadrons in {len(events)} events; OSCAR {len(oscar)} B, "
+          f"gzip text {len(gz_text)} B, binary {len(binary)} B")
+
+
 # keys the reference's EmissionFunctionArray path (MC_sampling = 2) reads,
 # with the values of its own iSS_parameters.dat
 EFA_KEYS = dict(MC_sampling=2, restrict_deltaf=1, deltaf_max_ratio=1.0, sample_pT_up_to=-1,
@@ -222,6 +284,12 @@ def main():
         finally:
             shutil.rmtree(work_root, ignore_errors=True)
         return
+    if only == "writers_reference":
+        try:
+            writers_case(work_root)
+        finally:
+            shutil.rmtree(work_root, ignore_errors=True)
+        return
     if only in ("samples_viscous_lcc", "samples_viscous_decays"):
         try:
             (lcc_case if only == "samples_viscous_lcc" else decays_case)(visc_params, work_root)
@@ -261,6 +329,7 @@ def main():
         lcc_case(visc_params, work_root)
         decays_case(visc_params, work_root)
         efa_cases(work_root)
+        writers_case(work_root)
     finally:
         shutil.rmtree(work_root, ignore_errors=True)
 

@@ -328,3 +328,18 @@ def reference_sampler(oc: OracleConfig, sp, lrf, keep, seed=1, capacity=None):
     if n < 0:
         raise RuntimeError(f"orc_reference_sampler status {n}")
     return out[:min(n, cap)], n, sec.value
+
+
+def events_needed(params: dict, sp, yields_fp64):
+    """FSSW::compute_number_of_sampling_needed (src/FSSW.cpp:851-869): the
+    number of events from the thermal pi+ yield (the species whose table
+    index is 1, summed over cells in FP64), number_of_particles_needed and
+    maximum_sampling_events; ten times more for 3+1D surfaces."""
+    p = {k.lower(): v for k, v in params.items()}
+    k = [i for i, s in enumerate(sp) if int(s["idx"]) == 1][0]
+    dn_pion = float(np.sum(yields_fp64[k]))
+    needed = int(float(p["number_of_particles_needed"]))     # the reference's long
+    nev = int(needed / (6.0 * dn_pion))
+    if int(p.get("hydro_mode", 2)) == 2:
+        nev *= 10
+    return max(1, min(int(float(p["maximum_sampling_events"])), nev))

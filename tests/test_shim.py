@@ -1,0 +1,106 @@
+"""The drop-in boundary for C++ callers and the command-line driver.
+
+* tests/shim/caller.cpp is written against the reference's `iSS` class the
+  way the reference's own main program uses it (src/main.cpp:22-74), plus
+  every other public member (src/iSS.h:16-102).  It compiles against the
+  library's header shim/iSS.h and links against libiss_gb300.so unchanged.
+  Without a GPU it must end with the library's ISS_ERR_CUDA status, not a
+  crash; on the GPU it samples the reference's continuous-integration cells.
+* iSS.e (the library's command-line driver, the reference's argv
+  conventions) runs the reference's CI cases (tests/RunAutoTest*.sh of the
+  reference: a one-cell surface, its music_input and parameter file) and
+  passes their check: the mean absolute difference between the cell's
+  T^{mu nu} and the one rebuilt from the samples, checkReconstructedTmunu.dat
+  column 3, is below 1e-3 (tests/TestOutputFiles.py of the reference).
+"""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from iss_gb300 import native
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CI = os.path.join(REPO, "tests", "golden", "ci")
+NATIVE = os.path.join(REPO, "iss_gb300", "_native")
+# the reference's CI cases: (script, music_input, parameter file, surface)
+CASES = [("Viscous1", "music_input_91", "iSS_parameters_CEdeltaf.dat", "testViscousOneFluidCell1.dat"),
+         ("Viscous2", "music_input_9", "iSS_parameters_CEdeltaf.dat", "testViscousOneFluidCell2.dat"),
+         ("Ideal1", "music_input_91", "iSS_parameters_ideal.dat", "testIdealOneFluidCell1.dat"),
+         ("Ideal2", "music_input_9", "iSS_parameters_ideal.dat", "testIdealOneFluidCell2.dat")]
+
+
+@pytest.fixture(scope="module")
+def caller(tmp_path_factory):
+    native.lib()   # builds the library when it is missing
+    out = str(tmp_path_factory.mktemp("shim") / "caller")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror",
+           "-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "iss_gb300", "csrc"),
+           os.path.join(REPO, "tests", "shim", "caller.cpp"), "-o", out,
+           "-L", NATIVE, "-liss_gb300", f"-Wl,-rpath,{NATIVE}"]
+    res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert res.returncode == 0, res.stdout
+    return out
+
+
+def run_dir(root, music, params, surface):
+    """The reference's CI layout: iSS_tables in the working directory, the
+    case's files in tests/."""
+    os.makedirs(os.path.join(root, "tests"), exist_ok=True)
+    link = os.path.join(root, "iSS_tables")
+    if not os.path.exists(link):
+        os.symlink(native.TABLE_DIR, link)
+    shutil.copy(os.path.join(CI, music), os.path.join(root, "tests", "music_input"))
+    for f in (params, surface):
+        shutil.copy(os.path.join(CI, f), os.path.join(root, "tests", f))
+    return ["tests/" + params, "tests", surface]
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(has_gpu(), reason="the no-device path needs a machine without a GPU")
+def test_caller_compiles_and_reports_missing_device(caller, tmp_path):
+    args = run_dir(str(tmp_path), *CASES[0][1:])
+    res = subprocess.run([caller, *args, "randomSeed=5"], cwd=str(tmp_path),
+                         stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+    assert res.returncode == 5, res.stdout           # ISS_ERR_CUDA, returned, not a crash
+    assert "MC_sampling 4" in res.stdout             # parameters read as the reference reads them
+    assert "shell 5" in res.stdout
+
+
+def tmunu_check(root):
+    data = np.loadtxt(os.path.join(root, "checkReconstructedTmunu.dat"))
+    return float(np.mean(np.abs(data[:, 2])))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_cli_passes_reference_ci_check(case, tmp_path):
+    root = str(tmp_path)
+    args = run_dir(root, *case[1:])
+    res = subprocess.run([os.path.join(NATIVE, "iSS.e"), *args, "randomSeed=17"], cwd=root,
+                         stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout[-3000:]
+    assert "Program executed normally." in res.stdout
+    diff = tmunu_check(root)
+    print(case[0], "mean |T_fluid - T_samples| =", diff)
+    assert diff < 1e-3
+
+
+@pytest.mark.gpu
+def test_caller_samples_reference_ci_cell(caller, tmp_path):
+    root = str(tmp_path)
+    args = run_dir(root, *CASES[0][1:])
+    res = subprocess.run([caller, *args, "randomSeed=23"], cwd=root,
+                         stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout[-3000:]
+    assert "Program executed normally." in res.stdout
+    assert tmunu_check(root) < 1e-3

@@ -80,6 +80,31 @@ def test_noalloc_scan_matches_generate_offsets():
 
 
 @pytest.mark.gpu
+def test_noalloc_scan_takes_no_device_memory_after_the_first_call():
+    """After the first call on the device (which loads the fixed array's
+    module), further calls leave the device's free memory unchanged: the
+    entry point itself allocates nothing."""
+    import torch
+    f = _fn()
+    counts = np.random.default_rng(3).integers(0, 50, size=1_000_000).astype(np.int32)
+    d_counts = torch.from_numpy(counts).cuda()
+    d_off = torch.empty(counts.size + 1, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    args = (C.c_void_p(d_counts.data_ptr()), counts.size, C.c_void_p(d_off.data_ptr()),
+            C.c_void_p(stream))
+    assert f(*args) == ISS_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert f(*args) == ISS_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    np.testing.assert_array_equal(d_off.cpu().numpy(),
+                                  np.concatenate([[0], np.cumsum(counts, dtype=np.int64)]))
+
+
+@pytest.mark.gpu
 def test_noalloc_scan_many_tiles():
     rng = np.random.default_rng(5)
     counts = rng.integers(0, 200, size=3_000_001).astype(np.int32)   # 733 tiles
