@@ -125,13 +125,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per hadron of the sampler kernel from the committed ncu
-    summary (profiles/sampler_kernel_viscous_3d.md, line 'dram_bytes_per_hadron:')."""
-    path = os.path.join(HERE, "profiles", "sampler_kernel_viscous_3d.md")
+PROFILE = os.path.join("profiles", "sampler_kernel_viscous_3d.md")
+SMS = 152               # GB300 streaming multiprocessors
+SCHEDULERS_PER_SM = 4   # warp schedulers, one warp instruction per cycle each
+
+
+def profiled(key):
+    """A per-hadron figure of the sample phase from the committed ncu summary
+    of the autotuned launch shape (PROFILE, line '<key>: value'): DRAM bytes
+    (dram_bytes_per_hadron) or warp instructions (warp_instructions_per_hadron)
+    of cell_assign_kernel + sampler_kernel per sampled hadron.  The bench
+    cannot run ncu itself; these are constants from that capture."""
     try:
-        for line in open(path):
-            if line.strip().startswith("dram_bytes_per_hadron:"):
+        for line in open(os.path.join(HERE, PROFILE)):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
@@ -605,7 +612,13 @@ def run_gpu(args, ws, rank, local):
         s.set_random_seed(20261203)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     tuning = None
-    if args.autotune:
+    if args.shape:
+        # an explicit launch shape (profiling runs: the autotuned shape without
+        # the autotuner's own launches)
+        kw = {k: int(v) for k, v in (kv.split("=") for kv in args.shape.split(","))}
+        s.set_tuning(**kw)
+        tuning = {"shape": s.get_tuning(), "autotuned": False, "explicit": True}
+    elif args.autotune:
         # the library's autotuner on this workload (untimed; results do not
         # depend on the launch shape)
         shape, ms_before, ms_after = s.autotune()
@@ -793,13 +806,29 @@ def run_gpu(args, ws, rank, local):
         samp_sec = local_stats[2]
         nh = local_stats[0]
         achieved = nh * ALG_BYTES_PER_HADRON / samp_sec / 1e9
-        traffic_per_h = profiled_traffic()
+        traffic_per_h = profiled("dram_bytes_per_hadron")
+        inst_per_h = profiled("warp_instructions_per_hadron")
         per_launch_h = nh / args.steps
+        clock_mhz = (clk or {}).get("sm_mhz") or 2070.0
+        issue = None
+        if inst_per_h:
+            # issue roofline: warp instructions per second against every
+            # scheduler issuing one per cycle at the sampled SM clock
+            peak_issue = SMS * SCHEDULERS_PER_SM * clock_mhz * 1e6
+            ach_issue = inst_per_h * nh / samp_sec
+            issue = {"bound": "issue", "achieved": ach_issue, "peak": peak_issue,
+                     "unit": "warp instructions/s", "frac": ach_issue / peak_issue,
+                     "warp_instructions_per_hadron": inst_per_h, "sm_mhz": clock_mhz,
+                     "source": f"ncu smsp__inst_executed.sum per hadron, {PROFILE}"}
         roofline = {"bound": "hbm", "kernel": "sample phase (cell_assign_kernel + sampler_kernel)",
                     "achieved": achieved,
                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "peak_source": peak_kind,
                     "traffic": (traffic_per_h * per_launch_h) if traffic_per_h else None,
+                    "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum per hadron "
+                                       f"of the autotuned shape on a 50k-cell case, {PROFILE}, times "
+                                       f"the hadrons of one step"),
+                    "issue": issue,
                     "algorithmic_bytes_per_launch": per_launch_h * ALG_BYTES_PER_HADRON,
                     "kernel_ms_per_launch": 1e3 * samp_sec / args.steps,
                     "yields_kernel_ms_per_launch": 1e3 * local_stats[3] / args.steps}
@@ -916,6 +945,9 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="default launch shape (default: the library's autotuner picks it on "
                          "the workload before the warm-up)")
+    ap.add_argument("--shape", default=None,
+                    help="explicit launch shape, e.g. item_size=256,yield_groups=4,sampler_ctas=3,"
+                         "assign_blocks=8 (replaces the autotuner)")
     ap.add_argument("--mc-sampling", type=int, choices=[2, 4], default=4,
                     help="4: the FSSW sampler; 2: the lab-frame EmissionFunctionArray sampler "
                          "(bulk delta f kind 1)")

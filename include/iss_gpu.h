@@ -74,6 +74,8 @@ typedef struct iss_timings {
     int64_t n_failures;   /* hadrons abandoned after the redraw cap (never expected)  */
     int32_t kernel_launches; /* kernels launched by the last iss_gpu_generate (without decays) */
     double ms_decays;     /* resonance decays (perform_decays = 1), not in ms_total   */
+    int32_t decay_reruns; /* decay passes rerun because a buffer was too small (the
+                             sizes are then kept for later calls; results unchanged) */
 } iss_timings_t;
 
 /* ---- construction, parameters ------------------------------------------ */

@@ -84,6 +84,15 @@ struct iss_handle {
     DevBuf<int32_t> d_dsorted;            // sorted pids, then their indices
     int n_decay_particles = 0;
     cudaEvent_t ev_decay[2] = {nullptr, nullptr};
+    // decay work buffers (grow-only): next-input ping-pong, the arena of
+    // stable products, per-input scratch, per-event bounds and the final list
+    DevBuf<HadronRec> dk_u[2], dk_arena, dk_final;
+    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_arena_ev, dk_chan, dk_ns, dk_nu, dk_etot;
+    DevBuf<int64_t> dk_soff, dk_uoff, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
+        dk_base, dk_off, dk_etiles, dk_evoff;
+    DevBuf<unsigned long long> dk_fail;
+    int64_t dk_scap_hint = 0, dk_ucap_hint = 0;   // sizes the last call needed
+    int32_t dk_reruns = 0;                         // decay passes rerun in the last call
     int64_t cdf_len = 0, guide_len = 0, n_tiles = 0;
     int hydro_mode = 2;
     int iEOS = 2;
@@ -199,6 +208,14 @@ struct iss_handle {
             d_dparticles.release();
             d_dchannels.release();
             d_dsorted.release();
+            for (auto* b : {&dk_u[0], &dk_u[1], &dk_arena, &dk_final}) b->release();
+            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_arena_ev, &dk_chan, &dk_ns, &dk_nu,
+                            &dk_etot})
+                b->release();
+            for (auto* b : {&dk_soff, &dk_uoff, &dk_tiles, &dk_first, &dk_last, &dk_gfirst, &dk_glast,
+                            &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
+                b->release();
+            dk_fail.release();
             learned.release_all();
             if (graph_exec) cudaGraphExecDestroy(graph_exec);
             if (gh) cudaFreeHost(gh);
@@ -646,8 +663,14 @@ float elapsed(iss_handle* h, int a, int b) {
 
 // Resonance decays of the sampled records, generation by generation over
 // all events (kernels_decay.cu); replaces d_hadrons and the event offsets
-// with the final-state lists.
-constexpr int kMaxDecayGenerations = 64;
+// with the final-state lists.  The sizes of the generations stay on the
+// device: generations are enqueued in batches of kDecayBatch and the host
+// waits once per batch (once in all for chains of up to kDecayBatch
+// generations) and once for the final lists.  A generation that does not fit
+// the arena or the next-input buffer writes nothing; the call then reruns
+// with buffers sized from what it needed (same results).  The work buffers
+// stay allocated in the handle for later calls.
+constexpr int kDecayBatch = 8;
 
 iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     DevConfig& c = h->cfg;
@@ -659,6 +682,10 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         if (!load_decay_table(h->particle_table_path, h->afterburner, &tab, &err))
             return fail(h, ISS_ERR_IO, "%s", err.c_str());
         const int n = static_cast<int>(tab.particles.size());
+        // the per-hadron channel cache packs (particle << 16) | channel
+        if (n >= 32768 || tab.channels.size() >= 65536)
+            return fail(h, ISS_ERR_UNSUPPORTED, "decay table too large (%d particles, %zu channels)", n,
+                        tab.channels.size());
         std::vector<std::pair<int32_t, int32_t>> by_pid;
         for (int i = 0; i < n; i++) by_pid.push_back({tab.particles[i].pid, i});
         // first entry of a repeated pid wins, as in the reference's lookups
@@ -695,126 +722,132 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     t.sorted_idx = h->d_dsorted.ptr + h->n_decay_particles;
     t.n_particles = h->n_decay_particles;
 
-    // every buffer of this function is released on every return
-    std::vector<DevBuf<HadronRec>> out_s;     // stable products of each generation
-    std::vector<DevBuf<int32_t>> out_ev;
-    std::vector<int64_t> out_n;
-    DevBuf<HadronRec> cur, nxt;
-    DevBuf<int32_t> cur_ev, nxt_ev, ns, nu;
-    DevBuf<int64_t> first, last, s_off, u_off, tiles, evoff, base;
-    DevBuf<unsigned long long> fails;
-    DevBuf<HadronRec> final_buf;
-    auto release = [&]() {
-        for (auto& b : out_s) b.release();
-        for (auto& b : out_ev) b.release();
-        cur.release(); nxt.release(); cur_ev.release(); nxt_ev.release(); ns.release(); nu.release();
-        first.release(); last.release(); s_off.release(); u_off.release(); tiles.release();
-        evoff.release(); base.release(); fails.release(); final_buf.release();
-    };
-#define DECAY_TRY(x)                                                                   \
-    do {                                                                               \
-        const cudaError_t e_ = (x);                                                    \
-        if (e_ != cudaSuccess) {                                                       \
-            release();                                                                 \
-            return fail(h, ISS_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));        \
-        }                                                                              \
-    } while (0)
-    int64_t n = h->n_hadrons;
-    DECAY_TRY(evoff.reserve(static_cast<size_t>(E) + 1));
-    DECAY_TRY(cudaMemcpyAsync(evoff.ptr, h->event_offsets.data(), 8 * (static_cast<size_t>(E) + 1),
-                              cudaMemcpyHostToDevice, s));
-    DECAY_TRY(first.reserve(std::max(E, 1)));
-    DECAY_TRY(last.reserve(std::max(E, 1)));
-    DECAY_TRY(fails.reserve(1));
-    DECAY_TRY(cudaMemsetAsync(fails.ptr, 0, sizeof(unsigned long long), s));
-    // generation 0: the sampled records (moved out of d_hadrons)
-    std::swap(cur.ptr, h->d_hadrons.ptr);
-    std::swap(cur.cap, h->d_hadrons.cap);
-    DECAY_TRY(cur_ev.reserve(static_cast<size_t>(std::max<int64_t>(n, 1))));
-    DECAY_TRY(launch_event_ids(evoff.ptr, E, cur_ev.ptr, s));
-    int gen = 0;
-    for (; n > 0 && gen < kMaxDecayGenerations; gen++) {
-        DECAY_TRY(launch_event_bounds(cur_ev.ptr, n, E, first.ptr, last.ptr, s));
-        DECAY_TRY(ns.reserve(static_cast<size_t>(n)));
-        DECAY_TRY(nu.reserve(static_cast<size_t>(n)));
-        DECAY_TRY(launch_decay_count(c, t, static_cast<uint32_t>(gen), cur.ptr, cur_ev.ptr, first.ptr,
-                                     n, ns.ptr, nu.ptr, s));
-        DECAY_TRY(s_off.reserve(static_cast<size_t>(n) + 1));
-        DECAY_TRY(u_off.reserve(static_cast<size_t>(n) + 1));
-        DECAY_TRY(tiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(n), 1))));
-        DECAY_TRY(launch_offsets_scan(ns.ptr, n, tiles.ptr, s_off.ptr, s));
-        DECAY_TRY(launch_offsets_scan(nu.ptr, n, tiles.ptr, u_off.ptr, s));
-        int64_t tot[2] = {0, 0};
-        DECAY_TRY(cudaMemcpyAsync(&tot[0], s_off.ptr + n, 8, cudaMemcpyDeviceToHost, s));
-        DECAY_TRY(cudaMemcpyAsync(&tot[1], u_off.ptr + n, 8, cudaMemcpyDeviceToHost, s));
-        DECAY_TRY(cudaStreamSynchronize(s));
-        out_s.emplace_back();
-        out_ev.emplace_back();
-        out_n.push_back(tot[0]);
-        DECAY_TRY(out_s.back().reserve(static_cast<size_t>(std::max<int64_t>(tot[0], 1))));
-        DECAY_TRY(out_ev.back().reserve(static_cast<size_t>(std::max<int64_t>(tot[0], 1))));
-        DECAY_TRY(nxt.reserve(static_cast<size_t>(std::max<int64_t>(tot[1], 1))));
-        DECAY_TRY(nxt_ev.reserve(static_cast<size_t>(std::max<int64_t>(tot[1], 1))));
-        DECAY_TRY(launch_decay_write(c, t, static_cast<uint32_t>(gen), cur.ptr, cur_ev.ptr, first.ptr,
-                                     n, s_off.ptr, u_off.ptr, out_s.back().ptr, out_ev.back().ptr,
-                                     nxt.ptr, nxt_ev.ptr, fails.ptr, s));
-        std::swap(cur, nxt);
-        std::swap(cur_ev, nxt_ev);
-        n = tot[1];
+    const int64_t n0 = h->n_hadrons;
+    h->dk_reruns = 0;
+    if (n0 <= 0 || E <= 0) {
+        *failures_out = 0;
+        return ISS_OK;
     }
-    if (n > 0) {
-        release();
-        return fail(h, ISS_ERR_SAMPLING, "decay chains longer than %d generations",
-                    kMaxDecayGenerations);
-    }
-    // final lists: event e = its generation-0 products, then generation 1, ...
-    const int G = static_cast<int>(out_n.size());
-    std::vector<int64_t> cnt(static_cast<size_t>(G) * E, 0);
-    std::vector<int64_t> firsts(static_cast<size_t>(G) * E, 0);
-    std::vector<int64_t> fb(static_cast<size_t>(E)), lb(static_cast<size_t>(E));
-    for (int g = 0; g < G; g++) {
-        DECAY_TRY(launch_event_bounds(out_ev[g].ptr, out_n[g], E, first.ptr, last.ptr, s));
-        DECAY_TRY(cudaMemcpyAsync(fb.data(), first.ptr, 8 * static_cast<size_t>(E), cudaMemcpyDeviceToHost, s));
-        DECAY_TRY(cudaMemcpyAsync(lb.data(), last.ptr, 8 * static_cast<size_t>(E), cudaMemcpyDeviceToHost, s));
-        DECAY_TRY(cudaStreamSynchronize(s));
-        for (int e = 0; e < E; e++) {
-            cnt[static_cast<size_t>(g) * E + e] = fb[e] >= 0 ? lb[e] - fb[e] : 0;
-            firsts[static_cast<size_t>(g) * E + e] = fb[e];
+    const int grid = h->num_sms * 4;
+    const int G = kDecayMaxGenerations;
+    // first sizes: what the last call needed, else gpu_decay_arena_factor
+    // (default 1.5) and gpu_decay_next_factor (0.5) times the sampled
+    // hadrons; too small only costs a rerun
+    const double fa = h->params.get_or("gpu_decay_arena_factor", 1.5);
+    const double fu = h->params.get_or("gpu_decay_next_factor", 0.5);
+    if (!(fa > 0.0) || !(fu > 0.0))
+        return fail(h, ISS_ERR_INVALID_ARG, "gpu_decay_arena_factor / gpu_decay_next_factor must be > 0");
+    int64_t s_cap = std::max<int64_t>(h->dk_scap_hint, static_cast<int64_t>(fa * static_cast<double>(n0)) + 64);
+    int64_t u_cap = std::max<int64_t>(h->dk_ucap_hint, static_cast<int64_t>(fu * static_cast<double>(n0)) + 64);
+    std::vector<int64_t> meta_h(kDecayMetaLen, 0);
+    for (int attempt = 0;; attempt++) {
+        const int64_t in_cap = std::max(n0, u_cap);
+        CUDA_TRY(h, h->dk_ev0.reserve(static_cast<size_t>(n0)));
+        for (int k = 0; k < 2; k++) {
+            CUDA_TRY(h, h->dk_u[k].reserve(static_cast<size_t>(u_cap)));
+            CUDA_TRY(h, h->dk_uev[k].reserve(static_cast<size_t>(u_cap)));
         }
-    }
-    std::vector<int64_t> off(static_cast<size_t>(E) + 1, 0);
-    for (int e = 0; e < E; e++) {
-        int64_t k = 0;
-        for (int g = 0; g < G; g++) k += cnt[static_cast<size_t>(g) * E + e];
-        off[e + 1] = off[e] + k;
-    }
-    const int64_t total = off[E];
-    DECAY_TRY(final_buf.reserve(static_cast<size_t>(std::max<int64_t>(total, 1))));
-    DECAY_TRY(base.reserve(static_cast<size_t>(std::max(E, 1))));
-    std::vector<int64_t> bg(static_cast<size_t>(E));
-    std::vector<int64_t> acc(off.begin(), off.end() - 1);
-    for (int g = 0; g < G; g++) {
-        for (int e = 0; e < E; e++) {
-            bg[e] = acc[e];
-            acc[e] += cnt[static_cast<size_t>(g) * E + e];
-            fb[e] = firsts[static_cast<size_t>(g) * E + e];
+        CUDA_TRY(h, h->dk_arena.reserve(static_cast<size_t>(s_cap)));
+        CUDA_TRY(h, h->dk_arena_ev.reserve(static_cast<size_t>(s_cap)));
+        CUDA_TRY(h, h->dk_final.reserve(static_cast<size_t>(s_cap)));
+        CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(in_cap)));
+        CUDA_TRY(h, h->dk_ns.reserve(static_cast<size_t>(in_cap)));
+        CUDA_TRY(h, h->dk_nu.reserve(static_cast<size_t>(in_cap)));
+        CUDA_TRY(h, h->dk_soff.reserve(static_cast<size_t>(in_cap) + 1));
+        CUDA_TRY(h, h->dk_uoff.reserve(static_cast<size_t>(in_cap) + 1));
+        CUDA_TRY(h, h->dk_tiles.reserve(2 * static_cast<size_t>(in_cap / 4096 + 1)));
+        CUDA_TRY(h, h->dk_first.reserve(static_cast<size_t>(E)));
+        CUDA_TRY(h, h->dk_last.reserve(static_cast<size_t>(E)));
+        CUDA_TRY(h, h->dk_gfirst.reserve(static_cast<size_t>(G) * E));
+        CUDA_TRY(h, h->dk_glast.reserve(static_cast<size_t>(G) * E));
+        CUDA_TRY(h, h->dk_base.reserve(static_cast<size_t>(G) * E));
+        CUDA_TRY(h, h->dk_meta.reserve(kDecayMetaLen));
+        CUDA_TRY(h, h->dk_off.reserve(static_cast<size_t>(E) + 1));
+        CUDA_TRY(h, h->dk_evoff.reserve(static_cast<size_t>(E) + 1));
+        CUDA_TRY(h, h->dk_etot.reserve(static_cast<size_t>(E)));
+        CUDA_TRY(h, h->dk_etiles.reserve(static_cast<size_t>(std::max(offsets_num_tiles(E), 1))));
+        CUDA_TRY(h, h->dk_fail.reserve(1));
+
+        std::fill(meta_h.begin(), meta_h.end(), 0);
+        meta_h[kDecayMetaNIn] = n0;
+        CUDA_TRY(h, cudaMemcpyAsync(h->dk_meta.ptr, meta_h.data(), 8 * meta_h.size(),
+                                    cudaMemcpyHostToDevice, s));
+        CUDA_TRY(h, cudaMemsetAsync(h->dk_gfirst.ptr, 0xFF, 8 * static_cast<size_t>(G) * E, s));
+        CUDA_TRY(h, cudaMemsetAsync(h->dk_glast.ptr, 0xFF, 8 * static_cast<size_t>(G) * E, s));
+        CUDA_TRY(h, cudaMemsetAsync(h->dk_fail.ptr, 0, sizeof(unsigned long long), s));
+        CUDA_TRY(h, cudaMemcpyAsync(h->dk_evoff.ptr, h->event_offsets.data(), 8 * (static_cast<size_t>(E) + 1),
+                                    cudaMemcpyHostToDevice, s));
+        CUDA_TRY(h, launch_event_ids(h->dk_evoff.ptr, E, h->dk_ev0.ptr, s));
+
+        DecayBuffers b{};
+        b.arena = h->dk_arena.ptr;
+        b.arena_ev = h->dk_arena_ev.ptr;
+        b.chan = h->dk_chan.ptr;
+        b.ns = h->dk_ns.ptr;
+        b.nu = h->dk_nu.ptr;
+        b.s_off = h->dk_soff.ptr;
+        b.u_off = h->dk_uoff.ptr;
+        b.tiles = h->dk_tiles.ptr;
+        b.first = h->dk_first.ptr;
+        b.last = h->dk_last.ptr;
+        b.gfirst = h->dk_gfirst.ptr;
+        b.glast = h->dk_glast.ptr;
+        b.meta = h->dk_meta.ptr;
+        b.failures = h->dk_fail.ptr;
+        b.s_cap = s_cap;
+        b.u_cap = u_cap;
+        b.g_max = static_cast<uint32_t>(G);
+        int g = 0;
+        int64_t head[2] = {0, 0};   // next input size, flags
+        for (;;) {
+            for (int k = 0; k < kDecayBatch && g < G; k++, g++) {
+                b.in = g == 0 ? h->d_hadrons.ptr : h->dk_u[(g - 1) & 1].ptr;
+                b.in_ev = g == 0 ? h->dk_ev0.ptr : h->dk_uev[(g - 1) & 1].ptr;
+                b.out_u = h->dk_u[g & 1].ptr;
+                b.out_u_ev = h->dk_uev[g & 1].ptr;
+                CUDA_TRY(h, launch_decay_generation(c, t, static_cast<uint32_t>(g), b, E, grid, s));
+            }
+            CUDA_TRY(h, cudaMemcpyAsync(&head[0], h->dk_meta.ptr + kDecayMetaNIn + g, 8,
+                                        cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(h, cudaMemcpyAsync(&head[1], h->dk_meta.ptr + kDecayMetaFlags, 8,
+                                        cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(h, cudaStreamSynchronize(s));
+            if (head[1] != 0 || head[0] == 0 || g >= G) break;
         }
-        DECAY_TRY(cudaMemcpyAsync(base.ptr, bg.data(), 8 * static_cast<size_t>(E), cudaMemcpyHostToDevice, s));
-        DECAY_TRY(cudaMemcpyAsync(first.ptr, fb.data(), 8 * static_cast<size_t>(E), cudaMemcpyHostToDevice, s));
-        DECAY_TRY(launch_gather(out_s[g].ptr, out_ev[g].ptr, first.ptr, base.ptr, out_n[g],
-                                final_buf.ptr, s));
-        DECAY_TRY(cudaStreamSynchronize(s));   // bg and fb are reused
+        CUDA_TRY(h, cudaMemcpyAsync(meta_h.data(), h->dk_meta.ptr, 8 * meta_h.size(),
+                                    cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(h, cudaStreamSynchronize(s));
+        const int64_t flags = meta_h[kDecayMetaFlags];
+        if (flags & 4)
+            return fail(h, ISS_ERR_SAMPLING, "decay chains longer than %d generations", G);
+        if (flags & 3) {
+            if (attempt >= 8) return fail(h, ISS_ERR_CUDA, "decay buffers did not settle");
+            h->dk_reruns++;
+            if (flags & 1) s_cap = std::max(s_cap * 2, meta_h[kDecayMetaNeedS] + meta_h[kDecayMetaNeedS] / 4);
+            if (flags & 2) u_cap = std::max(u_cap * 2, meta_h[kDecayMetaNeedU] + meta_h[kDecayMetaNeedU] / 4);
+            continue;
+        }
+        const int64_t total = meta_h[kDecayMetaSBase + g];
+        CUDA_TRY(h, launch_decay_assemble(b, g, E, h->dk_etot.ptr, h->dk_etiles.ptr, h->dk_off.ptr,
+                                          h->dk_base.ptr, h->dk_final.ptr, grid, s));
+        h->event_offsets.assign(static_cast<size_t>(E) + 1, 0);
+        unsigned long long nf = 0;
+        CUDA_TRY(h, cudaMemcpyAsync(h->event_offsets.data(), h->dk_off.ptr, 8 * (static_cast<size_t>(E) + 1),
+                                    cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(h, cudaMemcpyAsync(&nf, h->dk_fail.ptr, sizeof(nf), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(h, cudaStreamSynchronize(s));
+        if (h->event_offsets[E] != total)
+            return fail(h, ISS_ERR_CUDA, "decay lists disagree (%lld vs %lld hadrons)",
+                        static_cast<long long>(h->event_offsets[E]), static_cast<long long>(total));
+        *failures_out = nf;
+        // sizes for the next call: what this one needed, with headroom
+        h->dk_scap_hint = std::max(h->dk_scap_hint, total + total / 8 + 4096);
+        h->dk_ucap_hint = std::max(h->dk_ucap_hint, meta_h[kDecayMetaMaxU] + meta_h[kDecayMetaMaxU] / 8 + 4096);
+        std::swap(h->dk_final.ptr, h->d_hadrons.ptr);
+        std::swap(h->dk_final.cap, h->d_hadrons.cap);
+        h->n_hadrons = total;
+        return ISS_OK;
     }
-    unsigned long long nf = 0;
-    DECAY_TRY(cudaMemcpy(&nf, fails.ptr, sizeof(nf), cudaMemcpyDeviceToHost));
-    *failures_out = nf;
-    std::swap(final_buf.ptr, h->d_hadrons.ptr);
-    std::swap(final_buf.cap, h->d_hadrons.cap);
-    h->event_offsets = off;
-    h->n_hadrons = total;
-#undef DECAY_TRY
-    release();
-    return ISS_OK;
 }
 
 // host_out != nullptr: iss_gpu_generate_into -- the sampler runs in chunks of
@@ -1306,6 +1339,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
 
     iss_timings_t& t = h->timings;
     t.ms_decays = ms_decays;
+    t.decay_reruns = h->decays ? h->dk_reruns : 0;
     t.ms_prologue = elapsed(h, kEvStart, kEvPrologue);
     t.ms_yields = elapsed(h, kEvPrologue, kEvYields);
     t.ms_cdf = elapsed(h, kEvYields, kEvCdf);

@@ -76,23 +76,55 @@ cudaError_t launch_learned_train_rows(const DevConfig& cfg, const CellArrays& ce
                                       const int32_t* cell_of, int64_t n, void* x, void* tg,
                                       double* nll_plain, cudaStream_t stream);
 
-// kernels_decay.cu: one generation of resonance decays over all events
-// (event-sorted input with event ids; first[e] = index of event e's first
-// element), event ids from event offsets, event bounds of an event-sorted
-// array, and the final gather out[base[e] + i - first[e]] = in[i].
+// kernels_decay.cu: resonance decays, one generation over all events at a
+// time, sizes kept on the device.  DecayMeta (int64 slots of `meta`):
+// kDecayMetaNIn + g the input size of generation g (g <= g_max),
+// kDecayMetaSBase + g the start of generation g's stable products in the
+// arena, kDecayMetaFlags (1: arena too small, 2: next input buffer too small,
+// 4: chains longer than g_max), kDecayMetaNeedS / NeedU what the failing
+// generation needed, kDecayMetaMaxU the largest next input seen.
+constexpr int kDecayMetaFlags = 0;
+constexpr int kDecayMetaNeedS = 1;
+constexpr int kDecayMetaNeedU = 2;
+constexpr int kDecayMetaMaxU = 3;
+constexpr int kDecayMetaNIn = 8;
+constexpr int kDecayMaxGenerations = 64;
+constexpr int kDecayMetaSBase = kDecayMetaNIn + kDecayMaxGenerations + 1;
+constexpr int kDecayMetaLen = kDecayMetaSBase + kDecayMaxGenerations + 1;
+
+struct DecayBuffers {
+    const HadronRec* in;        // this generation's input (event-sorted)
+    const int32_t* in_ev;       // its event ids
+    HadronRec* out_u;           // next generation's input (unstable products)
+    int32_t* out_u_ev;
+    HadronRec* arena;           // stable products of all generations
+    int32_t* arena_ev;
+    int32_t* chan;              // per input hadron: (type << 16) | channel, or < 0
+    int32_t* ns;                // per input hadron: stable products
+    int32_t* nu;                // per input hadron: unstable products
+    int64_t* s_off;             // exclusive scans of ns / nu (input size + 1)
+    int64_t* u_off;
+    int64_t* tiles;             // 2 per scan tile of 4096 inputs
+    int64_t* first;             // [n_events] first input of each event (-1: none)
+    int64_t* last;
+    int64_t* gfirst;            // [g_max][n_events] per generation, its arena range per event
+    int64_t* glast;
+    int64_t* meta;              // DecayMeta
+    unsigned long long* failures;
+    int64_t s_cap, u_cap;       // arena and next-input capacities
+    uint32_t g_max;
+};
+
 cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cudaStream_t s);
-cudaError_t launch_event_bounds(const int32_t* ev, int64_t n, int n_events, int64_t* first,
-                                int64_t* last, cudaStream_t s);
-cudaError_t launch_decay_count(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                               const HadronRec* in, const int32_t* ev, const int64_t* first,
-                               int64_t n, int32_t* n_stable, int32_t* n_unstable, cudaStream_t s);
-cudaError_t launch_decay_write(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                               const HadronRec* in, const int32_t* ev, const int64_t* first,
-                               int64_t n, const int64_t* s_off, const int64_t* u_off,
-                               HadronRec* out_s, int32_t* ev_s, HadronRec* out_u, int32_t* ev_u,
-                               unsigned long long* failures, cudaStream_t s);
-cudaError_t launch_gather(const HadronRec* in, const int32_t* ev, const int64_t* first,
-                          const int64_t* base, int64_t n, HadronRec* out, cudaStream_t s);
+// one generation: input bounds, count (channel cache), two scans, sizes of
+// the next generation, write, and this generation's arena bounds per event
+cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                    const DecayBuffers& b, int n_events, int grid, cudaStream_t s);
+// final lists: per-event totals of generations < n_gen, event offsets (off,
+// n_events + 1), per (generation, event) bases, and the gather into out
+cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
+                                  int64_t* tiles, int64_t* off, int64_t* base, HadronRec* out, int grid,
+                                  cudaStream_t s);
 
 // kernels_output.cu: OSCAR text (FSSW::combine_samples_to_OSCAR) of hadrons
 // [h0, h1), which are the whole events [e_lo, e_hi).  ev_off: the events'

@@ -9,9 +9,17 @@
 // unstable daughters, then of the granddaughters, and so on.  Here each such
 // generation is one pass over all events at once: a count kernel (channel
 // choice, stable and unstable products per hadron), two exclusive scans, and
-// a write kernel that puts stable products into this generation's output and
-// unstable ones into the next generation's input, both in order.  The final
-// list of each event is the concatenation of its generations' outputs.
+// a write kernel that puts stable products into this generation's range of
+// one output arena and unstable ones into the next generation's input, both
+// in order.  The final list of each event is the concatenation of its
+// generations' outputs (dk_event_totals / dk_event_bases / dk_gather).
+//
+// The sizes of a generation live on the device (DecayMeta): every kernel
+// reads its input size there and loops over it with a fixed grid, so the
+// host enqueues whole batches of generations without waiting; a generation
+// whose products would not fit the arena or the next input buffer writes
+// nothing and raises a flag, and the host reruns the call with larger
+// buffers (the results do not depend on the buffer sizes).
 //
 // Every random number comes from Philox4x32-10 with counter
 // (draw, index of the hadron in its event's generation list, event,
@@ -85,25 +93,46 @@ __device__ __forceinline__ bool daughter_stable(const DecayTablesDev& t, int idx
     return idx < 0 || t.particles[idx].stable;
 }
 
+// channel cache of a hadron: (particle type << 16) | decay channel (the host
+// checks that both fit), or kChanStable (kept as it is) or kChanNone (no
+// product: no channel reached the uniform, or a channel of other than two
+// or three bodies)
+constexpr int32_t kChanStable = -1;
+constexpr int32_t kChanNone = -2;
+
+__device__ __forceinline__ int64_t meta_n(const int64_t* __restrict__ meta, uint32_t gen) {
+    return meta[kDecayMetaNIn + gen];
+}
+
 __global__ void __launch_bounds__(kDecayThreads)
 decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
-                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first, int64_t n,
+                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
+                   const int64_t* __restrict__ meta, int32_t* __restrict__ chan,
                    int32_t* __restrict__ n_stable, int32_t* __restrict__ n_unstable) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int e = ev[i];
-    const DecayPlan d = plan(t, cfg, in[i].pid, static_cast<uint32_t>(i - first[e]),
-                             cfg.event_offset + static_cast<uint32_t>(e), gen);
-    int s = 0, u = 0;
-    if (d.channel < 0) {
-        s = d.n;   // stable (or no channel: nothing)
-    } else {
-        for (int k = 0; k < d.n; k++) {
-            if (daughter_stable(t, t.channels[d.channel].daughter[k])) s++; else u++;
+    const int64_t n = meta_n(meta, gen);
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int e = ev[i];
+        const DecayPlan d = plan(t, cfg, in[i].pid, static_cast<uint32_t>(i - first[e]),
+                                 cfg.event_offset + static_cast<uint32_t>(e), gen);
+        int s = 0, u = 0;
+        int32_t c;
+        if (d.channel < 0) {
+            s = d.n;   // stable (or no channel: nothing)
+            c = d.n == 1 ? kChanStable : kChanNone;
+        } else if (d.n == 0) {
+            c = kChanNone;
+        } else {
+            c = static_cast<int32_t>((static_cast<uint32_t>(d.type) << 16) |
+                                     static_cast<uint32_t>(d.channel));
+            for (int k = 0; k < d.n; k++) {
+                if (daughter_stable(t, t.channels[d.channel].daughter[k])) s++; else u++;
+            }
         }
+        chan[i] = c;
+        n_stable[i] = s;
+        n_unstable[i] = u;
     }
-    n_stable[i] = s;
-    n_unstable[i] = u;
 }
 
 // The mother's 4-velocity: gamma = E/m and u = p/m (computing gamma from
@@ -135,30 +164,20 @@ __device__ __forceinline__ void boost(const Lorentz& L, float E, float px, float
     *oz = pz + c * L.uz;
 }
 
-__global__ void __launch_bounds__(kDecayThreads)
-decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
-                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first, int64_t n,
-                   const int64_t* __restrict__ s_off, const int64_t* __restrict__ u_off,
-                   HadronRec* __restrict__ out_s, int32_t* __restrict__ ev_s,
-                   HadronRec* __restrict__ out_u, int32_t* __restrict__ ev_u,
-                   unsigned long long* __restrict__ failures) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int e = ev[i];
-    const uint32_t ie = static_cast<uint32_t>(i - first[e]);
+// the products of hadron m of event e (index ie in its event's generation
+// list) through channel `channel` of particle `type`
+__device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                       const HadronRec& m, int e, uint32_t ie, int type, int channel,
+                                       int64_t ps, int64_t pu, HadronRec* __restrict__ out_s,
+                                       int32_t* __restrict__ ev_s, HadronRec* __restrict__ out_u,
+                                       int32_t* __restrict__ ev_u,
+                                       unsigned long long* __restrict__ failures) {
     const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
-    const HadronRec m = in[i];
-    const DecayPlan d = plan(t, cfg, m.pid, ie, eg, gen);
-    int64_t ps = s_off[i], pu = u_off[i];
-    if (d.channel < 0) {
-        if (d.n == 1) {
-            out_s[ps] = m;
-            ev_s[ps] = e;
-        }
-        return;
-    }
-    if (d.n == 0) return;
-    const DecayChannel& ch = t.channels[d.channel];
+    const DecayChannel& ch = t.channels[channel];
+    DecayPlan d;
+    d.channel = channel;
+    d.type = type;
+    d.n = ch.n_daughters;
     const DecayParticle& mp = t.particles[d.type];
     const float M = mp.mass;       // pole mass (the reference does not sample Breit-Wigner)
     float md[3];
@@ -257,15 +276,47 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
     }
 }
 
-// first[e] = index of event e's first element in an event-sorted array, and
-// last[e] = one past its last (both stay -1 for absent events)
-__global__ void event_bounds_kernel(const int32_t* __restrict__ ev, int64_t n,
-                                    int64_t* __restrict__ first, int64_t* __restrict__ last) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int e = ev[i];
-    if (i == 0 || ev[i - 1] != e) first[e] = i;
-    if (i == n - 1 || ev[i + 1] != e) last[e] = i + 1;
+__global__ void __launch_bounds__(kDecayThreads)
+decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
+                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
+                   const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
+                   const int64_t* __restrict__ s_off, const int64_t* __restrict__ u_off,
+                   HadronRec* __restrict__ out_s, int32_t* __restrict__ ev_s,
+                   HadronRec* __restrict__ out_u, int32_t* __restrict__ ev_u,
+                   unsigned long long* __restrict__ failures) {
+    // a generation that did not fit writes nothing (the host reruns the call)
+    if (meta[kDecayMetaFlags] != 0) return;
+    const int64_t n = meta_n(meta, gen);
+    const int64_t sbase = meta[kDecayMetaSBase + gen];
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t c = chan[i];
+        if (c == kChanNone) continue;
+        const int e = ev[i];
+        const int64_t ps = sbase + s_off[i];
+        if (c == kChanStable) {
+            out_s[ps] = in[i];
+            ev_s[ps] = e;
+            continue;
+        }
+        decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF, ps,
+                  u_off[i], out_s, ev_s, out_u, ev_u, failures);
+    }
+}
+
+// first[e] = index of event e's first element in the event-sorted range
+// [*lo, *hi) of ev (lo null: 0), and last[e] = one past its last (both stay
+// -1 for absent events)
+__global__ void dk_bounds_kernel(const int32_t* __restrict__ ev, const int64_t* __restrict__ lo_p,
+                                 const int64_t* __restrict__ hi_p, int64_t* __restrict__ first,
+                                 int64_t* __restrict__ last) {
+    const int64_t lo = lo_p ? *lo_p : 0, hi = *hi_p;
+    for (int64_t i = lo + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < hi;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int e = ev[i];
+        if (i == lo || ev[i - 1] != e) first[e] = i;
+        if (i == hi - 1 || ev[i + 1] != e) last[e] = i + 1;
+    }
 }
 
 // event ids of the sampled records from the event offsets
@@ -276,17 +327,210 @@ __global__ void event_ids_kernel(const int64_t* __restrict__ off, int n_events,
     for (int64_t i = off[e] + threadIdx.x; i < off[e + 1]; i += blockDim.x) ev[i] = e;
 }
 
-// out[base[e] + i - first[e]] = in[i]
-__global__ void gather_kernel(const HadronRec* __restrict__ in, const int32_t* __restrict__ ev,
-                              const int64_t* __restrict__ first, const int64_t* __restrict__ base,
-                              int64_t n, HadronRec* __restrict__ out) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int e = ev[i];
-    out[base[e] + (i - first[e])] = in[i];
+// ---- exclusive scans of the two count arrays, input size on the device ----
+
+constexpr int kDkScanThreads = 256;
+constexpr int kDkScanPer = 16;
+constexpr int kDkTile = kDkScanThreads * kDkScanPer;
+
+__device__ __forceinline__ long long dk_warp_incl(long long v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long x = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += x;
+    }
+    return v;
 }
 
-unsigned grid_for(int64_t n) { return static_cast<unsigned>((n + kDecayThreads - 1) / kDecayThreads); }
+// block-wide exclusive scan of one value per thread; *total = the sum
+__device__ long long dk_block_excl(long long v, long long* s_warp, long long* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long inc = dk_warp_incl(v);
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        const long long w = lane < nw ? s_warp[lane] : 0;
+        const long long wi = dk_warp_incl(w);
+        if (lane < nw) s_warp[lane] = wi - w;
+        if (lane == nw - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const long long out = s_warp[wid] + inc - v;
+    *total = s_warp[32];
+    __syncthreads();
+    return out;
+}
+
+// tile sums of both arrays: tiles[2 t] (stable), tiles[2 t + 1] (unstable)
+__global__ void __launch_bounds__(kDkScanThreads)
+dk_tile_sum_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b,
+                   const int64_t* __restrict__ meta, uint32_t gen, int64_t* __restrict__ tiles) {
+    __shared__ long long s_warp[33];
+    const int64_t n = meta_n(meta, gen);
+    const int64_t nt = (n + kDkTile - 1) / kDkTile;
+    for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
+        long long sa = 0, sb = 0;
+        for (int k = 0; k < kDkScanPer; k++) {
+            const int64_t i = tl * kDkTile + k * kDkScanThreads + threadIdx.x;
+            if (i < n) {
+                sa += a[i];
+                sb += b[i];
+            }
+        }
+        long long ta, tb;
+        dk_block_excl(sa, s_warp, &ta);
+        dk_block_excl(sb, s_warp, &tb);
+        if (threadIdx.x == 0) {
+            tiles[2 * tl] = ta;
+            tiles[2 * tl + 1] = tb;
+        }
+    }
+}
+
+// one block: tile sums -> tile offsets (in place), totals to oa[n], ob[n]
+__global__ void __launch_bounds__(kDkScanThreads)
+dk_tile_offset_kernel(int64_t* __restrict__ tiles, const int64_t* __restrict__ meta, uint32_t gen,
+                      int64_t* __restrict__ oa, int64_t* __restrict__ ob) {
+    __shared__ long long s_warp[33];
+    const int64_t n = meta_n(meta, gen);
+    const int64_t nt = (n + kDkTile - 1) / kDkTile;
+    long long ca = 0, cb = 0;
+    for (int64_t b0 = 0; b0 < nt; b0 += kDkScanThreads) {
+        const int64_t i = b0 + threadIdx.x;
+        const long long va = i < nt ? tiles[2 * i] : 0, vb = i < nt ? tiles[2 * i + 1] : 0;
+        long long ta, tb;
+        const long long ea = dk_block_excl(va, s_warp, &ta);
+        const long long eb = dk_block_excl(vb, s_warp, &tb);
+        if (i < nt) {
+            tiles[2 * i] = ca + ea;
+            tiles[2 * i + 1] = cb + eb;
+        }
+        ca += ta;
+        cb += tb;
+    }
+    if (threadIdx.x == 0) {
+        oa[n] = ca;
+        ob[n] = cb;
+    }
+}
+
+__device__ void dk_tile_scan_one(const int32_t* __restrict__ c, int64_t n, int64_t t0, long long base,
+                                 int32_t* s_in, long long* s_warp, int64_t* __restrict__ out) {
+    for (int k = 0; k < kDkScanPer; k++) {
+        const int e = k * kDkScanThreads + threadIdx.x;
+        const int64_t i = t0 + e;
+        s_in[(e / kDkScanPer) * (kDkScanPer + 1) + e % kDkScanPer] = i < n ? c[i] : 0;
+    }
+    __syncthreads();
+    const int32_t* mine = s_in + threadIdx.x * (kDkScanPer + 1);
+    long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < kDkScanPer; k++) acc += mine[k];
+    long long tot;
+    long long run = base + dk_block_excl(acc, s_warp, &tot);
+    const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kDkScanPer;
+#pragma unroll
+    for (int k = 0; k < kDkScanPer; k++) {
+        if (e0 + k < n) out[e0 + k] = run;
+        run += mine[k];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kDkScanThreads)
+dk_tile_scan_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b,
+                    const int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ tiles,
+                    int64_t* __restrict__ oa, int64_t* __restrict__ ob) {
+    __shared__ int32_t s_in[kDkScanThreads * (kDkScanPer + 1)];
+    __shared__ long long s_warp[33];
+    const int64_t n = meta_n(meta, gen);
+    const int64_t nt = (n + kDkTile - 1) / kDkTile;
+    for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
+        dk_tile_scan_one(a, n, tl * kDkTile, tiles[2 * tl], s_in, s_warp, oa);
+        dk_tile_scan_one(b, n, tl * kDkTile, tiles[2 * tl + 1], s_in, s_warp, ob);
+    }
+}
+
+// sizes of the next generation: the stable products go to the arena after
+// this generation's, the unstable ones are the next input; a generation
+// that does not fit (arena or next input) sets a flag, records what it
+// needed and stops the chain
+__global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ so,
+                                  const int64_t* __restrict__ uo, int64_t s_cap, int64_t u_cap,
+                                  uint32_t g_max) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int64_t n = meta[kDecayMetaNIn + gen];
+    const int64_t sb = meta[kDecayMetaSBase + gen];
+    const int64_t st = so[n], ut = uo[n];
+    int64_t next_n = ut, next_sb = sb + st;
+    if (meta[kDecayMetaFlags] == 0 && next_sb > s_cap) {
+        meta[kDecayMetaFlags] |= 1;
+        meta[kDecayMetaNeedS] = next_sb;
+    }
+    if (meta[kDecayMetaFlags] == 0 && ut > u_cap) {
+        meta[kDecayMetaFlags] |= 2;
+        meta[kDecayMetaNeedU] = ut;
+    }
+    if (meta[kDecayMetaFlags] == 0 && gen + 1 >= g_max && ut > 0) meta[kDecayMetaFlags] |= 4;
+    if (meta[kDecayMetaFlags] != 0) {
+        next_n = 0;
+        next_sb = sb;
+    }
+    meta[kDecayMetaNIn + gen + 1] = next_n;
+    meta[kDecayMetaSBase + gen + 1] = next_sb;
+    if (ut > meta[kDecayMetaMaxU]) meta[kDecayMetaMaxU] = ut;
+}
+
+// ---- the final lists ----------------------------------------------------
+
+// per event: the hadrons of its generations' outputs (rows g < n_gen of the
+// per-generation bounds, -1 where the event has none)
+__global__ void dk_event_totals_kernel(const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
+                                       int n_gen, int n_events, int32_t* __restrict__ tot) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_events) return;
+    int64_t k = 0;
+    for (int g = 0; g < n_gen; g++) {
+        const int64_t f = gfirst[static_cast<int64_t>(g) * n_events + e];
+        if (f >= 0) k += glast[static_cast<int64_t>(g) * n_events + e] - f;
+    }
+    tot[e] = static_cast<int32_t>(k);
+}
+
+// base[g][e]: where event e's products of generation g start in the final list
+__global__ void dk_event_bases_kernel(const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
+                                      const int64_t* __restrict__ off, int n_gen, int n_events,
+                                      int64_t* __restrict__ base) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_events) return;
+    int64_t b = off[e];
+    for (int g = 0; g < n_gen; g++) {
+        const int64_t r = static_cast<int64_t>(g) * n_events + e;
+        base[r] = b;
+        if (gfirst[r] >= 0) b += glast[r] - gfirst[r];
+    }
+}
+
+// final[base[g][e] + i - gfirst[g][e]] = arena[i], g the generation whose
+// arena range holds i
+__global__ void dk_gather_kernel(const HadronRec* __restrict__ arena, const int32_t* __restrict__ ev,
+                                 const int64_t* __restrict__ meta, int n_gen, int n_events,
+                                 const int64_t* __restrict__ gfirst, const int64_t* __restrict__ base,
+                                 HadronRec* __restrict__ out) {
+    const int64_t total = meta[kDecayMetaSBase + n_gen];
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = n_gen - 1;   // last g with sbase[g] <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (meta[kDecayMetaSBase + mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        const int64_t r = static_cast<int64_t>(lo) * n_events + ev[i];
+        out[base[r] + (i - gfirst[r])] = arena[i];
+    }
+}
 
 }  // namespace
 
@@ -296,40 +540,44 @@ cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_event_bounds(const int32_t* ev, int64_t n, int n_events, int64_t* first,
-                                int64_t* last, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(int64_t) * n_events, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(last, 0xFF, sizeof(int64_t) * n_events, s);
-    if (e != cudaSuccess || n <= 0) return e;
-    event_bounds_kernel<<<grid_for(n), kDecayThreads, 0, s>>>(ev, n, first, last);
+cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                    const DecayBuffers& b, int n_events, int grid, cudaStream_t s) {
+    const size_t ev_bytes = sizeof(int64_t) * static_cast<size_t>(n_events);
+    const int64_t* nin = b.meta + kDecayMetaNIn + gen;
+    const int64_t* sb0 = b.meta + kDecayMetaSBase + gen;
+    const int64_t* sb1 = b.meta + kDecayMetaSBase + gen + 1;
+    cudaError_t e = cudaMemsetAsync(b.first, 0xFF, ev_bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.last, 0xFF, ev_bytes, s);
+    if (e != cudaSuccess) return e;
+    dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.in_ev, nullptr, nin, b.first, b.last);
+    decay_count_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.meta,
+                                                      b.chan, b.ns, b.nu);
+    dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.ns, b.nu, b.meta, gen, b.tiles);
+    dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.s_off, b.u_off);
+    dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.ns, b.nu, b.meta, gen, b.tiles, b.s_off,
+                                                        b.u_off);
+    dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.s_off, b.u_off, b.s_cap, b.u_cap, b.g_max);
+    decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
+                                                      b.meta, b.s_off, b.u_off, b.arena, b.arena_ev,
+                                                      b.out_u, b.out_u_ev, b.failures);
+    // this generation's range of the arena, per event
+    int64_t* gf = b.gfirst + static_cast<int64_t>(gen) * n_events;
+    int64_t* gl = b.glast + static_cast<int64_t>(gen) * n_events;
+    dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.arena_ev, sb0, sb1, gf, gl);
     return cudaGetLastError();
 }
 
-cudaError_t launch_decay_count(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                               const HadronRec* in, const int32_t* ev, const int64_t* first,
-                               int64_t n, int32_t* n_stable, int32_t* n_unstable, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    decay_count_kernel<<<grid_for(n), kDecayThreads, 0, s>>>(cfg, t, gen, in, ev, first, n, n_stable,
-                                                              n_unstable);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_decay_write(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                               const HadronRec* in, const int32_t* ev, const int64_t* first,
-                               int64_t n, const int64_t* s_off, const int64_t* u_off,
-                               HadronRec* out_s, int32_t* ev_s, HadronRec* out_u, int32_t* ev_u,
-                               unsigned long long* failures, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    decay_write_kernel<<<grid_for(n), kDecayThreads, 0, s>>>(cfg, t, gen, in, ev, first, n, s_off,
-                                                              u_off, out_s, ev_s, out_u, ev_u,
-                                                              failures);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_gather(const HadronRec* in, const int32_t* ev, const int64_t* first,
-                          const int64_t* base, int64_t n, HadronRec* out, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    gather_kernel<<<grid_for(n), kDecayThreads, 0, s>>>(in, ev, first, base, n, out);
+cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
+                                  int64_t* tiles, int64_t* off, int64_t* base, HadronRec* out, int grid,
+                                  cudaStream_t s) {
+    if (n_events <= 0) return cudaSuccess;
+    const unsigned eb = static_cast<unsigned>((n_events + 255) / 256);
+    dk_event_totals_kernel<<<eb, 256, 0, s>>>(b.gfirst, b.glast, n_gen, n_events, ev_tot);
+    cudaError_t e = launch_offsets_scan(ev_tot, n_events, tiles, off, s);
+    if (e != cudaSuccess) return e;
+    dk_event_bases_kernel<<<eb, 256, 0, s>>>(b.gfirst, b.glast, off, n_gen, n_events, base);
+    dk_gather_kernel<<<grid, kDecayThreads, 0, s>>>(b.arena, b.arena_ev, b.meta, n_gen, n_events,
+                                                    b.gfirst, base, out);
     return cudaGetLastError();
 }
 

@@ -50,7 +50,8 @@ class Timings(C.Structure):
                 ("ms_counts", C.c_double), ("ms_sample", C.c_double), ("ms_total", C.c_double),
                 ("n_hadrons", C.c_int64), ("n_tries", C.c_int64),
                 ("n_cell_redraws", C.c_int64), ("n_failures", C.c_int64),
-                ("kernel_launches", C.c_int32), ("ms_decays", C.c_double)]
+                ("kernel_launches", C.c_int32), ("ms_decays", C.c_double),
+                ("decay_reruns", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -273,6 +273,48 @@ def test_resonance_decays_final_state():
     assert t["ms_decays"] > 0 and t["n_failures"] == 0
 
 
+def test_decay_order_determinism_and_buffer_reruns():
+    """The final lists in the reference's breadth-first order
+    (src/FSSW.cpp:1746-1779): an event's list starts with its first
+    generation -- each primary in order, itself if stable, else its stable
+    daughters -- so the stable primaries appear unchanged and in order
+    within the first part of the list, before any product of a later
+    generation.  The same seed gives bit-identical lists, and so
+    does a call whose first buffers are far too small (the device-side
+    generation sizes overflow, the call reruns with larger buffers)."""
+    g = O.load_golden("yields_viscous_14moment.npz")
+    a, _ = run_golden_case(g, n_events=200, seed=91)
+    ha, oa = a.all_hadrons()
+    b, params = run_golden_case(g, n_events=200, seed=91, extra={"perform_decays": 1})
+    hb, ob = b.all_hadrons()
+    assert b.timings()["n_failures"] == 0
+    stable = np.array(sorted(_stable_pids("pdg-s95pv1.dat")))
+    for e in range(200):
+        prim = ha[oa[e]:oa[e + 1]]
+        keep = [r.tobytes() for r in prim[np.isin(prim["pid"], stable)]]
+        fin = [r.tobytes() for r in hb[ob[e]:ob[e + 1]]]
+        # an ordered subsequence, matched greedily; at most 3 daughters per
+        # unstable primary lie between two matches of the first generation
+        j = 0
+        for k, r in enumerate(fin):
+            if j < len(keep) and r == keep[j]:
+                j += 1
+        assert j == len(keep), (e, j, len(keep))
+    # a second call on the same handle (buffers kept) and a fresh handle
+    # forced through reruns give the same bytes
+    b.set_random_seed(91)
+    b.generate_samples()
+    h2, o2 = b.all_hadrons()
+    assert h2.tobytes() == hb.tobytes() and np.array_equal(o2, ob)
+    assert b.timings()["decay_reruns"] == 0
+    c, _ = run_golden_case(g, n_events=200, seed=91,
+                           extra={"perform_decays": 1, "gpu_decay_arena_factor": 0.05,
+                                  "gpu_decay_next_factor": 0.01})
+    h3, o3 = c.all_hadrons()
+    assert c.timings()["decay_reruns"] >= 1
+    assert h3.tobytes() == hb.tobytes() and np.array_equal(o3, ob)
+
+
 def _viscous_params(**kw):
     return dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=0, include_deltaf_shear=1,
                 include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1, **kw)
