@@ -644,7 +644,7 @@ def run_gpu(args, ws, rank, local):
     barrier()
     torch.cuda.synchronize()
     clocks.mark_begin()
-    dev_ms, hadrons, t_sample, t_yields = [], [], [], []
+    dev_ms, hadrons, sampled, t_sample, t_yields = [], [], [], [], []
     phases = {k: 0.0 for k in ("ms_prologue", "ms_yields", "ms_cdf", "ms_counts", "ms_sample")}
     wall0 = time.perf_counter()
     step_wall, gen_wall = [], []
@@ -661,6 +661,7 @@ def run_gpu(args, ws, rank, local):
         # with --decays a step also includes the decays (and counts final hadrons)
         dev_ms.append(t["ms_total"] + (t["ms_decays"] if args.decays else 0.0))
         hadrons.append(t["n_hadrons"])
+        sampled.append(t["n_sampled"])
         t_sample.append(t["ms_sample"])
         t_yields.append(t["ms_yields"])
         for k in phases:
@@ -804,7 +805,8 @@ def run_gpu(args, ws, rank, local):
         peak, peak_kind = peaks()
         # dominant kernel: the sampler
         samp_sec = local_stats[2]
-        nh = local_stats[0]
+        # the sample phase processes the sampled hadrons (before any decays)
+        nh = sum(sampled)
         achieved = nh * ALG_BYTES_PER_HADRON / samp_sec / 1e9
         traffic_per_h = profiled("dram_bytes_per_hadron")
         inst_per_h = profiled("warp_instructions_per_hadron")

@@ -76,6 +76,7 @@ typedef struct iss_timings {
     double ms_decays;     /* resonance decays (perform_decays = 1), not in ms_total   */
     int32_t decay_reruns; /* decay passes rerun because a buffer was too small (the
                              sizes are then kept for later calls; results unchanged) */
+    int64_t n_sampled;    /* hadrons the sampler wrote (before resonance decays)      */
 } iss_timings_t;
 
 /* ---- construction, parameters ------------------------------------------ */

@@ -82,12 +82,13 @@ struct iss_handle {
     DevBuf<DecayParticle> d_dparticles;
     DevBuf<DecayChannel> d_dchannels;
     DevBuf<int32_t> d_dsorted;            // sorted pids, then their indices
+    DevBuf<int2> d_dhash;                 // pid -> particle index (kDecayHash slots)
     int n_decay_particles = 0;
     cudaEvent_t ev_decay[2] = {nullptr, nullptr};
     // decay work buffers (grow-only): next-input ping-pong, the arena of
     // stable products, per-input scratch, per-event bounds and the final list
     DevBuf<HadronRec> dk_u[2], dk_arena, dk_final;
-    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_arena_ev, dk_chan, dk_ns, dk_nu, dk_etot;
+    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_chan, dk_ns, dk_nu, dk_etot;
     DevBuf<int64_t> dk_soff, dk_uoff, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
         dk_base, dk_off, dk_etiles, dk_evoff;
     DevBuf<unsigned long long> dk_fail;
@@ -208,9 +209,9 @@ struct iss_handle {
             d_dparticles.release();
             d_dchannels.release();
             d_dsorted.release();
+            d_dhash.release();
             for (auto* b : {&dk_u[0], &dk_u[1], &dk_arena, &dk_final}) b->release();
-            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_arena_ev, &dk_chan, &dk_ns, &dk_nu,
-                            &dk_etot})
+            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_chan, &dk_ns, &dk_nu, &dk_etot})
                 b->release();
             for (auto* b : {&dk_soff, &dk_uoff, &dk_tiles, &dk_first, &dk_last, &dk_gfirst, &dk_glast,
                             &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
@@ -713,6 +714,19 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         CUDA_TRY(h, cudaMemcpy(h->d_dsorted.ptr, sorted.data(), 4 * sorted.size(),
                                cudaMemcpyHostToDevice));
         h->n_decay_particles = static_cast<int>(by_pid.size());
+        // open-addressing hash of the first index of every pid (linear probing)
+        if (by_pid.size() * 2 > static_cast<size_t>(kDecayHash))
+            return fail(h, ISS_ERR_UNSUPPORTED, "decay table has %zu particles", by_pid.size());
+        std::vector<int2> hash(static_cast<size_t>(kDecayHash), int2{0, -1});
+        for (const auto& pi : by_pid) {
+            if (pi.first == 0) continue;
+            uint32_t j = decay_hash(pi.first);
+            while (hash[j].x != 0) j = (j + 1) & (kDecayHash - 1);
+            hash[j] = int2{pi.first, pi.second};
+        }
+        CUDA_TRY(h, h->d_dhash.reserve(hash.size()));
+        CUDA_TRY(h, cudaMemcpy(h->d_dhash.ptr, hash.data(), sizeof(int2) * hash.size(),
+                               cudaMemcpyHostToDevice));
         h->decay_table_afterburner = h->afterburner;
     }
     DecayTablesDev t;
@@ -720,6 +734,7 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     t.channels = h->d_dchannels.ptr;
     t.sorted_pid = h->d_dsorted.ptr;
     t.sorted_idx = h->d_dsorted.ptr + h->n_decay_particles;
+    t.hash = h->d_dhash.ptr;
     t.n_particles = h->n_decay_particles;
 
     const int64_t n0 = h->n_hadrons;
@@ -748,7 +763,6 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
             CUDA_TRY(h, h->dk_uev[k].reserve(static_cast<size_t>(u_cap)));
         }
         CUDA_TRY(h, h->dk_arena.reserve(static_cast<size_t>(s_cap)));
-        CUDA_TRY(h, h->dk_arena_ev.reserve(static_cast<size_t>(s_cap)));
         CUDA_TRY(h, h->dk_final.reserve(static_cast<size_t>(s_cap)));
         CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(in_cap)));
         CUDA_TRY(h, h->dk_ns.reserve(static_cast<size_t>(in_cap)));
@@ -781,7 +795,6 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
 
         DecayBuffers b{};
         b.arena = h->dk_arena.ptr;
-        b.arena_ev = h->dk_arena_ev.ptr;
         b.chan = h->dk_chan.ptr;
         b.ns = h->dk_ns.ptr;
         b.nu = h->dk_nu.ptr;
@@ -1125,6 +1138,8 @@ iss_status replay_graph(iss_handle* h, bool* done) {
     t.ms_sample = elapsed(h, kEvSampleStart, kEvSample);
     t.ms_total = elapsed(h, kEvStart, kEvSample);
     t.n_hadrons = h->n_hadrons;
+    t.n_sampled = h->n_hadrons;
+    t.decay_reruns = 0;
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures);
@@ -1347,6 +1362,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     t.ms_sample = elapsed(h, kEvSampleStart, kEvSample);
     t.ms_total = elapsed(h, kEvStart, kEvSample);
     t.n_hadrons = h->n_hadrons;
+    t.n_sampled = n_units;
     t.n_tries = static_cast<int64_t>(ctr.tries);
     t.n_cell_redraws = static_cast<int64_t>(ctr.redraws);
     t.n_failures = static_cast<int64_t>(ctr.failures + decay_failures);

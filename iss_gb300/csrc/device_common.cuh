@@ -145,6 +145,10 @@ struct DecayChannel {
     int32_t n_daughters;
     double branching_ratio;
     int32_t daughter[5];
+    // ceil(2^53 x the FP64 sum of the branching ratios of this and the
+    // particle's earlier channels, summed in channel order): a 53-bit uniform
+    // m 2^-53 lies below that sum exactly when m < cum53
+    uint64_t cum53;
 };
 struct DecayTablesDev {
     const DecayParticle* particles;
@@ -152,7 +156,14 @@ struct DecayTablesDev {
     const int32_t* sorted_pid;   // pids in increasing order ...
     const int32_t* sorted_idx;   // ... and their particle indices
     int n_particles;
+    // open-addressing table pid -> particle index: kDecayHash (pid, index)
+    // pairs, linear probing from decay_hash(pid), pid 0 marks an empty slot
+    const int2* hash;
 };
+constexpr int kDecayHash = 2048;
+__host__ __device__ inline uint32_t decay_hash(int32_t pid) {
+    return (static_cast<uint32_t>(pid) * 2654435761u) >> 21;   // 11 bits: kDecayHash slots
+}
 
 // Counters written by the sampler.
 struct SampleCounters {

@@ -139,7 +139,13 @@ bool load_decay_table(const std::string& particle_table_path, int afterburner, D
         p.first_channel = static_cast<int32_t>(out->channels.size());
         p.n_channels = static_cast<int32_t>(r.ch.size());
         out->particles.push_back(p);
-        for (DecayChannel c : r.ch) out->channels.push_back(c);
+        double cum = 0.0;
+        for (DecayChannel c : r.ch) {
+            cum += c.branching_ratio;
+            const double x = std::ceil(std::ldexp(cum, 53));
+            c.cum53 = x <= 0.0 ? 0 : (x >= 18446744073709551615.0 ? ~0ull : static_cast<uint64_t>(x));
+            out->channels.push_back(c);
+        }
     }
     // daughters as indices (the first entry with that pid, as
     // particle_decay::get_particle_mass looks it up)

@@ -98,7 +98,6 @@ struct DecayBuffers {
     HadronRec* out_u;           // next generation's input (unstable products)
     int32_t* out_u_ev;
     HadronRec* arena;           // stable products of all generations
-    int32_t* arena_ev;
     int32_t* chan;              // per input hadron: (type << 16) | channel, or < 0
     int32_t* ns;                // per input hadron: stable products
     int32_t* nu;                // per input hadron: unstable products

@@ -42,46 +42,50 @@ __device__ __forceinline__ uint4 dblock(uint32_t draw, uint32_t i, uint32_t e, u
     return philox4x32_10(make_uint4(draw, i, e, gen | (kTagDecay << 16)), k0, k1);
 }
 
-// index of pid in the decay table (pids sorted with their indices), -1 if absent
-__device__ __forceinline__ int lookup(const DecayTablesDev& t, int pid) {
-    int lo = 0, hi = t.n_particles - 1;
-    while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        const int v = t.sorted_pid[mid];
-        if (v == pid) return t.sorted_idx[mid];
-        if (v < pid) lo = mid + 1; else hi = mid - 1;
+// particle index of pid from the hash table staged in shared memory, -1 if
+// absent (bounded probe)
+__device__ __forceinline__ int lookup_hash(const int2* __restrict__ h, int pid) {
+    uint32_t j = decay_hash(pid);
+    for (int k = 0; k < kDecayHash; k++, j = (j + 1) & (kDecayHash - 1)) {
+        const int2 v = h[j];
+        if (v.x == pid) return v.y;
+        if (v.x == 0) return -1;
     }
     return -1;
 }
 
 // The channel of an unstable particle (cumulated branching ratios against one
 // uniform, src/particle_decay.cpp:283-293), or -1 when the ratios do not
-// reach the uniform.
-__device__ __forceinline__ int pick_channel(const DecayTablesDev& t, int type, double u) {
+// reach the uniform.  The uniform is m 2^-53 (u53) and the FP64 partial sums
+// are held as the integers cum53 = ceil(2^53 sum): sum > u exactly when
+// m < cum53, so the choice equals the FP64 comparison without FP64 work.
+__device__ __forceinline__ int pick_channel(const DecayTablesDev& t, int type, unsigned long long m) {
     const int c0 = t.particles[type].first_channel, nc = t.particles[type].n_channels;
-    double cum = 0.0;
     for (int c = 0; c < nc; c++) {
-        cum += t.channels[c0 + c].branching_ratio;
-        if (cum > u) return c0 + c;
+        if (m < t.channels[c0 + c].cum53) return c0 + c;
     }
     return -1;
+}
+
+__device__ __forceinline__ unsigned long long u53_bits(uint32_t a, uint32_t b) {
+    return (static_cast<unsigned long long>(a >> 5) << 26) | static_cast<unsigned long long>(b >> 6);
 }
 
 struct DecayPlan {
     int type, channel, n;      // n: daughters (0: none written, 1: the particle itself)
 };
 
-__device__ DecayPlan plan(const DecayTablesDev& t, const DevConfig& cfg, int pid, uint32_t i,
-                          uint32_t eg, uint32_t gen) {
+__device__ DecayPlan plan(const DecayTablesDev& t, const int2* __restrict__ hash, const DevConfig& cfg,
+                          int pid, uint32_t i, uint32_t eg, uint32_t gen) {
     DecayPlan d{};
-    d.type = lookup(t, pid);
+    d.type = lookup_hash(hash, pid);
     d.channel = -1;
     if (d.type < 0 || t.particles[d.type].stable) {
         d.n = 1;
         return d;
     }
     const uint4 w = dblock(0u, i, eg, gen, cfg.key0, cfg.key1);
-    d.channel = pick_channel(t, d.type, u53(w.x, w.y));
+    d.channel = pick_channel(t, d.type, u53_bits(w.x, w.y));
     const int nd = d.channel >= 0 ? t.channels[d.channel].n_daughters : 0;
     // the reference decays into two or three bodies only; other channels
     // leave no product (src/particle_decay.cpp:294-330)
@@ -91,6 +95,14 @@ __device__ DecayPlan plan(const DecayTablesDev& t, const DevConfig& cfg, int pid
 
 __device__ __forceinline__ bool daughter_stable(const DecayTablesDev& t, int idx) {
     return idx < 0 || t.particles[idx].stable;
+}
+
+// one 40-byte record as five 8-byte words (records are 8-byte aligned)
+__device__ __forceinline__ void copy_rec(HadronRec* __restrict__ dst, const HadronRec* __restrict__ src) {
+    const uint2* s = reinterpret_cast<const uint2*>(src);
+    uint2* d = reinterpret_cast<uint2*>(dst);
+#pragma unroll
+    for (int k = 0; k < 5; k++) d[k] = s[k];
 }
 
 // channel cache of a hadron: (particle type << 16) | decay channel (the host
@@ -109,11 +121,14 @@ decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
                    const int64_t* __restrict__ meta, int32_t* __restrict__ chan,
                    int32_t* __restrict__ n_stable, int32_t* __restrict__ n_unstable) {
+    __shared__ int2 s_hash[kDecayHash];
+    for (int j = threadIdx.x; j < kDecayHash; j += blockDim.x) s_hash[j] = t.hash[j];
+    __syncthreads();
     const int64_t n = meta_n(meta, gen);
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int e = ev[i];
-        const DecayPlan d = plan(t, cfg, in[i].pid, static_cast<uint32_t>(i - first[e]),
+        const DecayPlan d = plan(t, s_hash, cfg, in[i].pid, static_cast<uint32_t>(i - first[e]),
                                  cfg.event_offset + static_cast<uint32_t>(e), gen);
         int s = 0, u = 0;
         int32_t c;
@@ -169,7 +184,7 @@ __device__ __forceinline__ void boost(const Lorentz& L, float E, float px, float
 __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
                                        const HadronRec& m, int e, uint32_t ie, int type, int channel,
                                        int64_t ps, int64_t pu, HadronRec* __restrict__ out_s,
-                                       int32_t* __restrict__ ev_s, HadronRec* __restrict__ out_u,
+                                       HadronRec* __restrict__ out_u,
                                        int32_t* __restrict__ ev_u,
                                        unsigned long long* __restrict__ failures) {
     const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
@@ -266,7 +281,6 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         r.z = dz;
         if (daughter_stable(t, di)) {
             out_s[ps] = r;
-            ev_s[ps] = e;
             ps++;
         } else {
             out_u[pu] = r;
@@ -281,9 +295,8 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
                    const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
                    const int64_t* __restrict__ s_off, const int64_t* __restrict__ u_off,
-                   HadronRec* __restrict__ out_s, int32_t* __restrict__ ev_s,
-                   HadronRec* __restrict__ out_u, int32_t* __restrict__ ev_u,
-                   unsigned long long* __restrict__ failures) {
+                   HadronRec* __restrict__ out_s, HadronRec* __restrict__ out_u,
+                   int32_t* __restrict__ ev_u, unsigned long long* __restrict__ failures) {
     // a generation that did not fit writes nothing (the host reruns the call)
     if (meta[kDecayMetaFlags] != 0) return;
     const int64_t n = meta_n(meta, gen);
@@ -295,12 +308,11 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
         const int e = ev[i];
         const int64_t ps = sbase + s_off[i];
         if (c == kChanStable) {
-            out_s[ps] = in[i];
-            ev_s[ps] = e;
+            copy_rec(out_s + ps, in + i);
             continue;
         }
         decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF, ps,
-                  u_off[i], out_s, ev_s, out_u, ev_u, failures);
+                  u_off[i], out_s, out_u, ev_u, failures);
     }
 }
 
@@ -316,6 +328,25 @@ __global__ void dk_bounds_kernel(const int32_t* __restrict__ ev, const int64_t* 
         const int e = ev[i];
         if (i == lo || ev[i - 1] != e) first[e] = i;
         if (i == hi - 1 || ev[i + 1] != e) last[e] = i + 1;
+    }
+}
+
+// this generation's arena range per event, from its input range
+// [first[e], last[e]) and the stable-product scan: [sbase + s_off[first],
+// sbase + s_off[last]); -1 where the event has none
+__global__ void dk_gen_bounds_kernel(const int64_t* __restrict__ first, const int64_t* __restrict__ last,
+                                     const int64_t* __restrict__ s_off, const int64_t* __restrict__ meta,
+                                     uint32_t gen, int n_events, int64_t* __restrict__ gfirst,
+                                     int64_t* __restrict__ glast) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_events || meta[kDecayMetaFlags] != 0) return;
+    const int64_t f = first[e];
+    if (f < 0) return;
+    const int64_t sb = meta[kDecayMetaSBase + gen];
+    const int64_t a = s_off[f], b = s_off[last[e]];
+    if (b > a) {
+        gfirst[e] = sb + a;
+        glast[e] = sb + b;
     }
 }
 
@@ -513,23 +544,18 @@ __global__ void dk_event_bases_kernel(const int64_t* __restrict__ gfirst, const 
     }
 }
 
-// final[base[g][e] + i - gfirst[g][e]] = arena[i], g the generation whose
-// arena range holds i
-__global__ void dk_gather_kernel(const HadronRec* __restrict__ arena, const int32_t* __restrict__ ev,
-                                 const int64_t* __restrict__ meta, int n_gen, int n_events,
-                                 const int64_t* __restrict__ gfirst, const int64_t* __restrict__ base,
-                                 HadronRec* __restrict__ out) {
-    const int64_t total = meta[kDecayMetaSBase + n_gen];
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int lo = 0, hi = n_gen - 1;   // last g with sbase[g] <= i
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (meta[kDecayMetaSBase + mid] <= i) lo = mid; else hi = mid - 1;
-        }
-        const int64_t r = static_cast<int64_t>(lo) * n_events + ev[i];
-        out[base[r] + (i - gfirst[r])] = arena[i];
-    }
+// the final list: block (e, g) copies event e's products of generation g,
+// arena[gfirst[g][e] ..) to final[base[g][e] ..), as 8-byte words
+__global__ void dk_gather_kernel(const HadronRec* __restrict__ arena, int n_events,
+                                 const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
+                                 const int64_t* __restrict__ base, HadronRec* __restrict__ out) {
+    const int64_t r = static_cast<int64_t>(blockIdx.y) * n_events + blockIdx.x;
+    const int64_t f = gfirst[r];
+    if (f < 0) return;
+    const int64_t words = 5 * (glast[r] - f);
+    const uint2* src = reinterpret_cast<const uint2*>(arena + f);
+    uint2* dst = reinterpret_cast<uint2*>(out + base[r]);
+    for (int64_t k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
 }
 
 }  // namespace
@@ -544,8 +570,6 @@ cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& 
                                     const DecayBuffers& b, int n_events, int grid, cudaStream_t s) {
     const size_t ev_bytes = sizeof(int64_t) * static_cast<size_t>(n_events);
     const int64_t* nin = b.meta + kDecayMetaNIn + gen;
-    const int64_t* sb0 = b.meta + kDecayMetaSBase + gen;
-    const int64_t* sb1 = b.meta + kDecayMetaSBase + gen + 1;
     cudaError_t e = cudaMemsetAsync(b.first, 0xFF, ev_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.last, 0xFF, ev_bytes, s);
     if (e != cudaSuccess) return e;
@@ -558,12 +582,13 @@ cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& 
                                                         b.u_off);
     dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.s_off, b.u_off, b.s_cap, b.u_cap, b.g_max);
     decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
-                                                      b.meta, b.s_off, b.u_off, b.arena, b.arena_ev,
-                                                      b.out_u, b.out_u_ev, b.failures);
+                                                      b.meta, b.s_off, b.u_off, b.arena, b.out_u,
+                                                      b.out_u_ev, b.failures);
     // this generation's range of the arena, per event
     int64_t* gf = b.gfirst + static_cast<int64_t>(gen) * n_events;
     int64_t* gl = b.glast + static_cast<int64_t>(gen) * n_events;
-    dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.arena_ev, sb0, sb1, gf, gl);
+    dk_gen_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.first, b.last, b.s_off, b.meta, gen,
+                                                                n_events, gf, gl);
     return cudaGetLastError();
 }
 
@@ -576,8 +601,8 @@ cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events
     cudaError_t e = launch_offsets_scan(ev_tot, n_events, tiles, off, s);
     if (e != cudaSuccess) return e;
     dk_event_bases_kernel<<<eb, 256, 0, s>>>(b.gfirst, b.glast, off, n_gen, n_events, base);
-    dk_gather_kernel<<<grid, kDecayThreads, 0, s>>>(b.arena, b.arena_ev, b.meta, n_gen, n_events,
-                                                    b.gfirst, base, out);
+    dk_gather_kernel<<<dim3(static_cast<unsigned>(n_events), static_cast<unsigned>(n_gen)), 256, 0, s>>>(
+        b.arena, n_events, b.gfirst, b.glast, base, out);
     return cudaGetLastError();
 }
 

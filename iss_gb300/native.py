@@ -51,7 +51,7 @@ class Timings(C.Structure):
                 ("n_hadrons", C.c_int64), ("n_tries", C.c_int64),
                 ("n_cell_redraws", C.c_int64), ("n_failures", C.c_int64),
                 ("kernel_launches", C.c_int32), ("ms_decays", C.c_double),
-                ("decay_reruns", C.c_int32)]
+                ("decay_reruns", C.c_int32), ("n_sampled", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
