@@ -88,8 +88,8 @@ struct iss_handle {
     // decay work buffers (grow-only): next-input ping-pong, the arena of
     // stable products, per-input scratch, per-event bounds and the final list
     DevBuf<HadronRec> dk_u[2], dk_arena, dk_final;
-    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_chan, dk_ns, dk_nu, dk_etot;
-    DevBuf<int64_t> dk_soff, dk_uoff, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
+    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_chan, dk_etot;
+    DevBuf<int64_t> dk_cnt, dk_coff, dk_list, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
         dk_base, dk_off, dk_etiles, dk_evoff;
     DevBuf<unsigned long long> dk_fail;
     int64_t dk_scap_hint = 0, dk_ucap_hint = 0;   // sizes the last call needed
@@ -211,10 +211,9 @@ struct iss_handle {
             d_dsorted.release();
             d_dhash.release();
             for (auto* b : {&dk_u[0], &dk_u[1], &dk_arena, &dk_final}) b->release();
-            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_chan, &dk_ns, &dk_nu, &dk_etot})
-                b->release();
-            for (auto* b : {&dk_soff, &dk_uoff, &dk_tiles, &dk_first, &dk_last, &dk_gfirst, &dk_glast,
-                            &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
+            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_chan, &dk_etot}) b->release();
+            for (auto* b : {&dk_cnt, &dk_coff, &dk_list, &dk_tiles, &dk_first, &dk_last, &dk_gfirst,
+                            &dk_glast, &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
                 b->release();
             dk_fail.release();
             learned.release_all();
@@ -755,7 +754,14 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     int64_t s_cap = std::max<int64_t>(h->dk_scap_hint, static_cast<int64_t>(fa * static_cast<double>(n0)) + 64);
     int64_t u_cap = std::max<int64_t>(h->dk_ucap_hint, static_cast<int64_t>(fu * static_cast<double>(n0)) + 64);
     std::vector<int64_t> meta_h(kDecayMetaLen, 0);
+    // the scans add (stable << 32 | unstable) counts of at most 3 each: the
+    // unstable half stays below 2^32 while a generation has < 2^32 / 3 inputs
+    constexpr int64_t kMaxDecayInputs = (int64_t(1) << 32) / 3 - 1;
+    if (n0 > kMaxDecayInputs)
+        return fail(h, ISS_ERR_UNSUPPORTED, "resonance decays of more than %lld sampled hadrons",
+                    static_cast<long long>(kMaxDecayInputs));
     for (int attempt = 0;; attempt++) {
+        u_cap = std::min(u_cap, kMaxDecayInputs);
         const int64_t in_cap = std::max(n0, u_cap);
         CUDA_TRY(h, h->dk_ev0.reserve(static_cast<size_t>(n0)));
         for (int k = 0; k < 2; k++) {
@@ -765,11 +771,10 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         CUDA_TRY(h, h->dk_arena.reserve(static_cast<size_t>(s_cap)));
         CUDA_TRY(h, h->dk_final.reserve(static_cast<size_t>(s_cap)));
         CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(in_cap)));
-        CUDA_TRY(h, h->dk_ns.reserve(static_cast<size_t>(in_cap)));
-        CUDA_TRY(h, h->dk_nu.reserve(static_cast<size_t>(in_cap)));
-        CUDA_TRY(h, h->dk_soff.reserve(static_cast<size_t>(in_cap) + 1));
-        CUDA_TRY(h, h->dk_uoff.reserve(static_cast<size_t>(in_cap) + 1));
-        CUDA_TRY(h, h->dk_tiles.reserve(2 * static_cast<size_t>(in_cap / 4096 + 1)));
+        CUDA_TRY(h, h->dk_cnt.reserve(static_cast<size_t>(in_cap)));
+        CUDA_TRY(h, h->dk_coff.reserve(static_cast<size_t>(in_cap) + 1));
+        CUDA_TRY(h, h->dk_list.reserve(static_cast<size_t>(in_cap)));
+        CUDA_TRY(h, h->dk_tiles.reserve(static_cast<size_t>(in_cap / 4096 + 1)));
         CUDA_TRY(h, h->dk_first.reserve(static_cast<size_t>(E)));
         CUDA_TRY(h, h->dk_last.reserve(static_cast<size_t>(E)));
         CUDA_TRY(h, h->dk_gfirst.reserve(static_cast<size_t>(G) * E));
@@ -796,10 +801,9 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         DecayBuffers b{};
         b.arena = h->dk_arena.ptr;
         b.chan = h->dk_chan.ptr;
-        b.ns = h->dk_ns.ptr;
-        b.nu = h->dk_nu.ptr;
-        b.s_off = h->dk_soff.ptr;
-        b.u_off = h->dk_uoff.ptr;
+        b.cnt = h->dk_cnt.ptr;
+        b.off = h->dk_coff.ptr;
+        b.list = h->dk_list.ptr;
         b.tiles = h->dk_tiles.ptr;
         b.first = h->dk_first.ptr;
         b.last = h->dk_last.ptr;

@@ -119,8 +119,8 @@ __device__ __forceinline__ int64_t meta_n(const int64_t* __restrict__ meta, uint
 __global__ void __launch_bounds__(kDecayThreads)
 decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
-                   const int64_t* __restrict__ meta, int32_t* __restrict__ chan,
-                   int32_t* __restrict__ n_stable, int32_t* __restrict__ n_unstable) {
+                   int64_t* __restrict__ meta, int32_t* __restrict__ chan, int64_t* __restrict__ cnt,
+                   int64_t* __restrict__ list) {
     __shared__ int2 s_hash[kDecayHash];
     for (int j = threadIdx.x; j < kDecayHash; j += blockDim.x) s_hash[j] = t.hash[j];
     __syncthreads();
@@ -145,8 +145,21 @@ decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
             }
         }
         chan[i] = c;
-        n_stable[i] = s;
-        n_unstable[i] = u;
+        cnt[i] = (static_cast<int64_t>(s) << 32) | static_cast<int64_t>(u);
+        // the decaying inputs, appended warp by warp (their products' slots
+        // come from the scan, so the list's order does not matter)
+        const unsigned active = __activemask();
+        const unsigned want = __ballot_sync(active, c >= 0);
+        if (want) {
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(active) - 1;
+            unsigned long long base = 0;
+            if (lane == leader)
+                base = atomicAdd(reinterpret_cast<unsigned long long*>(meta + kDecayMetaNDec + gen),
+                                 static_cast<unsigned long long>(__popc(want)));
+            base = __shfl_sync(active, base, leader);
+            if (c >= 0) list[base + __popc(want & ((1u << lane) - 1u))] = i;
+        }
     }
 }
 
@@ -290,29 +303,41 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
     }
 }
 
+// the stable inputs of a generation, copied unchanged into its arena range
 __global__ void __launch_bounds__(kDecayThreads)
-decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
-                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
-                   const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
-                   const int64_t* __restrict__ s_off, const int64_t* __restrict__ u_off,
-                   HadronRec* __restrict__ out_s, HadronRec* __restrict__ out_u,
-                   int32_t* __restrict__ ev_u, unsigned long long* __restrict__ failures) {
+decay_copy_kernel(uint32_t gen, const HadronRec* __restrict__ in, const int32_t* __restrict__ chan,
+                  const int64_t* __restrict__ meta, const int64_t* __restrict__ off,
+                  HadronRec* __restrict__ out_s) {
     // a generation that did not fit writes nothing (the host reruns the call)
     if (meta[kDecayMetaFlags] != 0) return;
     const int64_t n = meta_n(meta, gen);
     const int64_t sbase = meta[kDecayMetaSBase + gen];
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (chan[i] == kChanStable) copy_rec(out_s + sbase + (off[i] >> 32), in + i);
+    }
+}
+
+// the decaying inputs of a generation (its list), each writing its products
+// at its scan offsets
+__global__ void __launch_bounds__(kDecayThreads)
+decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
+                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
+                   const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
+                   const int64_t* __restrict__ list, const int64_t* __restrict__ off,
+                   HadronRec* __restrict__ out_s, HadronRec* __restrict__ out_u,
+                   int32_t* __restrict__ ev_u, unsigned long long* __restrict__ failures) {
+    if (meta[kDecayMetaFlags] != 0) return;
+    const int64_t nd = meta[kDecayMetaNDec + gen];
+    const int64_t sbase = meta[kDecayMetaSBase + gen];
+    for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nd;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t i = list[k];
         const int32_t c = chan[i];
-        if (c == kChanNone) continue;
         const int e = ev[i];
-        const int64_t ps = sbase + s_off[i];
-        if (c == kChanStable) {
-            copy_rec(out_s + ps, in + i);
-            continue;
-        }
-        decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF, ps,
-                  u_off[i], out_s, out_u, ev_u, failures);
+        const int64_t o = off[i];
+        decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF,
+                  sbase + (o >> 32), o & 0xFFFFFFFFll, out_s, out_u, ev_u, failures);
     }
 }
 
@@ -332,10 +357,10 @@ __global__ void dk_bounds_kernel(const int32_t* __restrict__ ev, const int64_t* 
 }
 
 // this generation's arena range per event, from its input range
-// [first[e], last[e]) and the stable-product scan: [sbase + s_off[first],
-// sbase + s_off[last]); -1 where the event has none
+// [first[e], last[e]) and the stable half of the packed scan: [sbase +
+// stable(off[first]), sbase + stable(off[last])); -1 where the event has none
 __global__ void dk_gen_bounds_kernel(const int64_t* __restrict__ first, const int64_t* __restrict__ last,
-                                     const int64_t* __restrict__ s_off, const int64_t* __restrict__ meta,
+                                     const int64_t* __restrict__ off, const int64_t* __restrict__ meta,
                                      uint32_t gen, int n_events, int64_t* __restrict__ gfirst,
                                      int64_t* __restrict__ glast) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,7 +368,7 @@ __global__ void dk_gen_bounds_kernel(const int64_t* __restrict__ first, const in
     const int64_t f = first[e];
     if (f < 0) return;
     const int64_t sb = meta[kDecayMetaSBase + gen];
-    const int64_t a = s_off[f], b = s_off[last[e]];
+    const int64_t a = off[f] >> 32, b = off[last[e]] >> 32;
     if (b > a) {
         gfirst[e] = sb + a;
         glast[e] = sb + b;
@@ -394,93 +419,75 @@ __device__ long long dk_block_excl(long long v, long long* s_warp, long long* to
     return out;
 }
 
-// tile sums of both arrays: tiles[2 t] (stable), tiles[2 t + 1] (unstable)
+// Exclusive scan of the packed counts (stable << 32 | unstable): one int64
+// scan gives both offsets, since no partial sum of the unstable half reaches
+// 2^32 (it is bounded by the next-input capacity).
+// tile sums: tiles[t] for the tiles of 4096 inputs
 __global__ void __launch_bounds__(kDkScanThreads)
-dk_tile_sum_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b,
-                   const int64_t* __restrict__ meta, uint32_t gen, int64_t* __restrict__ tiles) {
+dk_tile_sum_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ meta, uint32_t gen,
+                   int64_t* __restrict__ tiles) {
     __shared__ long long s_warp[33];
     const int64_t n = meta_n(meta, gen);
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
     for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
-        long long sa = 0, sb = 0;
+        long long acc = 0;
         for (int k = 0; k < kDkScanPer; k++) {
             const int64_t i = tl * kDkTile + k * kDkScanThreads + threadIdx.x;
-            if (i < n) {
-                sa += a[i];
-                sb += b[i];
-            }
+            if (i < n) acc += c[i];
         }
-        long long ta, tb;
-        dk_block_excl(sa, s_warp, &ta);
-        dk_block_excl(sb, s_warp, &tb);
-        if (threadIdx.x == 0) {
-            tiles[2 * tl] = ta;
-            tiles[2 * tl + 1] = tb;
-        }
+        long long tot;
+        dk_block_excl(acc, s_warp, &tot);
+        if (threadIdx.x == 0) tiles[tl] = tot;
     }
 }
 
-// one block: tile sums -> tile offsets (in place), totals to oa[n], ob[n]
+// one block: tile sums -> tile offsets (in place), the total to off[n]
 __global__ void __launch_bounds__(kDkScanThreads)
 dk_tile_offset_kernel(int64_t* __restrict__ tiles, const int64_t* __restrict__ meta, uint32_t gen,
-                      int64_t* __restrict__ oa, int64_t* __restrict__ ob) {
+                      int64_t* __restrict__ off) {
     __shared__ long long s_warp[33];
     const int64_t n = meta_n(meta, gen);
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
-    long long ca = 0, cb = 0;
+    long long carry = 0;
     for (int64_t b0 = 0; b0 < nt; b0 += kDkScanThreads) {
         const int64_t i = b0 + threadIdx.x;
-        const long long va = i < nt ? tiles[2 * i] : 0, vb = i < nt ? tiles[2 * i + 1] : 0;
-        long long ta, tb;
-        const long long ea = dk_block_excl(va, s_warp, &ta);
-        const long long eb = dk_block_excl(vb, s_warp, &tb);
-        if (i < nt) {
-            tiles[2 * i] = ca + ea;
-            tiles[2 * i + 1] = cb + eb;
-        }
-        ca += ta;
-        cb += tb;
+        const long long v = i < nt ? tiles[i] : 0;
+        long long tot;
+        const long long ex = dk_block_excl(v, s_warp, &tot);
+        if (i < nt) tiles[i] = carry + ex;
+        carry += tot;
     }
-    if (threadIdx.x == 0) {
-        oa[n] = ca;
-        ob[n] = cb;
-    }
-}
-
-__device__ void dk_tile_scan_one(const int32_t* __restrict__ c, int64_t n, int64_t t0, long long base,
-                                 int32_t* s_in, long long* s_warp, int64_t* __restrict__ out) {
-    for (int k = 0; k < kDkScanPer; k++) {
-        const int e = k * kDkScanThreads + threadIdx.x;
-        const int64_t i = t0 + e;
-        s_in[(e / kDkScanPer) * (kDkScanPer + 1) + e % kDkScanPer] = i < n ? c[i] : 0;
-    }
-    __syncthreads();
-    const int32_t* mine = s_in + threadIdx.x * (kDkScanPer + 1);
-    long long acc = 0;
-#pragma unroll
-    for (int k = 0; k < kDkScanPer; k++) acc += mine[k];
-    long long tot;
-    long long run = base + dk_block_excl(acc, s_warp, &tot);
-    const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kDkScanPer;
-#pragma unroll
-    for (int k = 0; k < kDkScanPer; k++) {
-        if (e0 + k < n) out[e0 + k] = run;
-        run += mine[k];
-    }
-    __syncthreads();
+    if (threadIdx.x == 0) off[n] = carry;
 }
 
 __global__ void __launch_bounds__(kDkScanThreads)
-dk_tile_scan_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b,
-                    const int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ tiles,
-                    int64_t* __restrict__ oa, int64_t* __restrict__ ob) {
-    __shared__ int32_t s_in[kDkScanThreads * (kDkScanPer + 1)];
+dk_tile_scan_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ meta, uint32_t gen,
+                    const int64_t* __restrict__ tiles, int64_t* __restrict__ off) {
+    __shared__ long long s_in[kDkScanThreads * (kDkScanPer + 1)];
     __shared__ long long s_warp[33];
     const int64_t n = meta_n(meta, gen);
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
     for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
-        dk_tile_scan_one(a, n, tl * kDkTile, tiles[2 * tl], s_in, s_warp, oa);
-        dk_tile_scan_one(b, n, tl * kDkTile, tiles[2 * tl + 1], s_in, s_warp, ob);
+        const int64_t t0 = tl * kDkTile;
+        for (int k = 0; k < kDkScanPer; k++) {
+            const int e = k * kDkScanThreads + threadIdx.x;
+            const int64_t i = t0 + e;
+            s_in[(e / kDkScanPer) * (kDkScanPer + 1) + e % kDkScanPer] = i < n ? c[i] : 0;
+        }
+        __syncthreads();
+        const long long* mine = s_in + threadIdx.x * (kDkScanPer + 1);
+        long long acc = 0;
+#pragma unroll
+        for (int k = 0; k < kDkScanPer; k++) acc += mine[k];
+        long long tot;
+        long long run = tiles[tl] + dk_block_excl(acc, s_warp, &tot);
+        const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kDkScanPer;
+#pragma unroll
+        for (int k = 0; k < kDkScanPer; k++) {
+            if (e0 + k < n) off[e0 + k] = run;
+            run += mine[k];
+        }
+        __syncthreads();
     }
 }
 
@@ -488,13 +495,12 @@ dk_tile_scan_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b
 // this generation's, the unstable ones are the next input; a generation
 // that does not fit (arena or next input) sets a flag, records what it
 // needed and stops the chain
-__global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ so,
-                                  const int64_t* __restrict__ uo, int64_t s_cap, int64_t u_cap,
-                                  uint32_t g_max) {
+__global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ off,
+                                  int64_t s_cap, int64_t u_cap, uint32_t g_max) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int64_t n = meta[kDecayMetaNIn + gen];
     const int64_t sb = meta[kDecayMetaSBase + gen];
-    const int64_t st = so[n], ut = uo[n];
+    const int64_t st = off[n] >> 32, ut = off[n] & 0xFFFFFFFFll;
     int64_t next_n = ut, next_sb = sb + st;
     if (meta[kDecayMetaFlags] == 0 && next_sb > s_cap) {
         meta[kDecayMetaFlags] |= 1;
@@ -575,19 +581,19 @@ cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& 
     if (e != cudaSuccess) return e;
     dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.in_ev, nullptr, nin, b.first, b.last);
     decay_count_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.meta,
-                                                      b.chan, b.ns, b.nu);
-    dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.ns, b.nu, b.meta, gen, b.tiles);
-    dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.s_off, b.u_off);
-    dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.ns, b.nu, b.meta, gen, b.tiles, b.s_off,
-                                                        b.u_off);
-    dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.s_off, b.u_off, b.s_cap, b.u_cap, b.g_max);
+                                                      b.chan, b.cnt, b.list);
+    dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles);
+    dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.off);
+    dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles, b.off);
+    dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.g_max);
+    decay_copy_kernel<<<grid, kDecayThreads, 0, s>>>(gen, b.in, b.chan, b.meta, b.off, b.arena);
     decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
-                                                      b.meta, b.s_off, b.u_off, b.arena, b.out_u,
+                                                      b.meta, b.list, b.off, b.arena, b.out_u,
                                                       b.out_u_ev, b.failures);
     // this generation's range of the arena, per event
     int64_t* gf = b.gfirst + static_cast<int64_t>(gen) * n_events;
     int64_t* gl = b.glast + static_cast<int64_t>(gen) * n_events;
-    dk_gen_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.first, b.last, b.s_off, b.meta, gen,
+    dk_gen_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.first, b.last, b.off, b.meta, gen,
                                                                 n_events, gf, gl);
     return cudaGetLastError();
 }
