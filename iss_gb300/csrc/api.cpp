@@ -89,7 +89,7 @@ struct iss_handle {
     // stable products, per-input scratch, per-event bounds and the final list
     DevBuf<HadronRec> dk_u[2], dk_arena, dk_final;
     DevBuf<int32_t> dk_uev[2], dk_ev0, dk_chan, dk_etot;
-    DevBuf<int64_t> dk_cnt, dk_coff, dk_list, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
+    DevBuf<int64_t> dk_cnt, dk_coff, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
         dk_base, dk_off, dk_etiles, dk_evoff;
     DevBuf<unsigned long long> dk_fail;
     int64_t dk_scap_hint = 0, dk_ucap_hint = 0;   // sizes the last call needed
@@ -212,7 +212,7 @@ struct iss_handle {
             d_dhash.release();
             for (auto* b : {&dk_u[0], &dk_u[1], &dk_arena, &dk_final}) b->release();
             for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_chan, &dk_etot}) b->release();
-            for (auto* b : {&dk_cnt, &dk_coff, &dk_list, &dk_tiles, &dk_first, &dk_last, &dk_gfirst,
+            for (auto* b : {&dk_cnt, &dk_coff, &dk_tiles, &dk_first, &dk_last, &dk_gfirst,
                             &dk_glast, &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
                 b->release();
             dk_fail.release();
@@ -773,7 +773,6 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(in_cap)));
         CUDA_TRY(h, h->dk_cnt.reserve(static_cast<size_t>(in_cap)));
         CUDA_TRY(h, h->dk_coff.reserve(static_cast<size_t>(in_cap) + 1));
-        CUDA_TRY(h, h->dk_list.reserve(static_cast<size_t>(in_cap)));
         CUDA_TRY(h, h->dk_tiles.reserve(static_cast<size_t>(in_cap / 4096 + 1)));
         CUDA_TRY(h, h->dk_first.reserve(static_cast<size_t>(E)));
         CUDA_TRY(h, h->dk_last.reserve(static_cast<size_t>(E)));
@@ -803,7 +802,6 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         b.chan = h->dk_chan.ptr;
         b.cnt = h->dk_cnt.ptr;
         b.off = h->dk_coff.ptr;
-        b.list = h->dk_list.ptr;
         b.tiles = h->dk_tiles.ptr;
         b.first = h->dk_first.ptr;
         b.last = h->dk_last.ptr;

@@ -80,7 +80,7 @@ cudaError_t launch_learned_train_rows(const DevConfig& cfg, const CellArrays& ce
 // time, sizes kept on the device.  DecayMeta (int64 slots of `meta`):
 // kDecayMetaNIn + g the input size of generation g (g <= g_max),
 // kDecayMetaSBase + g the start of generation g's stable products in the
-// arena, kDecayMetaNDec + g its decaying inputs (listed in `list`), kDecayMetaFlags (1: arena too small, 2: next input buffer too small,
+// arena, kDecayMetaFlags (1: arena too small, 2: next input buffer too small,
 // 4: chains longer than g_max), kDecayMetaNeedS / NeedU what the failing
 // generation needed, kDecayMetaMaxU the largest next input seen.
 constexpr int kDecayMetaFlags = 0;
@@ -90,8 +90,7 @@ constexpr int kDecayMetaMaxU = 3;
 constexpr int kDecayMetaNIn = 8;
 constexpr int kDecayMaxGenerations = 64;
 constexpr int kDecayMetaSBase = kDecayMetaNIn + kDecayMaxGenerations + 1;
-constexpr int kDecayMetaNDec = kDecayMetaSBase + kDecayMaxGenerations + 1;   // decaying inputs
-constexpr int kDecayMetaLen = kDecayMetaNDec + kDecayMaxGenerations + 1;
+constexpr int kDecayMetaLen = kDecayMetaSBase + kDecayMaxGenerations + 1;
 
 struct DecayBuffers {
     const HadronRec* in;        // this generation's input (event-sorted)
@@ -102,7 +101,6 @@ struct DecayBuffers {
     int32_t* chan;              // per input hadron: (type << 16) | channel, or < 0
     int64_t* cnt;               // per input hadron: (stable products << 32) | unstable ones
     int64_t* off;               // exclusive scan of cnt (input size + 1): both offsets at once
-    int64_t* list;              // the decaying inputs of the generation (any order)
     int64_t* tiles;             // one per scan tile of 4096 inputs
     int64_t* first;             // [n_events] first input of each event (-1: none)
     int64_t* last;

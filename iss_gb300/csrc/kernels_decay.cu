@@ -119,8 +119,8 @@ __device__ __forceinline__ int64_t meta_n(const int64_t* __restrict__ meta, uint
 __global__ void __launch_bounds__(kDecayThreads)
 decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
-                   int64_t* __restrict__ meta, int32_t* __restrict__ chan, int64_t* __restrict__ cnt,
-                   int64_t* __restrict__ list) {
+                   const int64_t* __restrict__ meta, int32_t* __restrict__ chan,
+                   int64_t* __restrict__ cnt) {
     __shared__ int2 s_hash[kDecayHash];
     for (int j = threadIdx.x; j < kDecayHash; j += blockDim.x) s_hash[j] = t.hash[j];
     __syncthreads();
@@ -146,20 +146,6 @@ decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
         }
         chan[i] = c;
         cnt[i] = (static_cast<int64_t>(s) << 32) | static_cast<int64_t>(u);
-        // the decaying inputs, appended warp by warp (their products' slots
-        // come from the scan, so the list's order does not matter)
-        const unsigned active = __activemask();
-        const unsigned want = __ballot_sync(active, c >= 0);
-        if (want) {
-            const int lane = threadIdx.x & 31;
-            const int leader = __ffs(active) - 1;
-            unsigned long long base = 0;
-            if (lane == leader)
-                base = atomicAdd(reinterpret_cast<unsigned long long*>(meta + kDecayMetaNDec + gen),
-                                 static_cast<unsigned long long>(__popc(want)));
-            base = __shfl_sync(active, base, leader);
-            if (c >= 0) list[base + __popc(want & ((1u << lane) - 1u))] = i;
-        }
     }
 }
 
@@ -303,42 +289,55 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
     }
 }
 
-// the stable inputs of a generation, copied unchanged into its arena range
-__global__ void __launch_bounds__(kDecayThreads)
-decay_copy_kernel(uint32_t gen, const HadronRec* __restrict__ in, const int32_t* __restrict__ chan,
-                  const int64_t* __restrict__ meta, const int64_t* __restrict__ off,
-                  HadronRec* __restrict__ out_s) {
-    // a generation that did not fit writes nothing (the host reruns the call)
-    if (meta[kDecayMetaFlags] != 0) return;
-    const int64_t n = meta_n(meta, gen);
-    const int64_t sbase = meta[kDecayMetaSBase + gen];
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        if (chan[i] == kChanStable) copy_rec(out_s + sbase + (off[i] >> 32), in + i);
-    }
-}
+// The write pass of a generation.  Each warp walks its chunks of 32 inputs:
+// stable inputs are copied into the arena at once, decaying ones are queued
+// in shared memory, and whenever 32 are queued the whole warp decays them
+// together, so lanes that copy do not wait on lanes that decay.  Every
+// product goes to the slot its scan offsets give, whatever the order.
+constexpr int kDecayQueue = 64;
 
-// the decaying inputs of a generation (its list), each writing its products
-// at its scan offsets
 __global__ void __launch_bounds__(kDecayThreads)
 decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
                    const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
-                   const int64_t* __restrict__ list, const int64_t* __restrict__ off,
-                   HadronRec* __restrict__ out_s, HadronRec* __restrict__ out_u,
-                   int32_t* __restrict__ ev_u, unsigned long long* __restrict__ failures) {
+                   const int64_t* __restrict__ off, HadronRec* __restrict__ out_s,
+                   HadronRec* __restrict__ out_u, int32_t* __restrict__ ev_u,
+                   unsigned long long* __restrict__ failures) {
+    __shared__ int64_t s_q[kDecayThreads / 32][kDecayQueue];
+    // a generation that did not fit writes nothing (the host reruns the call)
     if (meta[kDecayMetaFlags] != 0) return;
-    const int64_t nd = meta[kDecayMetaNDec + gen];
+    const int64_t n = meta_n(meta, gen);
     const int64_t sbase = meta[kDecayMetaSBase + gen];
-    for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nd;
-         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t i = list[k];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int64_t* q = s_q[wid];
+    int qn = 0;   // queued inputs (warp-uniform, < 32 between chunks)
+    auto decay = [&](int64_t i) {
         const int32_t c = chan[i];
         const int e = ev[i];
         const int64_t o = off[i];
         decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF,
                   sbase + (o >> 32), o & 0xFFFFFFFFll, out_s, out_u, ev_u, failures);
+    };
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+    for (int64_t b0 = (static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + wid) * 32; b0 < n;
+         b0 += warps * 32) {
+        const int64_t i = b0 + lane;
+        const int32_t c = i < n ? chan[i] : kChanNone;
+        if (c == kChanStable) copy_rec(out_s + sbase + (off[i] >> 32), in + i);
+        const unsigned want = __ballot_sync(FULL, c >= 0);
+        if (c >= 0) q[qn + __popc(want & ((1u << lane) - 1u))] = i;
+        qn += __popc(want);
+        __syncwarp();
+        if (qn >= 32) {
+            decay(q[lane]);
+            __syncwarp();
+            if (lane < qn - 32) q[lane] = q[32 + lane];
+            __syncwarp();
+            qn -= 32;
+        }
     }
+    if (lane < qn) decay(q[lane]);
 }
 
 // first[e] = index of event e's first element in the event-sorted range
@@ -581,15 +580,14 @@ cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& 
     if (e != cudaSuccess) return e;
     dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.in_ev, nullptr, nin, b.first, b.last);
     decay_count_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.meta,
-                                                      b.chan, b.cnt, b.list);
+                                                      b.chan, b.cnt);
     dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles);
     dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.off);
     dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles, b.off);
     dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.g_max);
-    decay_copy_kernel<<<grid, kDecayThreads, 0, s>>>(gen, b.in, b.chan, b.meta, b.off, b.arena);
     decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
-                                                      b.meta, b.list, b.off, b.arena, b.out_u,
-                                                      b.out_u_ev, b.failures);
+                                                      b.meta, b.off, b.arena, b.out_u, b.out_u_ev,
+                                                      b.failures);
     // this generation's range of the arena, per event
     int64_t* gf = b.gfirst + static_cast<int64_t>(gen) * n_events;
     int64_t* gl = b.glast + static_cast<int64_t>(gen) * n_events;
