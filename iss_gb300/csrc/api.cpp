@@ -820,7 +820,7 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
                 b.in_ev = g == 0 ? h->dk_ev0.ptr : h->dk_uev[(g - 1) & 1].ptr;
                 b.out_u = h->dk_u[g & 1].ptr;
                 b.out_u_ev = h->dk_uev[g & 1].ptr;
-                CUDA_TRY(h, launch_decay_generation(c, t, static_cast<uint32_t>(g), b, E, grid, s));
+                CUDA_TRY(h, launch_decay_generation(c, t, static_cast<uint32_t>(g), b, E, h->num_sms, s));
             }
             CUDA_TRY(h, cudaMemcpyAsync(&head[0], h->dk_meta.ptr + kDecayMetaNIn + g, 8,
                                         cudaMemcpyDeviceToHost, s));

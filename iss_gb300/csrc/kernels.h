@@ -116,7 +116,7 @@ cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cuda
 // one generation: input bounds, count (channel cache), two scans, sizes of
 // the next generation, write, and this generation's arena bounds per event
 cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                                    const DecayBuffers& b, int n_events, int grid, cudaStream_t s);
+                                    const DecayBuffers& b, int n_events, int num_sms, cudaStream_t s);
 // final lists: per-event totals of generations < n_gen, event offsets (off,
 // n_events + 1), per (generation, event) bases, and the gather into out
 cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,

@@ -296,7 +296,7 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
 // product goes to the slot its scan offsets give, whatever the order.
 constexpr int kDecayQueue = 64;
 
-__global__ void __launch_bounds__(kDecayThreads)
+__global__ void __launch_bounds__(kDecayThreads, 3)
 decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
                    const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
                    const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
@@ -572,7 +572,10 @@ cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cuda
 }
 
 cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                                    const DecayBuffers& b, int n_events, int grid, cudaStream_t s) {
+                                    const DecayBuffers& b, int n_events, int num_sms, cudaStream_t s) {
+    // grid-stride kernels launched with what fits on the SMs at once: eight
+    // blocks of 256 for the light ones, three for the write pass (80 registers)
+    const int grid = num_sms * 8, grid_write = num_sms * 3;
     const size_t ev_bytes = sizeof(int64_t) * static_cast<size_t>(n_events);
     const int64_t* nin = b.meta + kDecayMetaNIn + gen;
     cudaError_t e = cudaMemsetAsync(b.first, 0xFF, ev_bytes, s);
@@ -585,7 +588,7 @@ cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& 
     dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.off);
     dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles, b.off);
     dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.g_max);
-    decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
+    decay_write_kernel<<<grid_write, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
                                                       b.meta, b.off, b.arena, b.out_u, b.out_u_ev,
                                                       b.failures);
     // this generation's range of the arena, per event
