@@ -357,22 +357,41 @@ def surface_spread(s, batch, b_cells, b_events, params, iSS):
     return out
 
 
-def yields_vs_oracle(s, run_params):
-    """Per-species yields of the timed surface (FP32 arithmetic with an FP64
-    reduction on the GPU, read from the handle) against the FP64 CPU oracle
-    (oracle/, the reference's yields restated, pinned bit-exact to the
-    reference's own values): every cell, every species."""
+def _oracle_yields_chunk(job):
+    """FP64 oracle yields of one slice of the cells, summed over the slice
+    (a worker of yields_vs_oracle)."""
+    workload, lo, hi, run_params = job
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib as O
     from iss_gb300 import surfaces as S
-    fo = S.viscous_3d(N_CELLS, seed=SEED_SURFACE).fo_surf()
+    fo = make_surface(workload, WORKLOADS[workload]["cells"]).fo_surf()[lo:hi]
     lrf, keep = O.lrf_cells(fo)
-    sp = O.chosen_species(S.TABLE_DIR, 0)
+    ab = int(run_params.get("afterburner_type", 0))
+    sp = O.chosen_species(S.TABLE_DIR, ab)
     oc = O.OracleConfig(dict(run_params), S.TABLE_DIR, n_events=1, seed=1)
-    ref = O.yields(oc, sp, lrf, keep).sum(1)
+    return O.yields(oc, sp, lrf, keep).sum(1)
+
+
+def yields_vs_oracle(s, run_params, workload="viscous"):
+    """Per-species yields of the timed surface (FP32 arithmetic with an FP64
+    reduction on the GPU, read from the handle) against the FP64 CPU oracle
+    (oracle/, the reference's yields restated, pinned bit-exact to the
+    reference's own values): every cell, every species.  The cells are split
+    over one process per host core (the per-cell yields are independent)."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib as O
+    from iss_gb300 import surfaces as S
+    n = WORKLOADS[workload]["cells"]
+    k = max(1, min(os.cpu_count() or 1, 32))
+    edges = np.linspace(0, n, k + 1).astype(np.int64)
+    jobs = [(workload, int(edges[j]), int(edges[j + 1]), dict(run_params)) for j in range(k)]
+    with mp.get_context("spawn").Pool(k) as pool:
+        ref = np.sum(pool.map(_oracle_yields_chunk, jobs, chunksize=1), axis=0)
+    sp = O.chosen_species(S.TABLE_DIR, int(run_params.get("afterburner_type", 0)))
     gpu = s.species_yields()
     rel = np.abs(gpu - ref) / np.maximum(np.abs(ref), 1e-300)
-    return {"cells": int(fo.shape[0]), "species": int(len(sp)), "max_rel_err": float(rel.max()),
+    return {"cells": int(n), "species": int(len(sp)), "max_rel_err": float(rel.max()),
             "median_rel_err": float(np.median(rel)), "bar": 1e-6,
             "worst_species_pid": int(sp["pid"][int(rel.argmax())])}
 
@@ -489,17 +508,20 @@ def learned_report(s, args):
                                   "ms_per_step": s.timings()["ms_total"]}
     s.set_params(gpu_learned_exact=1, gpu_sampler=0)
     n_ev = int(s.getVal("number_of_repeated_sampling"))
-    n_cmp = min(args.spectra_events, n_ev)
+    n_cmp = min(args.spectra_events or (200 if args.workload == "finite_density" else 1000), n_ev)
+
+    def first_events():
+        # the first n_cmp events only (one copy per event)
+        return np.concatenate([s.get_hadron_list_iev(e) for e in range(n_cmp)])
+
     s.set_random_seed(99)
     s.generate_samples()
-    plain, off = s.all_hadrons()
-    plain = plain[:off[n_cmp]].copy()
+    plain = first_events()
     s.set_params(gpu_sampler=1)
     s.set_random_seed(99)
     s.generate_samples()
     st = s.learned_stats()
-    lrn, off = s.all_hadrons()
-    lrn = lrn[:off[n_cmp]]
+    lrn = first_events()
     assert len(lrn) == len(plain)
     # the learned species: the most abundant ones (the pair tables take the
     # species with enough hadrons per cell)
@@ -775,10 +797,11 @@ def run_gpu(args, ws, rank, local):
         learned.update(learned_report(s, args))
         s.set_params(gpu_sampler=0)
     yields_check = None
-    if rank == 0 and args.workload == "viscous" and args.cells == N_CELLS and not args.no_oracle_check:
+    if (rank == 0 and args.workload in ("viscous", "finite_density")
+            and args.cells == WORKLOADS[args.workload]["cells"] and not args.no_oracle_check):
         s.set_params(gpu_sampler=0)
         s.generate_samples()
-        yields_check = yields_vs_oracle(s, params)
+        yields_check = yields_vs_oracle(s, params, args.workload)
     per_surface = None
     if batch is not None and rank == 0:
         per_surface = surface_spread(s, batch, b_cells, b_events, params, iSS)
@@ -958,8 +981,9 @@ def main():
     ap.add_argument("--no-learned", dest="learned_arm", action="store_false",
                     help="skip the learned arm of the default line (training, timed steps with "
                          "gpu_sampler = 1, spectra against the plain sampler)")
-    ap.add_argument("--spectra-events", type=int, default=1000,
-                    help="events of the learned-vs-plain spectra comparison")
+    ap.add_argument("--spectra-events", type=int, default=None,
+                    help="events of the learned-vs-plain spectra comparison (default 1000; 200 for "
+                         "the finite-density surface)")
     ap.add_argument("--train-momenta", type=int, default=50_000_000)
     ap.add_argument("--train-steps", type=int, default=3000)
     args = ap.parse_args()
