@@ -228,3 +228,45 @@ def test_network_lowers_the_proposals_of_the_mixture_branch(trained):
     assert st["n_excess_tries"] == 0 and st0["n_excess_tries"] == 0
     assert st["n_violations"] <= 3e-3 * st["n_tries"], st
     assert st["n_tries"] < 0.97 * st0["n_tries"], (st, st0)
+
+
+def test_learned_sampler_exact_at_finite_density():
+    """The finite-density configuration (mu_B up to 0.4 GeV, baryon diffusion,
+    SMASH species): the network retrained on that surface's plain samples,
+    then the exact learned sampler against the plain one on the same events --
+    counts and ids bit-identical, no violation, and the spectra of the
+    learned species consistent (at most 2 of the tests below p = 0.01, none
+    below the family-wise level)."""
+    surf = S.finite_density_3d(6000, seed=3)
+    s = iSS(".", inputfile="")
+    params = dict(S.DEFAULT_PARAMETERS, hydro_mode=2, afterburner_type=2, include_deltaf_shear=1,
+                  include_deltaf_bulk=1, bulk_deltaf_kind=11, turn_on_bulk=1,
+                  include_deltaf_diffusion=1, turn_on_rhob=1, turn_on_diff=1,
+                  quantum_statistics=1, dN_dy_sampling_model=30, number_of_repeated_sampling=10)
+    s.set_params(**params)
+    s.set_surface(surf.fo_surf())
+    curve = s.learned_train(n_momenta=2_000_000, first_seed=10, n_seeds=4, n_steps=800,
+                            batch=8192, learning_rate=2e-3, init_seed=1)
+    assert np.all(np.isfinite(curve)) and curve[-50:].mean() < curve[:20].mean()
+    s.set_params(number_of_repeated_sampling=600, gpu_sampler=0)
+    s.set_random_seed(5)
+    s.generate_samples()
+    plain, _ = s.all_hadrons()
+    c_plain = s.counts()
+    learned, c_learned, st, _ = _learned_run(s, 0.8, seed=5)
+    np.testing.assert_array_equal(c_plain, c_learned)
+    np.testing.assert_array_equal(plain["pid"], learned["pid"])
+    assert st["n_species"] >= 3 and st["n_violations"] == 0, st
+    pids = s.species()[np.argsort(-s.species_yields())][:st["n_species"]]
+    pvals = {}
+    for pid in pids[:6]:
+        a, b = plain[plain["pid"] == pid], learned[learned["pid"] == pid]
+        if len(a) < 5000:
+            continue
+        for k, v in spectra_pvalues(a, b).items():
+            pvals[(int(pid), k)] = v
+    assert len(pvals) >= 10
+    low = sorted(pvals.items(), key=lambda kv: kv[1])
+    assert sum(v < 0.01 for v in pvals.values()) <= 2, low[:5]
+    assert low[0][1] > ALPHA / len(pvals), low[:5]
+    s.close()
