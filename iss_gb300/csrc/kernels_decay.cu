@@ -105,6 +105,16 @@ __device__ __forceinline__ void copy_rec(HadronRec* __restrict__ dst, const Hadr
     for (int k = 0; k < 5; k++) d[k] = s[k];
 }
 
+// a record built in registers, stored as five 8-byte words
+__device__ __forceinline__ void store_rec(HadronRec* __restrict__ dst, const HadronRec& r) {
+    float2* d = reinterpret_cast<float2*>(dst);
+    d[0] = make_float2(__int_as_float(r.pid), r.mass);
+    d[1] = make_float2(r.E, r.px);
+    d[2] = make_float2(r.py, r.pz);
+    d[3] = make_float2(r.t, r.x);
+    d[4] = make_float2(r.y, r.z);
+}
+
 // channel cache of a hadron: (particle type << 16) | decay channel (the host
 // checks that both fit), or kChanStable (kept as it is) or kChanNone (no
 // product: no channel reached the uniform, or a channel of other than two
@@ -224,16 +234,20 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         const float span = M - m1 - m2 - m3;
         float E1 = m1, E2 = m2, p1 = 0.f, p2 = 0.f, c12 = 0.f;
         bool ok = false;
-        for (int it = 0; it < kThreeBodyTries && !ok; it++) {
+        // two (E1, E2) candidates per Philox block: (x, y), then (z, w)
+        for (int it = 0; it < kThreeBodyTries / 2 && !ok; it++) {
             const uint4 w = dblock(16u + static_cast<uint32_t>(it), ie, eg, gen, cfg.key0, cfg.key1);
-            E1 = u01f(w.x) * span + m1;
-            E2 = u01f(w.y) * span + m2;
-            if (E1 + E2 > M) continue;
-            p1 = sqrtf(fmaxf(E1 * E1 - m1 * m1, 0.0f));
-            p2 = sqrtf(fmaxf(E2 * E2 - m2 * m2, 0.0f));
-            const float E3 = M - E1 - E2;
-            c12 = (E3 * E3 - p1 * p1 - p2 * p2 - m3 * m3) / (2.0f * p1 * p2);
-            ok = (c12 >= -1.0f && c12 <= 1.0f);
+#pragma unroll
+            for (int h = 0; h < 2 && !ok; h++) {
+                E1 = u01f(h ? w.z : w.x) * span + m1;
+                E2 = u01f(h ? w.w : w.y) * span + m2;
+                if (E1 + E2 > M) continue;
+                p1 = sqrtf(fmaxf(E1 * E1 - m1 * m1, 0.0f));
+                p2 = sqrtf(fmaxf(E2 * E2 - m2 * m2, 0.0f));
+                const float E3 = M - E1 - E2;
+                c12 = (E3 * E3 - p1 * p1 - p2 * p2 - m3 * m3) / (2.0f * p1 * p2);
+                ok = (c12 >= -1.0f && c12 <= 1.0f);
+            }
         }
         if (!ok) {
             atomicAdd(failures, 1ull);
@@ -279,10 +293,10 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         r.y = dy;
         r.z = dz;
         if (daughter_stable(t, di)) {
-            out_s[ps] = r;
+            store_rec(out_s + ps, r);
             ps++;
         } else {
-            out_u[pu] = r;
+            store_rec(out_u + pu, r);
             ev_u[pu] = e;
             pu++;
         }
