@@ -192,6 +192,11 @@ def test_learned_sampler_matches_plain_sampler(trained):
     # c = 1 - M (1 - alpha) against M: at least a few per cent at alpha = 0.8)
     assert 0.01 * st["n_tries"] < st["n_excess_tries"] < 0.8 * st["n_tries"], st
     assert st["n_excess_hadrons"] < st["n_hadrons"]
+    # the bound of an exact envelope certified by a <= 1 alone: no fewer
+    # proposals per hadron than the plain proposal (alpha -> 0, M at its cap)
+    _, _, st0, _ = _learned_run(s, 1e-4, safety=1e6)
+    assert st0["n_hadrons"] == st["n_hadrons"]
+    assert st["n_tries"] >= st0["n_tries"], (st, st0)
     sp = O.chosen_species(S.TABLE_DIR, 0)
     tot = s.species_yields() * n_events
     learned_pids = [int(sp["pid"][k]) for k in np.argsort(-tot)[:st["n_species"]]]
