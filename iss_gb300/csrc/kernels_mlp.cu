@@ -100,7 +100,9 @@ mma_selftest_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __
 
 constexpr int kFwdWG = 3;
 constexpr int kFwdThreads = 128 * kFwdWG;
-constexpr int kFwdSmem = static_cast<int>(kFwdImgElems * 2) + kFwdWG * kTile * kHid * 2 + 64;
+// biases of the hidden layers and the used outputs, staged in shared memory
+constexpr int kFwdBias = (kLayers - 1) * kHid + kOut;
+constexpr int kFwdSmem = static_cast<int>(kFwdImgElems * 2) + kFwdWG * kTile * kHid * 2 + 64 + kFwdBias * 4;
 
 // barrier over the 128 threads of warpgroup `id - 1` (named barrier `id`)
 __device__ __forceinline__ void wg_sync(int id) {
@@ -137,11 +139,16 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
     uint8_t* sH = sW + kFwdImgElems * 2 + g * (kTile * kHid * 2);   // inputs, then activations
     uint64_t* bars = reinterpret_cast<uint64_t*>(sW + kFwdImgElems * 2 + kFwdWG * kTile * kHid * 2);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kFwdWG);
+    float* sBias = reinterpret_cast<float*>(sW + kFwdImgElems * 2 + kFwdWG * kTile * kHid * 2 + 64);
     {
         const uint4* src = reinterpret_cast<const uint4*>(img);
         uint4* dst = reinterpret_cast<uint4*>(sW);
         for (int i = threadIdx.x; i < static_cast<int>(kFwdImgElems * 2 / 16); i += kFwdThreads)
             dst[i] = src[i];
+        for (int i = threadIdx.x; i < kFwdBias; i += kFwdThreads) {
+            const int l = i / kHid, c = i % kHid;
+            sBias[i] = (l < kLayers - 1 || c < kOut) ? params[b_offset(l) + c] : 0.0f;
+        }
     }
     if (threadIdx.x == 0) {
         for (int w = 0; w < kFwdWG; w++) mbar_init(bars + w, 1);
@@ -187,19 +194,25 @@ mlp_fwd_kernel(const __nv_bfloat16* __restrict__ img, const float* __restrict__ 
             if (!ok) break;
             fence_after_sync();
             const float* bias = params + b_offset(l);
+            const float* sb = sBias + l * kHid;
             if (l < kLayers - 1) {
-                for (int c0 = 0; c0 < kHid; c0 += 32) {
-                    float v[32];
-                    tmem_ld32(tmem_lane_addr(tmem, warp, c0), v);
+                // 64 columns per wait: two TMEM loads in flight at a time
+                for (int c0 = 0; c0 < kHid; c0 += 64) {
+                    uint32_t va[32], vb[32];
+                    tmem_ld32_nowait(tmem_lane_addr(tmem, warp, c0), va);
+                    tmem_ld32_nowait(tmem_lane_addr(tmem, warp, c0 + 32), vb);
+                    tmem_wait_ld();
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
+                    for (int q = 0; q < 8; q++) {
                         uint4 pk;
                         uint32_t* pw = reinterpret_cast<uint32_t*>(&pk);
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            const int c = c0 + 8 * q + 2 * j;
-                            pw[j] = pack_bf16x2(fmaxf(v[8 * q + 2 * j] + __ldg(bias + c), 0.0f),
-                                                fmaxf(v[8 * q + 2 * j + 1] + __ldg(bias + c + 1), 0.0f));
+                            const int k = 8 * q + 2 * j;          // column within the 64
+                            const uint32_t x0 = k < 32 ? va[k] : vb[k - 32];
+                            const uint32_t x1 = k < 32 ? va[k + 1] : vb[k - 31];
+                            pw[j] = pack_bf16x2(fmaxf(__uint_as_float(x0) + sb[c0 + k], 0.0f),
+                                                fmaxf(__uint_as_float(x1) + sb[c0 + k + 1], 0.0f));
                         }
                         *reinterpret_cast<uint4*>(sH + kmajor_offset(t, c0 + 8 * q, kHid)) = pk;
                         if (acts && valid)
