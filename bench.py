@@ -536,6 +536,39 @@ def learned_report(s, args):
     return out
 
 
+def batch_stream_e2e(s, batch, b_events, args):
+    """End-to-end steps of a surface batch through the C ABI: every step
+    uploads the batch's surfaces from pinned host memory
+    (iss_gpu_set_surface_batch) and streams all its hadrons to the host
+    (iss_gpu_generate_stream, chunks of --stream-events events through a
+    device ring of two chunks), where a consumer reads each chunk (its
+    checksum of E).  Returns the e2e list of run_gpu's layout."""
+    import torch
+    pinned = [torch.from_numpy(np.ascontiguousarray(b, dtype=np.float32)).pin_memory().numpy()
+              for b in batch]
+    seen = [0, 0.0]
+
+    def consume(had, first, off):
+        seen[0] += len(had)
+        seen[1] += float(had["E"].sum(dtype=np.float64))
+
+    s.set_random_seed(20261203)
+    s.set_surface_batch(pinned, b_events)
+    s.generate_stream(args.stream_events, consume)   # untimed: host buffers, first launches
+    seen[0] = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_surface_batch(pinned, b_events)
+        s.generate_stream(args.stream_events, consume)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    n_in = sum(p.nbytes for p in pinned)
+    n_out = seen[0] * 40
+    s.generate_samples()   # untimed: the handle's hadrons again, for the per-surface report
+    return [seen[0], sec, n_in, n_out // args.steps, [0.0, 1e3 * sec / args.steps], None, None]
+
+
 def e2e_handles(s, make_handle, n_handles, fo_pinned, out_t, steps, step_s, local):
     """End-to-end steps through the C ABI on n_handles handles, each driven by
     its own host thread with its own page-locked output buffer.  A handle's
@@ -599,7 +632,10 @@ def run_gpu(args, ws, rank, local):
         total_cells = int(b_cells.sum())
         fo = None
         n_events = int(b_events.sum())
-        args.no_e2e = True      # the records of a batch (~1e2 GB) stay on the device
+        # the records of a batch (~1e2 GB) do not fit the host buffers of the
+        # e2e leg below: the batch's e2e leg streams them (batch_stream_e2e)
+        batch_e2e = not args.no_e2e
+        args.no_e2e = True
     else:
         surf = make_surface(args.workload, args.cells)
         fo = surf.fo_surf()
@@ -714,6 +750,11 @@ def run_gpu(args, ws, rank, local):
     # end-to-end steps through the C ABI with host buffers
     e2e = None
     e2e_note = None
+    if batch is not None and batch_e2e:
+        e2e = batch_stream_e2e(s, batch, b_events, args)
+        e2e_note = (f"streamed: iss_gpu_set_surface_batch from pinned memory, then "
+                    f"iss_gpu_generate_stream in chunks of {args.stream_events} events through a "
+                    f"device ring of two chunks; a host consumer reads every chunk")
     if not args.no_e2e:
         n_h = max(hadrons)
         out_t = torch.empty((int(n_h * 1.2) + 1024) * 40, dtype=torch.uint8).pin_memory()
@@ -984,6 +1025,8 @@ def main():
     ap.add_argument("--spectra-events", type=int, default=None,
                     help="events of the learned-vs-plain spectra comparison (default 1000; 200 for "
                          "the finite-density surface)")
+    ap.add_argument("--stream-events", type=int, default=1024,
+                    help="events per chunk of the batch workload's streamed e2e leg")
     ap.add_argument("--train-momenta", type=int, default=50_000_000)
     ap.add_argument("--train-steps", type=int, default=3000)
     args = ap.parse_args()

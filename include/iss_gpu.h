@@ -171,6 +171,25 @@ iss_status iss_gpu_generate(iss_handle* h);
 iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capacity,
                                  int64_t* n_total);
 
+/* Streamed generate (no counterpart in the reference, whose hadron lists all
+ * stay in host memory): the same sampling as iss_gpu_generate, with the
+ * hadrons handed to `fn` chunk by chunk instead of kept.  Events are taken
+ * chunk_events at a time; fn(user, hadrons, n, first_event, n_events,
+ * offsets) receives the n hadrons of events [first_event, first_event +
+ * n_events) in a page-locked buffer of the library, event k's records at
+ * [offsets[k], offsets[k+1]).  The buffer is valid until fn returns.  fn runs
+ * on the calling thread while the next chunk is being sampled on the device,
+ * and the device holds the records of two chunks only, so runs whose hadrons
+ * would not fit in device memory at once (large batches, many oversampled
+ * events) stream through a bounded buffer.  The hadrons are the ones
+ * iss_gpu_generate draws for the same seed, bit for bit.  Afterwards the
+ * handle holds timings and counts but no hadrons (the accessors return
+ * ISS_ERR_NO_SAMPLES).  perform_decays needs every event on the device and
+ * returns ISS_ERR_UNSUPPORTED here. */
+typedef void (*iss_stream_fn)(void* user, const iss_hadron_t* hadrons, int64_t n_hadrons,
+                              int32_t first_event, int32_t n_events, const int64_t* event_offsets);
+iss_status iss_gpu_generate_stream(iss_handle* h, int32_t chunk_events, iss_stream_fn fn, void* user);
+
 /* iSS::shell (src/iSS.cpp:41-56): read_surface + set_seed_from_params +
  * generate. */
 iss_status iss_gpu_shell(iss_handle* h);

@@ -113,6 +113,9 @@ struct iss_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;     // device->host copies of iss_gpu_generate_into
     std::vector<cudaEvent_t> chunk_ev;      // end of each sampling chunk
+    std::vector<cudaEvent_t> copy_ev;       // streamed generates: end of each chunk's copy
+    iss_hadron_t* stream_host = nullptr;    // streamed generates: two page-locked chunk buffers
+    int64_t stream_host_cap = 0;            // records per buffer
     cudaEvent_t ev[kEvCount] = {};
     DevBuf<float> d_fo34;
     DevBuf<float4> d_cells;          // 8 arrays of n_cells float4
@@ -204,6 +207,9 @@ struct iss_handle {
                 if (e) cudaEventDestroy(e);
             for (auto& e : chunk_ev)
                 if (e) cudaEventDestroy(e);
+            for (auto& e : copy_ev)
+                if (e) cudaEventDestroy(e);
+            if (stream_host) cudaFreeHost(stream_host);
             for (auto& e : ev_decay)
                 if (e) cudaEventDestroy(e);
             d_dparticles.release();
@@ -937,8 +943,9 @@ iss_status run_learned_pairs(iss_handle* h) {
 // graph's buffers have 15 % headroom over the captured call; a call whose
 // draws do not fit samples nothing (graph_limits_kernel) and runs eagerly.
 
-bool graph_eligible(iss_handle* h, const iss_hadron_t* host_out) {
+bool graph_eligible(iss_handle* h, const iss_hadron_t* host_out, bool streamed = false) {
     return h->params.get_or("gpu_graph", 0) == 1 && !h->graph_unavailable && host_out == nullptr &&
+           !streamed &&
            !h->decays &&
            !h->use_learned && h->params.get_or("sample_upto_desired_particle_number", 0) != 1;
 }
@@ -1160,9 +1167,20 @@ iss_status replay_graph(iss_handle* h, bool* done) {
     return ISS_OK;
 }
 
+// A streamed generate (iss_gpu_generate_stream): the hadrons of every chunk
+// of chunk_events events go to fn, the device keeping two chunks at a time.
+struct StreamSink {
+    int32_t chunk_events;
+    iss_stream_fn fn;
+    void* user;
+};
+
 iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
-                        bool* copied = nullptr) {
+                        bool* copied = nullptr, const StreamSink* sink = nullptr) {
     if (copied) *copied = false;
+    if (sink && h->decays)
+        return fail(h, ISS_ERR_UNSUPPORTED, "perform_decays needs every event's hadrons on the device: "
+                    "not with a streamed generate");
     if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface: call iss_gpu_read_surface first");
     iss_status st = ensure_cuda(h);
     if (st != ISS_OK) return st;
@@ -1170,7 +1188,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     if (st != ISS_OK) return st;
     h->samples_valid = false;
     h->host_valid = false;
-    if (graph_eligible(h, host_out) && h->graph_exec) {
+    if (graph_eligible(h, host_out, sink != nullptr) && h->graph_exec) {
         bool done = false;
         st = replay_graph(h, &done);
         if (st != ISS_OK || done) return st;
@@ -1223,6 +1241,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     const int E = c.n_events;
     int n_chunks = (host_out && !h->decays) ? std::min(h->tune.copy_chunks, std::max(E, 1)) : 1;
     c.chunk_events = std::max(1, (E + n_chunks - 1) / n_chunks);
+    if (sink) c.chunk_events = std::max(1, std::min(sink->chunk_events, std::max(E, 1)));
     n_chunks = std::max(1, (E + c.chunk_events - 1) / c.chunk_events);
     CUDA_TRY(h, h->d_error.reserve(1));
     CUDA_TRY(h, h->d_work.reserve(static_cast<size_t>(n_chunks)));
@@ -1267,7 +1286,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
     chunk_item[n_chunks] = n_items;
     if (count_err == 2) return fail(h, ISS_ERR_OUT_OF_RANGE, "negative particle yield (dN < 0)");
     if (count_err != 0) return fail(h, ISS_ERR_SAMPLING, "count draw did not converge");
-    const bool graph_mode = graph_eligible(h, host_out);
+    const bool graph_mode = graph_eligible(h, host_out, sink != nullptr);
     // a call that will be captured gets 15 % headroom in the buffers whose
     // size depends on the draws, so that later calls fit the same graph
     const auto headroom = [&](int64_t v) { return graph_mode ? v + v / 7 + 1024 : std::max<int64_t>(v, 1); };
@@ -1299,12 +1318,84 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
             h->chunk_ev.push_back(e);
         }
     }
-    CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(headroom(n_units))));
-    CUDA_TRY(h, h->d_cell_of.reserve(static_cast<size_t>(headroom(n_units))));
+    // streamed: the record buffer and cell_of hold two chunks (ring slots
+    // ch & 1), the largest chunk sets their size
+    int64_t ring = 0;
+    if (sink) {
+        for (int ch = 0; ch < n_chunks; ch++) {
+            const int e0 = ch * c.chunk_events, e1 = std::min(E, e0 + c.chunk_events);
+            ring = std::max(ring, h->event_offsets[e1] - h->event_offsets[e0]);
+        }
+        ring = std::max<int64_t>(ring, 1);
+        if (!h->copy_stream)
+            CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        while (static_cast<int>(h->chunk_ev.size()) < n_chunks) {
+            cudaEvent_t e;
+            CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            h->chunk_ev.push_back(e);
+        }
+        while (static_cast<int>(h->copy_ev.size()) < n_chunks) {
+            cudaEvent_t e;
+            CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            h->copy_ev.push_back(e);
+        }
+        if (h->stream_host_cap < ring) {
+            if (h->stream_host) cudaFreeHost(h->stream_host);
+            h->stream_host = nullptr;
+            h->stream_host_cap = 0;
+            CUDA_TRY(h, cudaMallocHost(reinterpret_cast<void**>(&h->stream_host),
+                                       2 * sizeof(iss_hadron_t) * static_cast<size_t>(ring)));
+            h->stream_host_cap = ring;
+        }
+    }
+    CUDA_TRY(h, h->d_hadrons.reserve(static_cast<size_t>(sink ? 2 * ring : headroom(n_units))));
+    CUDA_TRY(h, h->d_cell_of.reserve(static_cast<size_t>(sink ? 2 * ring : headroom(n_units))));
     CUDA_TRY(h, cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long) * n_chunks, s));
     CUDA_TRY(h, cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
     CUDA_TRY(h, cudaEventRecord(h->ev[kEvSampleStart], s));
-    for (int ch = 0; ch < n_chunks; ch++) {
+    // hands chunk ch's records (already copied to the host) to the sink
+    std::vector<int64_t> rel;
+    const auto deliver = [&](int ch) -> iss_status {
+        CUDA_TRY(h, cudaEventSynchronize(h->copy_ev[ch]));
+        const int e0 = ch * c.chunk_events, e1 = std::min(E, e0 + c.chunk_events);
+        const int64_t b = h->event_offsets[e0];
+        rel.assign(static_cast<size_t>(e1 - e0) + 1, 0);
+        for (int e = e0; e <= e1; e++) rel[e - e0] = h->event_offsets[e] - b;
+        sink->fn(sink->user, h->stream_host + (ch & 1) * ring, rel[e1 - e0], e0, e1 - e0, rel.data());
+        return ISS_OK;
+    };
+    for (int ch = 0; ch < n_chunks && sink; ch++) {
+        const int e0 = ch * c.chunk_events, e1 = std::min(E, e0 + c.chunk_events);
+        const int64_t b = h->event_offsets[e0], n = h->event_offsets[e1] - b;
+        const int slot = ch & 1;
+        // ring slot `slot` was last read by the copy of chunk ch - 2
+        if (ch >= 2) CUDA_TRY(h, cudaStreamWaitEvent(s, h->copy_ev[ch - 2], 0));
+        DevConfig cc = c;
+        cc.slot_base = b;
+        CUDA_TRY(h, launch_sampler(cc, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
+                                   h->d_guide.ptr, h->d_qtot.ptr, h->d_offsets.ptr, h->d_item_off.ptr,
+                                   h->d_item_seg.ptr, chunk_item[ch], chunk_item[ch + 1],
+                                   h->d_cell_of.ptr + slot * ring, h->d_hadrons.ptr + slot * ring,
+                                   h->d_work.ptr + ch, h->d_counters.ptr, h->num_sms, s));
+        CUDA_TRY(h, cudaEventRecord(h->chunk_ev[ch], s));
+        // the previous chunk's records reach the caller while this one samples
+        // (its host buffer, slot ^ 1, is free again once the sink returns)
+        if (ch >= 1) {
+            const iss_status dst = deliver(ch - 1);
+            if (dst != ISS_OK) return dst;
+        }
+        CUDA_TRY(h, cudaStreamWaitEvent(h->copy_stream, h->chunk_ev[ch], 0));
+        if (n > 0)
+            CUDA_TRY(h, cudaMemcpyAsync(h->stream_host + slot * ring, h->d_hadrons.ptr + slot * ring,
+                                        sizeof(iss_hadron_t) * static_cast<size_t>(n),
+                                        cudaMemcpyDeviceToHost, h->copy_stream));
+        CUDA_TRY(h, cudaEventRecord(h->copy_ev[ch], h->copy_stream));
+    }
+    if (sink && n_chunks > 0) {
+        const iss_status dst = deliver(n_chunks - 1);
+        if (dst != ISS_OK) return dst;
+    }
+    for (int ch = 0; ch < n_chunks && !sink; ch++) {
         CUDA_TRY(h, launch_sampler(c, cell_arrays(h), h->d_species.ptr, h->d_pids.ptr, h->d_cdf.ptr,
                                    h->d_guide.ptr, h->d_qtot.ptr,
                                    h->d_offsets.ptr, h->d_item_off.ptr, h->d_item_seg.ptr,
@@ -1335,6 +1426,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
 
     h->n_events = c.n_events;
     h->n_hadrons = n_units;
+    const bool streamed = sink != nullptr;
     unsigned long long decay_failures = 0;
     float ms_decays = 0.f;
     if (h->decays) {
@@ -1380,7 +1472,7 @@ iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t
         h->lstats.ms_network = elapsed(h, kEvLearnStart, kEvLearnEnd);
         h->lstats.ms_forward = elapsed(h, kEvFwdStart, kEvFwdEnd);
     }
-    h->samples_valid = true;
+    h->samples_valid = !streamed;   // a streamed generate keeps no records
     if (ctr.error_code == 1) {
         const int k = ctr.error_species;
         return fail(h, ISS_ERR_OUT_OF_RANGE,
@@ -1837,6 +1929,19 @@ iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capac
                     "on the device)", static_cast<long long>(h->n_hadrons),
                     static_cast<long long>(capacity));
     return ISS_OK;
+}
+
+iss_status iss_gpu_generate_stream(iss_handle* h, int32_t chunk_events, iss_stream_fn fn, void* user) {
+    if (!h) return ISS_ERR_INVALID_ARG;
+    if (!fn || chunk_events < 1) return fail(h, ISS_ERR_INVALID_ARG, "no sink or chunk_events < 1");
+    if (!h->seed_set) {
+        iss_status st = iss_gpu_set_seed_from_params(h);
+        if (st != ISS_OK) return st;
+    }
+    const iss_status tst = maybe_autotune(h);
+    if (tst != ISS_OK) return tst;
+    const StreamSink sink{chunk_events, fn, user};
+    return run_generate(h, nullptr, 0, nullptr, &sink);
 }
 
 iss_status iss_gpu_shell(iss_handle* h) {

@@ -88,6 +88,9 @@ struct DevConfig {
     int mc_sampling;         // 4: the FSSW sampler; 2: the lab-frame sampler
     float pt_max, yme_range, df_max_ratio;
     int restrict_df;
+    // streamed generates: the record buffer and cell_of hold one chunk, whose
+    // first record has the global slot slot_base (0 otherwise)
+    int64_t slot_base;
 };
 
 // floats per (species slot, cell) record of the learned proposal: for each of

@@ -1403,8 +1403,8 @@ cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
                 if (c1 <= q1) lo1 = m1; else hi1 = m1 - 1;
             }
         }
-        if (v0) cell_of[base + d0 * mult] = static_cast<int32_t>(sg.c0) + lo0;
-        if (v1) cell_of[base + d1 * mult] = static_cast<int32_t>(sg.c0) + lo1;
+        if (v0) cell_of[base - cfg.slot_base + d0 * mult] = static_cast<int32_t>(sg.c0) + lo0;
+        if (v1) cell_of[base - cfg.slot_base + d1 * mult] = static_cast<int32_t>(sg.c0) + lo1;
         }
     }
 }
@@ -1476,7 +1476,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
             if (!active && rank < avail) {
                 const int64_t d = next + rank;
                 u.s = cur_s;
-                u.slot = seg_base + d * cur_mult;
+                u.slot = seg_base - cfg.slot_base + d * cur_mult;
                 u.i = static_cast<uint32_t>(d);
                 u.mult = cur_mult;
                 u.phase = 0;

@@ -30,7 +30,7 @@ EXPORTED = [
     "iss_gpu_create", "iss_gpu_destroy", "iss_gpu_set_param", "iss_gpu_get_param",
     "iss_gpu_parse_param_line", "iss_gpu_set_seed", "iss_gpu_set_seed_from_params",
     "iss_gpu_read_surface", "iss_gpu_set_surface", "iss_gpu_set_surface_batch",
-    "iss_gpu_generate", "iss_gpu_generate_into",
+    "iss_gpu_generate", "iss_gpu_generate_into", "iss_gpu_generate_stream",
     "iss_gpu_shell",
     "iss_gpu_clear", "iss_gpu_num_events", "iss_gpu_num_particles", "iss_gpu_get_hadron",
     "iss_gpu_copy_event", "iss_gpu_copy_all", "iss_gpu_write_output",
@@ -43,6 +43,11 @@ EXPORTED = [
     "iss_gpu_mma_selftest", "iss_gpu_learned_train", "iss_gpu_learned_stats",
     "iss_gpu_learned_copy_rows", "iss_gpu_get_tuning", "iss_gpu_set_tuning", "iss_gpu_autotune",
 ]
+
+
+# iss_stream_fn(user, hadrons, n_hadrons, first_event, n_events, event_offsets)
+STREAM_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
+                        C.POINTER(C.c_int64))
 
 
 class Timings(C.Structure):
@@ -114,6 +119,7 @@ def lib():
         L.iss_gpu_set_surface_batch.argtypes = [h, v, v, v, C.c_int32]
         L.iss_gpu_generate.argtypes = [h]
         L.iss_gpu_generate_into.argtypes = [h, v, C.c_int64, C.POINTER(C.c_int64)]
+        L.iss_gpu_generate_stream.argtypes = [h, C.c_int32, STREAM_FN, v]
         L.iss_gpu_shell.argtypes = [h]
         L.iss_gpu_clear.argtypes = [h]
         L.iss_gpu_num_events.argtypes = [h, C.POINTER(C.c_int32)]
@@ -258,6 +264,33 @@ class iSS:
         off = np.zeros(nev + 1, dtype=np.int64)
         self._check(self._L.iss_gpu_copy_all(self._h, None, 0, _ptr(off), None))
         return out[:n.value], off
+
+    def generate_stream(self, chunk_events, fn):
+        """generate_samples with the hadrons handed to fn(hadrons, first_event,
+        event_offsets) chunk by chunk (chunk_events events each) instead of
+        kept: `hadrons` is a HADRON_DTYPE view of the library's page-locked
+        buffer, valid only during the call (copy what you keep); event k of
+        the chunk is hadrons[event_offsets[k]:event_offsets[k+1]].  The device
+        holds two chunks of records at a time."""
+        errors = []
+
+        def tramp(user, ptr, n, first, nev, off):
+            try:
+                offs = np.ctypeslib.as_array(off, shape=(nev + 1,)).copy()
+                if n > 0:
+                    buf = (C.c_char * (int(n) * HADRON_DTYPE.itemsize)).from_address(ptr)
+                    had = np.frombuffer(buf, dtype=HADRON_DTYPE, count=int(n))
+                else:
+                    had = np.zeros(0, dtype=HADRON_DTYPE)
+                fn(had, int(first), offs)
+            except Exception as e:   # re-raised after the call
+                errors.append(e)
+
+        cb = STREAM_FN(tramp)
+        st = self._L.iss_gpu_generate_stream(self._h, int(chunk_events), cb, None)
+        if errors:
+            raise errors[0]
+        return self._check(st)
 
     def shell(self):
         return self._check(self._L.iss_gpu_shell(self._h))
