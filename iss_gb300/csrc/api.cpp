@@ -1178,14 +1178,14 @@ struct StreamSink {
 iss_status run_generate(iss_handle* h, iss_hadron_t* host_out = nullptr, int64_t capacity = 0,
                         bool* copied = nullptr, const StreamSink* sink = nullptr) {
     if (copied) *copied = false;
-    if (sink && h->decays)
-        return fail(h, ISS_ERR_UNSUPPORTED, "perform_decays needs every event's hadrons on the device: "
-                    "not with a streamed generate");
     if (!h->surface_loaded) return fail(h, ISS_ERR_NO_SURFACE, "no surface: call iss_gpu_read_surface first");
     iss_status st = ensure_cuda(h);
     if (st != ISS_OK) return st;
     st = prepare(h);
     if (st != ISS_OK) return st;
+    if (sink && h->decays)
+        return fail(h, ISS_ERR_UNSUPPORTED, "perform_decays needs every event's hadrons on the device: "
+                    "not with a streamed generate");
     h->samples_valid = false;
     h->host_valid = false;
     if (graph_eligible(h, host_out, sink != nullptr) && h->graph_exec) {
