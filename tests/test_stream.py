@@ -80,3 +80,25 @@ def test_stream_refuses_decays():
     with pytest.raises(native.IssError):
         s.generate_stream(4, lambda *a: None)
     s.close()
+
+
+@pytest.mark.parametrize("extra", [{"local_charge_conservation": 1},
+                                   {"MC_sampling": 2, "bulk_deltaf_kind": 1, "restrict_deltaf": 1,
+                                    "deltaf_max_ratio": 1.0, "sample_pT_up_to": -1,
+                                    "sample_y_minus_eta_s_range": 3}],
+                         ids=["local_charge_conservation", "MC_sampling_2"])
+def test_stream_equals_generate_other_samplers(extra):
+    """Pairs of records per draw (local charge conservation) and the
+    lab-frame sampler stream bit-identically too."""
+    s = iSS(".", inputfile="")
+    s.set_params(**dict(PARAMS, number_of_repeated_sampling=40, **extra))
+    s.set_surface(S.viscous_3d(2000, seed=9).fo_surf())
+    s.set_random_seed(313)
+    s.generate_samples()
+    ref, ref_off = s.all_hadrons()
+    s.set_random_seed(313)
+    had, off, _ = _collect(s, 6)
+    assert len(ref) > 0
+    assert np.array_equal(off, ref_off)
+    assert had.tobytes() == ref.tobytes()
+    s.close()
