@@ -552,15 +552,18 @@ def batch_stream_e2e(s, batch, b_events, args):
     memory and counts its records (anything heavier would time the consumer,
     not the library).  Returns the e2e list of run_gpu's layout."""
     import torch
-    pinned = [torch.from_numpy(np.ascontiguousarray(b, dtype=np.float32)).pin_memory().numpy()
-              for b in batch]
+    # the batch's records concatenated once into page-locked memory, as a
+    # caller that keeps its surfaces in one buffer would hold them
+    flat = torch.from_numpy(np.concatenate([np.asarray(b, dtype=np.float32) for b in batch])).pin_memory()
+    flat = flat.numpy()
+    cell_off = np.concatenate([[0], np.cumsum([len(b) for b in batch])]).astype(np.int64)
     seen = [0]
 
     def consume(had, first, off):
         seen[0] += len(had)
 
     s.set_random_seed(20261203)
-    s.set_surface_batch(pinned, b_events)
+    s.set_surface_batch_flat(flat, cell_off, b_events)
     s.generate_stream(args.stream_events, consume)   # untimed: host buffers, first launches
     seen[0] = 0
     torch.cuda.synchronize()
@@ -568,12 +571,12 @@ def batch_stream_e2e(s, batch, b_events, args):
     t_set = 0.0
     for _ in range(args.steps):
         ta = time.perf_counter()
-        s.set_surface_batch(pinned, b_events)
+        s.set_surface_batch_flat(flat, cell_off, b_events)
         t_set += time.perf_counter() - ta
         s.generate_stream(args.stream_events, consume)
     torch.cuda.synchronize()
     sec = time.perf_counter() - t0
-    n_in = sum(p.nbytes for p in pinned)
+    n_in = flat.nbytes
     n_out = seen[0] * 40
     s.generate_samples()   # untimed: the handle's hadrons again, for the per-surface report
     return [seen[0], sec, n_in, n_out // args.steps,
@@ -763,7 +766,7 @@ def run_gpu(args, ws, rank, local):
     e2e_note = None
     if batch is not None and batch_e2e:
         e2e = batch_stream_e2e(s, batch, b_events, args)
-        e2e_note = (f"streamed: iss_gpu_set_surface_batch from pinned memory, then "
+        e2e_note = (f"streamed: iss_gpu_set_surface_batch from one pinned buffer, then "
                     f"iss_gpu_generate_stream in chunks of {args.stream_events} events through a "
                     f"device ring of two chunks; a host consumer receives every chunk")
     if not args.no_e2e:

@@ -251,6 +251,16 @@ class iSS:
         return self._check(self._L.iss_gpu_set_surface_batch(self._h, _ptr(recs), _ptr(off),
                                                              _ptr(ev), len(surfaces)))
 
+    def set_surface_batch_flat(self, records, cell_offsets, events):
+        """set_surface_batch on records already concatenated (float32 [n][34],
+        e.g. page-locked) with cell_offsets[b] the first record of surface b
+        (n_surfaces + 1 entries): no host copy before the C ABI call."""
+        assert records.dtype == np.float32 and records.flags.c_contiguous and records.shape[1] == 34
+        off = np.ascontiguousarray(cell_offsets, dtype=np.int64)
+        ev = np.ascontiguousarray(events, dtype=np.int32)
+        return self._check(self._L.iss_gpu_set_surface_batch(self._h, _ptr(records), _ptr(off),
+                                                             _ptr(ev), len(ev)))
+
     def generate_samples(self):
         return self._check(self._L.iss_gpu_generate(self._h))
 
