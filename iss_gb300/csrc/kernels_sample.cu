@@ -200,6 +200,7 @@ __device__ double gamma_draw(uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
 // a work item is cfg.item_size consecutive draws of one (event, species)
 // segment; the cell assignment takes them 64 at a time (two per lane)
 constexpr int kAssignSub = 64;
+constexpr float kTwoPiF = 6.2831853071795865f;
 // guide buckets spanning at most this many cells past their first are
 // resolved with one batch of CDF reads (cell_assign_kernel)
 constexpr int kAssignSpan = 3;
@@ -721,7 +722,10 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
     const float Etil = p.a + K;
     const float em = expf(-Etil);
-    const float a_q = (p.sign == -1) ? p.qa / (-expm1f(-Etil)) : 1.0f / (1.0f + em);
+    // 1 - e^-Etil from em where that is accurate (Etil > 0.05: relative
+    // error below 3e-6); expm1f near Bose condensation only
+    const float a_q = (p.sign == -1) ? p.qa / (Etil > 0.05f ? 1.0f - em : -expm1f(-Etil))
+                                     : 1.0f / (1.0f + em);
     float a_c = 1.0f;
     if (kMode == 0 && p.compat) {
         a_c = compat_ratio(p, Etil) / p.rmax;
@@ -749,7 +753,8 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float cth = fminf(c_lo + 2.0f * uZ / (a_lin + sqrtf(a_lin * a_lin + 2.0f * bD * uZ)), 1.0f);
     const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
     float sphi, cphi;
-    sincospif(2.0f * u01f(B.y), &sphi, &cphi);
+    // azimuth in [-pi, pi), where the SFU's sine and cosine are accurate to 2^-20
+    __sincosf(kTwoPiF * (u01f(B.y) - 0.5f), &sphi, &cphi);
     float e1x, e1y, e1z;
     prop_e1(p, e1x, e1y, e1z);
     const float e2x = p.ny * e1z - p.nz * e1y;

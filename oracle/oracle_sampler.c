@@ -218,7 +218,7 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     if (cth > 1.0) cth = 1.0;
     double sth2 = 1.0 - cth * cth;
     const double sth = sth2 > 0 ? sqrt(sth2) : 0.0;
-    const double phi = 2.0 * ORC_PI * orc_u01(Bw[1]);
+    const double phi = 2.0 * ORC_PI * (orc_u01(Bw[1]) - 0.5);   /* azimuth in [-pi, pi) */
     const double cph = cos(phi), sph = sin(phi);
     const double T = c->T;
     const double pm = T * ptil;
