@@ -525,7 +525,7 @@ __device__ bool setup_prop_lean(const DevConfig& cfg, const CellArrays& cells, c
     p.w3 = 2.0f;
     p.w32 = 2.0f + 2.0f * p.mt;
     p.W = p.w32 + 0.5f * p.mt * p.mt;
-    p.qa = -expm1f(-p.a);
+    p.qa = p.a > 0.05f ? 1.0f - __expf(-p.a) : -expm1f(-p.a);   // as a_q's denominator in the try
     p.compat = 0;
     p.cpoly = p.mut * p.mut - 0.5f * p.mt * p.mt;
     p.rmax = 1.0f;
