@@ -264,13 +264,14 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
     return c;
 }
 
-// [0, 1), 24 bits
+// [0, 1), 23 bits: the top 23 bits as the mantissa of a float in [1, 2),
+// minus 1 (exact; no integer-to-float conversion)
 __device__ __forceinline__ float u01f(uint32_t x) {
-    return static_cast<float>(x >> 8) * (1.0f / 16777216.0f);
+    return __uint_as_float((x >> 9) | 0x3F800000u) - 1.0f;
 }
-// (0, 1], 24 bits
+// (0, 1], 23 bits: 2 minus the same float in [1, 2) (exact, never 0)
 __device__ __forceinline__ float u01f_pos(uint32_t x) {
-    return static_cast<float>((x >> 8) + 1u) * (1.0f / 16777216.0f);
+    return 2.0f - __uint_as_float((x >> 9) | 0x3F800000u);
 }
 // [0, 1), 53 bits
 __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {

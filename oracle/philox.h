@@ -28,11 +28,12 @@ static inline void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t ke
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* [0, 1) with 24-bit resolution (exact in float and double) */
-static inline double orc_u01(uint32_t x) { return (double)(x >> 8) * (1.0 / 16777216.0); }
-/* (0, 1] with 24-bit resolution, safe for log() */
+/* [0, 1) with 23-bit resolution: (x >> 9) 2^-23, the GPU's float built
+ * from those bits as a mantissa in [1, 2) minus 1 (exact in float and double) */
+static inline double orc_u01(uint32_t x) { return (double)(x >> 9) * (1.0 / 8388608.0); }
+/* (0, 1] with 23-bit resolution, safe for log(): 1 - (x >> 9) 2^-23 */
 static inline double orc_u01_pos(uint32_t x) {
-    return (double)((x >> 8) + 1u) * (1.0 / 16777216.0);
+    return (double)(8388608u - (x >> 9)) * (1.0 / 8388608.0);
 }
 /* [0, 1) with 53-bit resolution from two words */
 static inline double orc_u53(uint32_t a, uint32_t b) {
