@@ -28,8 +28,10 @@ CU_SOURCES = ["kernels_prologue.cu", "kernels_cells.cu", "kernels_sample.cu", "k
 # the prologue reproduces the reference's float/double rounding points exactly,
 # so mul+add must not be contracted into FMAs there
 CU_EXTRA = {"kernels_prologue.cu": ["--fmad=false"],
-            # the sampler's acceptance tests tolerate approximate transcendentals
-            "kernels_sample.cu": ["--use_fast_math"]}
+            # the sampler's acceptance tests tolerate approximate transcendentals,
+            # and so do the decay kinematics (energy conserved to 2e-5)
+            "kernels_sample.cu": ["--use_fast_math"],
+            "kernels_decay.cu": ["--use_fast_math"]}
 CXX_SOURCES = ["api.cpp", "learned.cpp", "host/params.cpp", "host/tables.cpp", "host/surface_io.cpp",
                "host/writers.cpp", "shim/iSS.cpp"]
 CLI_SOURCES = ["cli/main.cpp"]

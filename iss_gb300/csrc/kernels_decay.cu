@@ -36,6 +36,8 @@ namespace {
 constexpr int kDecayThreads = 256;
 constexpr uint32_t kTagDecay = 4u;
 constexpr int kThreeBodyTries = 100000;
+// angles uniform on [-pi, pi), where the SFU's sine and cosine are accurate to 2^-20
+constexpr float kTwoPiD = 6.2831853071795865f;
 
 __device__ __forceinline__ uint4 dblock(uint32_t draw, uint32_t i, uint32_t e, uint32_t gen,
                                         uint32_t k0, uint32_t k1) {
@@ -217,7 +219,7 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         const float a = M * M - m1 * m1 - m2 * m2;
         const float p = sqrtf(fmaxf(a * a - 4.0f * m1 * m1 * m2 * m2, 0.0f)) / (2.0f * M);
         float sphi, cphi;
-        sincospif(2.0f * u01f(w1.x), &sphi, &cphi);
+        __sincosf(kTwoPiD * (u01f(w1.x) - 0.5f), &sphi, &cphi);
         const float cth = 2.0f * (u01f(w1.y) - 0.5f);
         const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
         px[0] = p * sth * cphi;
@@ -256,8 +258,8 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         const float tp2x = p2 * sqrtf(fmaxf(1.0f - c12 * c12, 0.0f)), tp2z = p2 * c12;
         const float tp3x = -tp2x, tp3z = -(p1 + tp2z);
         float sphi, cphi, sksi, cksi;
-        sincospif(2.0f * u01f(w1.x), &sphi, &cphi);
-        sincospif(2.0f * u01f(w1.y), &sksi, &cksi);
+        __sincosf(kTwoPiD * (u01f(w1.x) - 0.5f), &sphi, &cphi);
+        __sincosf(kTwoPiD * (u01f(w1.y) - 0.5f), &sksi, &cksi);
         const float cth = 2.0f * u01f(w1.z) - 1.0f;
         const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
         px[0] = -p1 * sth * cksi;
