@@ -1112,7 +1112,7 @@ __device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __re
         const float w = kap < 1e-4f ? 2.0f * uw - 1.0f
                                     : fmaxf(-1.0f, 1.0f + log1pf((1.0f - uw) * expm1f(-2.0f * kap)) / kap);
         float sphi, cphi;
-        sincospif(2.0f * u01f(B.y), &sphi, &cphi);
+        __sincosf(kTwoPiF * (u01f(B.y) - 0.5f), &sphi, &cphi);
         around(mx, my, mz, fminf(w, 1.0f), sphi, cphi, nx, ny, nz);
         return true;
     }
@@ -1131,7 +1131,7 @@ __device__ __forceinline__ bool propose_mixture(const Prop& p, const float* __re
     const float uZ = u01f(B.y) * (a_lin * L + 0.5f * bD * L * L);
     const float cth = fminf(c_lo + 2.0f * uZ / (a_lin + sqrtf(a_lin * a_lin + 2.0f * bD * uZ)), 1.0f);
     float sphi, cphi;
-    sincospif(2.0f * u01f(B.z), &sphi, &cphi);
+    __sincosf(kTwoPiF * (u01f(B.z) - 0.5f), &sphi, &cphi);
     around(p.nx, p.ny, p.nz, cth, sphi, cphi, nx, ny, nz);
     return true;
 }
