@@ -185,7 +185,9 @@ iss_status iss_gpu_generate_into(iss_handle* h, iss_hadron_t* out, int64_t capac
  * iss_gpu_generate draws for the same seed, bit for bit.  Afterwards the
  * handle holds timings and counts but no hadrons (the accessors return
  * ISS_ERR_NO_SAMPLES).  perform_decays needs every event on the device and
- * returns ISS_ERR_UNSUPPORTED here. */
+ * returns ISS_ERR_UNSUPPORTED here.  fn must not call the library with the
+ * same handle (the generate is still running) and must not let a C++
+ * exception escape into this C call. */
 typedef void (*iss_stream_fn)(void* user, const iss_hadron_t* hadrons, int64_t n_hadrons,
                               int32_t first_event, int32_t n_events, const int64_t* event_offsets);
 iss_status iss_gpu_generate_stream(iss_handle* h, int32_t chunk_events, iss_stream_fn fn, void* user);
