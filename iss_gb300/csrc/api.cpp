@@ -85,14 +85,15 @@ struct iss_handle {
     DevBuf<int2> d_dhash;                 // pid -> particle index (kDecayHash slots)
     int n_decay_particles = 0;
     cudaEvent_t ev_decay[2] = {nullptr, nullptr};
-    // decay work buffers (grow-only): next-input ping-pong, the arena of
-    // stable products, per-input scratch, per-event bounds and the final list
-    DevBuf<HadronRec> dk_u[2], dk_arena, dk_final;
-    DevBuf<int32_t> dk_uev[2], dk_ev0, dk_chan, dk_etot;
-    DevBuf<int64_t> dk_cnt, dk_coff, dk_tiles, dk_first, dk_last, dk_gfirst, dk_glast, dk_meta,
-        dk_base, dk_off, dk_etiles, dk_evoff;
+    // decay work buffers (grow-only): one generation's records (ping-pong),
+    // the per-input arrays of all generations, per-(generation, event) tables
+    // and the final lists
+    DevBuf<HadronRec> dk_u[2], dk_final;
+    DevBuf<int32_t> dk_ev, dk_pid, dk_chan, dk_etot;
+    DevBuf<int64_t> dk_cnt, dk_coff, dk_tiles, dk_first, dk_last, dk_scnt, dk_shift, dk_meta,
+        dk_off, dk_etiles, dk_evoff;
     DevBuf<unsigned long long> dk_fail;
-    int64_t dk_scap_hint = 0, dk_ucap_hint = 0;   // sizes the last call needed
+    int64_t dk_scap_hint = 0, dk_ucap_hint = 0, dk_icap_hint = 0;   // sizes the last call needed
     int32_t dk_reruns = 0;                         // decay passes rerun in the last call
     int64_t cdf_len = 0, guide_len = 0, n_tiles = 0;
     int hydro_mode = 2;
@@ -216,10 +217,10 @@ struct iss_handle {
             d_dchannels.release();
             d_dsorted.release();
             d_dhash.release();
-            for (auto* b : {&dk_u[0], &dk_u[1], &dk_arena, &dk_final}) b->release();
-            for (auto* b : {&dk_uev[0], &dk_uev[1], &dk_ev0, &dk_chan, &dk_etot}) b->release();
-            for (auto* b : {&dk_cnt, &dk_coff, &dk_tiles, &dk_first, &dk_last, &dk_gfirst,
-                            &dk_glast, &dk_meta, &dk_base, &dk_off, &dk_etiles, &dk_evoff})
+            for (auto* b : {&dk_u[0], &dk_u[1], &dk_final}) b->release();
+            for (auto* b : {&dk_ev, &dk_pid, &dk_chan, &dk_etot}) b->release();
+            for (auto* b : {&dk_cnt, &dk_coff, &dk_tiles, &dk_first, &dk_last, &dk_scnt, &dk_shift,
+                            &dk_meta, &dk_off, &dk_etiles, &dk_evoff})
                 b->release();
             dk_fail.release();
             learned.release_all();
@@ -669,13 +670,13 @@ float elapsed(iss_handle* h, int a, int b) {
 
 // Resonance decays of the sampled records, generation by generation over
 // all events (kernels_decay.cu); replaces d_hadrons and the event offsets
-// with the final-state lists.  The sizes of the generations stay on the
-// device: generations are enqueued in batches of kDecayBatch and the host
-// waits once per batch (once in all for chains of up to kDecayBatch
-// generations) and once for the final lists.  A generation that does not fit
-// the arena or the next-input buffer writes nothing; the call then reruns
-// with buffers sized from what it needed (same results).  The work buffers
-// stay allocated in the handle for later calls.
+// with the final-state lists.  The count sweep runs on the device in batches
+// of kDecayBatch generations with one host wait per batch (the sizes stay on
+// the device); the layout and the write sweep follow, then one wait for the
+// event offsets.  A generation whose products do not fit a buffer ends the
+// count sweep with a flag; the call then reruns the sweep with buffers sized
+// from what it needed (same results).  The work buffers stay allocated in the
+// handle for later calls.
 constexpr int kDecayBatch = 8;
 
 iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
@@ -748,17 +749,19 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         *failures_out = 0;
         return ISS_OK;
     }
-    const int grid = h->num_sms * 4;
     const int G = kDecayMaxGenerations;
     // first sizes: what the last call needed, else gpu_decay_arena_factor
-    // (default 1.5) and gpu_decay_next_factor (0.5) times the sampled
-    // hadrons; too small only costs a rerun
+    // (default 1.5) times the sampled hadrons for the final lists,
+    // gpu_decay_next_factor (0.5) for one generation's records and the
+    // sampled hadrons plus twice that for the inputs of all generations; too
+    // small only costs a rerun of the count sweep
     const double fa = h->params.get_or("gpu_decay_arena_factor", 1.5);
     const double fu = h->params.get_or("gpu_decay_next_factor", 0.5);
     if (!(fa > 0.0) || !(fu > 0.0))
         return fail(h, ISS_ERR_INVALID_ARG, "gpu_decay_arena_factor / gpu_decay_next_factor must be > 0");
     int64_t s_cap = std::max<int64_t>(h->dk_scap_hint, static_cast<int64_t>(fa * static_cast<double>(n0)) + 64);
     int64_t u_cap = std::max<int64_t>(h->dk_ucap_hint, static_cast<int64_t>(fu * static_cast<double>(n0)) + 64);
+    int64_t i_cap = std::max<int64_t>(h->dk_icap_hint, n0 + 2 * u_cap);
     std::vector<int64_t> meta_h(kDecayMetaLen, 0);
     // the scans add (stable << 32 | unstable) counts of at most 3 each: the
     // unstable half stays below 2^32 while a generation has < 2^32 / 3 inputs
@@ -766,25 +769,23 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     if (n0 > kMaxDecayInputs)
         return fail(h, ISS_ERR_UNSUPPORTED, "resonance decays of more than %lld sampled hadrons",
                     static_cast<long long>(kMaxDecayInputs));
+    const size_t GE = static_cast<size_t>(G) * static_cast<size_t>(E);
     for (int attempt = 0;; attempt++) {
         u_cap = std::min(u_cap, kMaxDecayInputs);
-        const int64_t in_cap = std::max(n0, u_cap);
-        CUDA_TRY(h, h->dk_ev0.reserve(static_cast<size_t>(n0)));
-        for (int k = 0; k < 2; k++) {
-            CUDA_TRY(h, h->dk_u[k].reserve(static_cast<size_t>(u_cap)));
-            CUDA_TRY(h, h->dk_uev[k].reserve(static_cast<size_t>(u_cap)));
-        }
-        CUDA_TRY(h, h->dk_arena.reserve(static_cast<size_t>(s_cap)));
+        i_cap = std::max(i_cap, n0);
+        const int64_t gen_cap = std::max(n0, u_cap);
+        for (int k = 0; k < 2; k++) CUDA_TRY(h, h->dk_u[k].reserve(static_cast<size_t>(u_cap)));
         CUDA_TRY(h, h->dk_final.reserve(static_cast<size_t>(s_cap)));
-        CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(in_cap)));
-        CUDA_TRY(h, h->dk_cnt.reserve(static_cast<size_t>(in_cap)));
-        CUDA_TRY(h, h->dk_coff.reserve(static_cast<size_t>(in_cap) + 1));
-        CUDA_TRY(h, h->dk_tiles.reserve(static_cast<size_t>(in_cap / 4096 + 1)));
-        CUDA_TRY(h, h->dk_first.reserve(static_cast<size_t>(E)));
-        CUDA_TRY(h, h->dk_last.reserve(static_cast<size_t>(E)));
-        CUDA_TRY(h, h->dk_gfirst.reserve(static_cast<size_t>(G) * E));
-        CUDA_TRY(h, h->dk_glast.reserve(static_cast<size_t>(G) * E));
-        CUDA_TRY(h, h->dk_base.reserve(static_cast<size_t>(G) * E));
+        CUDA_TRY(h, h->dk_ev.reserve(static_cast<size_t>(i_cap)));
+        CUDA_TRY(h, h->dk_pid.reserve(static_cast<size_t>(i_cap)));
+        CUDA_TRY(h, h->dk_chan.reserve(static_cast<size_t>(i_cap)));
+        CUDA_TRY(h, h->dk_coff.reserve(static_cast<size_t>(i_cap) + G + 1));
+        CUDA_TRY(h, h->dk_cnt.reserve(static_cast<size_t>(gen_cap)));
+        CUDA_TRY(h, h->dk_tiles.reserve(static_cast<size_t>(gen_cap / 4096 + 1)));
+        CUDA_TRY(h, h->dk_first.reserve(GE));
+        CUDA_TRY(h, h->dk_last.reserve(GE));
+        CUDA_TRY(h, h->dk_scnt.reserve(GE));
+        CUDA_TRY(h, h->dk_shift.reserve(GE));
         CUDA_TRY(h, h->dk_meta.reserve(kDecayMetaLen));
         CUDA_TRY(h, h->dk_off.reserve(static_cast<size_t>(E) + 1));
         CUDA_TRY(h, h->dk_evoff.reserve(static_cast<size_t>(E) + 1));
@@ -796,61 +797,65 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         meta_h[kDecayMetaNIn] = n0;
         CUDA_TRY(h, cudaMemcpyAsync(h->dk_meta.ptr, meta_h.data(), 8 * meta_h.size(),
                                     cudaMemcpyHostToDevice, s));
-        CUDA_TRY(h, cudaMemsetAsync(h->dk_gfirst.ptr, 0xFF, 8 * static_cast<size_t>(G) * E, s));
-        CUDA_TRY(h, cudaMemsetAsync(h->dk_glast.ptr, 0xFF, 8 * static_cast<size_t>(G) * E, s));
+        CUDA_TRY(h, cudaMemsetAsync(h->dk_first.ptr, 0xFF, 8 * GE, s));
+        CUDA_TRY(h, cudaMemsetAsync(h->dk_last.ptr, 0xFF, 8 * GE, s));
         CUDA_TRY(h, cudaMemsetAsync(h->dk_fail.ptr, 0, sizeof(unsigned long long), s));
         CUDA_TRY(h, cudaMemcpyAsync(h->dk_evoff.ptr, h->event_offsets.data(), 8 * (static_cast<size_t>(E) + 1),
                                     cudaMemcpyHostToDevice, s));
-        CUDA_TRY(h, launch_event_ids(h->dk_evoff.ptr, E, h->dk_ev0.ptr, s));
 
         DecayBuffers b{};
-        b.arena = h->dk_arena.ptr;
+        b.rec0 = h->d_hadrons.ptr;
+        b.ev = h->dk_ev.ptr;
+        b.pid = h->dk_pid.ptr;
         b.chan = h->dk_chan.ptr;
         b.cnt = h->dk_cnt.ptr;
         b.off = h->dk_coff.ptr;
         b.tiles = h->dk_tiles.ptr;
         b.first = h->dk_first.ptr;
         b.last = h->dk_last.ptr;
-        b.gfirst = h->dk_gfirst.ptr;
-        b.glast = h->dk_glast.ptr;
+        b.scnt = h->dk_scnt.ptr;
+        b.shift = h->dk_shift.ptr;
         b.meta = h->dk_meta.ptr;
         b.failures = h->dk_fail.ptr;
         b.s_cap = s_cap;
         b.u_cap = u_cap;
+        b.i_cap = i_cap;
         b.g_max = static_cast<uint32_t>(G);
+        CUDA_TRY(h, launch_decay_first_generation(h->dk_evoff.ptr, E, b, s));
+        // count sweep: batches of generations, one wait (and a copy of the
+        // sizes) per batch
         int g = 0;
-        int64_t head[2] = {0, 0};   // next input size, flags
         for (;;) {
-            for (int k = 0; k < kDecayBatch && g < G; k++, g++) {
-                b.in = g == 0 ? h->d_hadrons.ptr : h->dk_u[(g - 1) & 1].ptr;
-                b.in_ev = g == 0 ? h->dk_ev0.ptr : h->dk_uev[(g - 1) & 1].ptr;
-                b.out_u = h->dk_u[g & 1].ptr;
-                b.out_u_ev = h->dk_uev[g & 1].ptr;
-                CUDA_TRY(h, launch_decay_generation(c, t, static_cast<uint32_t>(g), b, E, h->num_sms, s));
-            }
-            CUDA_TRY(h, cudaMemcpyAsync(&head[0], h->dk_meta.ptr + kDecayMetaNIn + g, 8,
-                                        cudaMemcpyDeviceToHost, s));
-            CUDA_TRY(h, cudaMemcpyAsync(&head[1], h->dk_meta.ptr + kDecayMetaFlags, 8,
+            for (int k = 0; k < kDecayBatch && g < G; k++, g++)
+                CUDA_TRY(h, launch_decay_count_generation(c, t, static_cast<uint32_t>(g), b, E, h->num_sms, s));
+            CUDA_TRY(h, cudaMemcpyAsync(meta_h.data(), h->dk_meta.ptr, 8 * meta_h.size(),
                                         cudaMemcpyDeviceToHost, s));
             CUDA_TRY(h, cudaStreamSynchronize(s));
-            if (head[1] != 0 || head[0] == 0 || g >= G) break;
+            if (meta_h[kDecayMetaFlags] != 0 || meta_h[kDecayMetaNIn + g] == 0 || g >= G) break;
         }
-        CUDA_TRY(h, cudaMemcpyAsync(meta_h.data(), h->dk_meta.ptr, 8 * meta_h.size(),
-                                    cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(h, cudaStreamSynchronize(s));
         const int64_t flags = meta_h[kDecayMetaFlags];
         if (flags & 4)
             return fail(h, ISS_ERR_SAMPLING, "decay chains longer than %d generations", G);
-        if (flags & 3) {
+        if (flags & 11) {
             if (attempt >= 8) return fail(h, ISS_ERR_CUDA, "decay buffers did not settle");
             h->dk_reruns++;
             if (flags & 1) s_cap = std::max(s_cap * 2, meta_h[kDecayMetaNeedS] + meta_h[kDecayMetaNeedS] / 4);
             if (flags & 2) u_cap = std::max(u_cap * 2, meta_h[kDecayMetaNeedU] + meta_h[kDecayMetaNeedU] / 4);
+            if (flags & 8) i_cap = std::max(i_cap * 2, meta_h[kDecayMetaNeedI] + meta_h[kDecayMetaNeedI] / 4);
             continue;
         }
-        const int64_t total = meta_h[kDecayMetaSBase + g];
-        CUDA_TRY(h, launch_decay_assemble(b, g, E, h->dk_etot.ptr, h->dk_etiles.ptr, h->dk_off.ptr,
-                                          h->dk_base.ptr, h->dk_final.ptr, grid, s));
+        // generations with inputs: 0 .. n_gen - 1
+        int n_gen = 0;
+        while (n_gen < g && meta_h[kDecayMetaNIn + n_gen] > 0) n_gen++;
+        const int64_t total = meta_h[kDecayMetaSBase + n_gen];
+        CUDA_TRY(h, launch_decay_layout(b, n_gen, E, h->dk_etot.ptr, h->dk_etiles.ptr, h->dk_off.ptr, s));
+        // write sweep
+        for (int k = 0; k < n_gen; k++) {
+            const HadronRec* in = k == 0 ? h->d_hadrons.ptr : h->dk_u[(k - 1) & 1].ptr;
+            CUDA_TRY(h, launch_decay_write_generation(c, t, static_cast<uint32_t>(k), meta_h[kDecayMetaNIn + k],
+                                                      meta_h[kDecayMetaIBase + k], in, h->dk_u[k & 1].ptr, b, E,
+                                                      h->num_sms, h->dk_final.ptr, s));
+        }
         h->event_offsets.assign(static_cast<size_t>(E) + 1, 0);
         unsigned long long nf = 0;
         CUDA_TRY(h, cudaMemcpyAsync(h->event_offsets.data(), h->dk_off.ptr, 8 * (static_cast<size_t>(E) + 1),
@@ -862,8 +867,10 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
                         static_cast<long long>(h->event_offsets[E]), static_cast<long long>(total));
         *failures_out = nf;
         // sizes for the next call: what this one needed, with headroom
+        const int64_t inputs = meta_h[kDecayMetaIBase + n_gen];
         h->dk_scap_hint = std::max(h->dk_scap_hint, total + total / 8 + 4096);
         h->dk_ucap_hint = std::max(h->dk_ucap_hint, meta_h[kDecayMetaMaxU] + meta_h[kDecayMetaMaxU] / 8 + 4096);
+        h->dk_icap_hint = std::max(h->dk_icap_hint, inputs + inputs / 8 + 4096);
         std::swap(h->dk_final.ptr, h->d_hadrons.ptr);
         std::swap(h->dk_final.cap, h->d_hadrons.cap);
         h->n_hadrons = total;

@@ -77,51 +77,64 @@ cudaError_t launch_learned_train_rows(const DevConfig& cfg, const CellArrays& ce
                                       double* nll_plain, cudaStream_t stream);
 
 // kernels_decay.cu: resonance decays, one generation over all events at a
-// time, sizes kept on the device.  DecayMeta (int64 slots of `meta`):
-// kDecayMetaNIn + g the input size of generation g (g <= g_max),
-// kDecayMetaSBase + g the start of generation g's stable products in the
-// arena, kDecayMetaFlags (1: arena too small, 2: next input buffer too small,
-// 4: chains longer than g_max), kDecayMetaNeedS / NeedU what the failing
-// generation needed, kDecayMetaMaxU the largest next input seen.
+// time: a count sweep on particle ids (sizes and final places, kept on the
+// device), then a write sweep with the kinematics.  DecayMeta (int64 slots of
+// `meta`): kDecayMetaNIn + g the input size of generation g (g <= g_max),
+// kDecayMetaSBase + g the stable products of generations < g,
+// kDecayMetaIBase + g where generation g's inputs start in the per-input
+// arrays, kDecayMetaFlags (1: final lists too small, 2: one generation's
+// records too small, 4: chains longer than g_max, 8: per-input arrays too
+// small), kDecayMetaNeedS / NeedU / NeedI what the failing generation
+// needed, kDecayMetaMaxU the largest next input seen.
 constexpr int kDecayMetaFlags = 0;
 constexpr int kDecayMetaNeedS = 1;
 constexpr int kDecayMetaNeedU = 2;
 constexpr int kDecayMetaMaxU = 3;
+constexpr int kDecayMetaNeedI = 4;
 constexpr int kDecayMetaNIn = 8;
 constexpr int kDecayMaxGenerations = 64;
 constexpr int kDecayMetaSBase = kDecayMetaNIn + kDecayMaxGenerations + 1;
-constexpr int kDecayMetaLen = kDecayMetaSBase + kDecayMaxGenerations + 1;
+constexpr int kDecayMetaIBase = kDecayMetaSBase + kDecayMaxGenerations + 1;
+constexpr int kDecayMetaLen = kDecayMetaIBase + kDecayMaxGenerations + 1;
 
 struct DecayBuffers {
-    const HadronRec* in;        // this generation's input (event-sorted)
-    const int32_t* in_ev;       // its event ids
-    HadronRec* out_u;           // next generation's input (unstable products)
-    int32_t* out_u_ev;
-    HadronRec* arena;           // stable products of all generations
-    int32_t* chan;              // per input hadron: (type << 16) | channel, or < 0
-    int64_t* cnt;               // per input hadron: (stable products << 32) | unstable ones
-    int64_t* off;               // exclusive scan of cnt (input size + 1): both offsets at once
+    const HadronRec* rec0;      // the sampled records (generation 0's input), event-sorted
+    int32_t* ev;                // [i_cap] event of every input, generations back to back
+    int32_t* pid;               // [i_cap] particle id of every input of generations >= 1
+    int32_t* chan;              // [i_cap] per input: (type << 16) | channel, or < 0
+    int64_t* cnt;               // [largest generation] (stable products << 32) | unstable ones
+    int64_t* off;               // [i_cap + g_max + 1] generation g's exclusive scan of cnt
+                                // (inputs + 1 entries) from IBase + g: both offsets at once
     int64_t* tiles;             // one per scan tile of 4096 inputs
-    int64_t* first;             // [n_events] first input of each event (-1: none)
-    int64_t* last;
-    int64_t* gfirst;            // [g_max][n_events] per generation, its arena range per event
-    int64_t* glast;
+    int64_t* first;             // [g_max][n_events] input range of each event per generation
+    int64_t* last;              //   (-1: none)
+    int64_t* scnt;              // [g_max][n_events] stable products of each event per generation
+    int64_t* shift;             // [g_max][n_events] final place of the event's first stable
+                                //   product of the generation, less its stable scan offset
     int64_t* meta;              // DecayMeta
     unsigned long long* failures;
-    int64_t s_cap, u_cap;       // arena and next-input capacities
+    int64_t s_cap, u_cap, i_cap;   // final lists, one generation's records, per-input arrays
     uint32_t g_max;
 };
 
-cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cudaStream_t s);
-// one generation: input bounds, count (channel cache), two scans, sizes of
-// the next generation, write, and this generation's arena bounds per event
-cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                                    const DecayBuffers& b, int n_events, int num_sms, cudaStream_t s);
-// final lists: per-event totals of generations < n_gen, event offsets (off,
-// n_events + 1), per (generation, event) bases, and the gather into out
-cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
-                                  int64_t* tiles, int64_t* off, int64_t* base, HadronRec* out, int grid,
-                                  cudaStream_t s);
+// event ids and input ranges of generation 0 from the sampled event offsets
+cudaError_t launch_decay_first_generation(const int64_t* evoff, int n_events, const DecayBuffers& b,
+                                          cudaStream_t s);
+// count sweep of one generation: channel cache, packed scan, sizes of the
+// next generation, its inputs' ids and events, per-event ranges
+cudaError_t launch_decay_count_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                          const DecayBuffers& b, int n_events, int num_sms,
+                                          cudaStream_t s);
+// final lists of generations < n_gen: per-event totals, event offsets
+// (evoff, n_events + 1) and the per (generation, event) shifts
+cudaError_t launch_decay_layout(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
+                                int64_t* tiles, int64_t* evoff, cudaStream_t s);
+// write sweep of generation gen (n inputs from ib): stable products to out,
+// unstable ones to out_u (the next generation's records)
+cudaError_t launch_decay_write_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                          int64_t n, int64_t ib, const HadronRec* in, HadronRec* out_u,
+                                          const DecayBuffers& b, int n_events, int num_sms,
+                                          HadronRec* out, cudaStream_t s);
 
 // kernels_output.cu: OSCAR text (FSSW::combine_samples_to_OSCAR) of hadrons
 // [h0, h1), which are the whole events [e_lo, e_hi).  ev_off: the events'

@@ -7,24 +7,33 @@
 // the end of the list (unstable).  The output of an event is therefore, in
 // order, the stable products of the sampled hadrons, then those of their
 // unstable daughters, then of the granddaughters, and so on.  Here each such
-// generation is one pass over all events at once: a count kernel (channel
-// choice, stable and unstable products per hadron), two exclusive scans, and
-// a write kernel that puts stable products into this generation's range of
-// one output arena and unstable ones into the next generation's input, both
-// in order.  The final list of each event is the concatenation of its
-// generations' outputs (dk_event_totals / dk_event_bases / dk_gather).
+// generation is one pass over all events at once, in two sweeps.
 //
-// The sizes of a generation live on the device (DecayMeta): every kernel
-// reads its input size there and loops over it with a fixed grid, so the
-// host enqueues whole batches of generations without waiting; a generation
-// whose products would not fit the arena or the next input buffer writes
-// nothing and raises a flag, and the host reruns the call with larger
-// buffers (the results do not depend on the buffer sizes).
+// The count sweep runs the generations on particle ids alone: a hadron's
+// channel and the kinds of its products do not depend on momenta.  Per
+// generation a count kernel (channel choice; stable and unstable products per
+// hadron), one packed exclusive scan and a daughters kernel (ids and events
+// of the unstable products: the next generation's input) give the sizes of
+// every generation and, per event, its range of inputs and its number of
+// stable products.  That fixes each event's final list, and the place of
+// every generation's stable products in it, before any kinematics run.
+//
+// The write sweep runs the generations again with momenta: stable inputs are
+// copied and decaying ones decay, their stable products going straight to
+// their final places and the unstable ones to the next generation's records.
+//
+// The sizes live on the device (DecayMeta): each count-sweep kernel reads its
+// input size there, so the host enqueues batches of generations without
+// waiting.  A generation whose products would not fit a buffer raises a flag
+// and ends the chain before the write sweep; the host then reruns the count
+// sweep with larger buffers (the results do not depend on the buffer sizes).
 //
 // Every random number comes from Philox4x32-10 with counter
 // (draw, index of the hadron in its event's generation list, event,
 // generation | kTagDecay << 16): results do not depend on thread mapping.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -127,20 +136,31 @@ constexpr int32_t kChanNone = -2;
 __device__ __forceinline__ int64_t meta_n(const int64_t* __restrict__ meta, uint32_t gen) {
     return meta[kDecayMetaNIn + gen];
 }
+// where generation gen's inputs start in the per-input arrays (its scan
+// starts at meta_ib + gen: each scan has one entry more than its inputs)
+__device__ __forceinline__ int64_t meta_ib(const int64_t* __restrict__ meta, uint32_t gen) {
+    return meta[kDecayMetaIBase + gen];
+}
 
+// Count kernel of generation gen: the channel cache and the packed counts of
+// every input.  The particle id comes from the sampled records (generation 0)
+// or from the ids the daughters kernel wrote (later generations).
 __global__ void __launch_bounds__(kDecayThreads)
-decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
-                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
-                   const int64_t* __restrict__ meta, int32_t* __restrict__ chan,
-                   int64_t* __restrict__ cnt) {
+decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ rec0,
+                   const int32_t* __restrict__ pid_all, const int32_t* __restrict__ ev_all,
+                   const int64_t* __restrict__ first, const int64_t* __restrict__ meta,
+                   int32_t* __restrict__ chan_all, int64_t* __restrict__ cnt) {
     __shared__ int2 s_hash[kDecayHash];
     for (int j = threadIdx.x; j < kDecayHash; j += blockDim.x) s_hash[j] = t.hash[j];
     __syncthreads();
-    const int64_t n = meta_n(meta, gen);
+    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen);
+    const int32_t* ev = ev_all + ib;
+    int32_t* chan = chan_all + ib;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int e = ev[i];
-        const DecayPlan d = plan(t, s_hash, cfg, in[i].pid, static_cast<uint32_t>(i - first[e]),
+        const int pid = gen == 0 ? rec0[i].pid : pid_all[ib + i];
+        const DecayPlan d = plan(t, s_hash, cfg, pid, static_cast<uint32_t>(i - first[e]),
                                  cfg.event_offset + static_cast<uint32_t>(e), gen);
         int s = 0, u = 0;
         int32_t c;
@@ -191,12 +211,12 @@ __device__ __forceinline__ void boost(const Lorentz& L, float E, float px, float
 }
 
 // the products of hadron m of event e (index ie in its event's generation
-// list) through channel `channel` of particle `type`
+// list) through channel `channel` of particle `type`: stable ones from
+// out_s[ps], unstable ones from out_u[pu]
 __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
                                        const HadronRec& m, int e, uint32_t ie, int type, int channel,
                                        int64_t ps, int64_t pu, HadronRec* __restrict__ out_s,
                                        HadronRec* __restrict__ out_u,
-                                       int32_t* __restrict__ ev_u,
                                        unsigned long long* __restrict__ failures) {
     const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
     const DecayChannel& ch = t.channels[channel];
@@ -299,31 +319,28 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
             ps++;
         } else {
             store_rec(out_u + pu, r);
-            ev_u[pu] = e;
             pu++;
         }
     }
 }
 
 // The write pass of a generation.  Each warp walks its chunks of 32 inputs:
-// stable inputs are copied into the arena at once, decaying ones are queued
-// in shared memory, and whenever 32 are queued the whole warp decays them
-// together, so lanes that copy do not wait on lanes that decay.  Every
-// product goes to the slot its scan offsets give, whatever the order.
+// stable inputs are copied to their final places at once, decaying ones are
+// queued in shared memory, and whenever 32 are queued the whole warp decays
+// them together, so lanes that copy do not wait on lanes that decay.  Stable
+// product k of input i (event e) goes to shift[e] + stable(off[i]) + k, where
+// shift[e] is the final place of the event's first stable product of this
+// generation less its scan offset; unstable ones to out_u[unstable(off[i])].
 constexpr int kDecayQueue = 64;
 
 __global__ void __launch_bounds__(kDecayThreads, 3)
-decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ in,
-                   const int32_t* __restrict__ ev, const int64_t* __restrict__ first,
-                   const int32_t* __restrict__ chan, const int64_t* __restrict__ meta,
-                   const int64_t* __restrict__ off, HadronRec* __restrict__ out_s,
-                   HadronRec* __restrict__ out_u, int32_t* __restrict__ ev_u,
+decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, int64_t n,
+                   const HadronRec* __restrict__ in, const int32_t* __restrict__ ev,
+                   const int64_t* __restrict__ first, const int32_t* __restrict__ chan,
+                   const int64_t* __restrict__ off, const int64_t* __restrict__ shift,
+                   HadronRec* __restrict__ out, HadronRec* __restrict__ out_u,
                    unsigned long long* __restrict__ failures) {
     __shared__ int64_t s_q[kDecayThreads / 32][kDecayQueue];
-    // a generation that did not fit writes nothing (the host reruns the call)
-    if (meta[kDecayMetaFlags] != 0) return;
-    const int64_t n = meta_n(meta, gen);
-    const int64_t sbase = meta[kDecayMetaSBase + gen];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int64_t* q = s_q[wid];
@@ -333,14 +350,14 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
         const int e = ev[i];
         const int64_t o = off[i];
         decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF,
-                  sbase + (o >> 32), o & 0xFFFFFFFFll, out_s, out_u, ev_u, failures);
+                  shift[e] + (o >> 32), o & 0xFFFFFFFFll, out, out_u, failures);
     };
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
     for (int64_t b0 = (static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + wid) * 32; b0 < n;
          b0 += warps * 32) {
         const int64_t i = b0 + lane;
         const int32_t c = i < n ? chan[i] : kChanNone;
-        if (c == kChanStable) copy_rec(out_s + sbase + (off[i] >> 32), in + i);
+        if (c == kChanStable) copy_rec(out + shift[ev[i]] + (off[i] >> 32), in + i);
         const unsigned want = __ballot_sync(FULL, c >= 0);
         if (c >= 0) q[qn + __popc(want & ((1u << lane) - 1u))] = i;
         qn += __popc(want);
@@ -356,40 +373,6 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRe
     if (lane < qn) decay(q[lane]);
 }
 
-// first[e] = index of event e's first element in the event-sorted range
-// [*lo, *hi) of ev (lo null: 0), and last[e] = one past its last (both stay
-// -1 for absent events)
-__global__ void dk_bounds_kernel(const int32_t* __restrict__ ev, const int64_t* __restrict__ lo_p,
-                                 const int64_t* __restrict__ hi_p, int64_t* __restrict__ first,
-                                 int64_t* __restrict__ last) {
-    const int64_t lo = lo_p ? *lo_p : 0, hi = *hi_p;
-    for (int64_t i = lo + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < hi;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int e = ev[i];
-        if (i == lo || ev[i - 1] != e) first[e] = i;
-        if (i == hi - 1 || ev[i + 1] != e) last[e] = i + 1;
-    }
-}
-
-// this generation's arena range per event, from its input range
-// [first[e], last[e]) and the stable half of the packed scan: [sbase +
-// stable(off[first]), sbase + stable(off[last])); -1 where the event has none
-__global__ void dk_gen_bounds_kernel(const int64_t* __restrict__ first, const int64_t* __restrict__ last,
-                                     const int64_t* __restrict__ off, const int64_t* __restrict__ meta,
-                                     uint32_t gen, int n_events, int64_t* __restrict__ gfirst,
-                                     int64_t* __restrict__ glast) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_events || meta[kDecayMetaFlags] != 0) return;
-    const int64_t f = first[e];
-    if (f < 0) return;
-    const int64_t sb = meta[kDecayMetaSBase + gen];
-    const int64_t a = off[f] >> 32, b = off[last[e]] >> 32;
-    if (b > a) {
-        gfirst[e] = sb + a;
-        glast[e] = sb + b;
-    }
-}
-
 // event ids of the sampled records from the event offsets
 __global__ void event_ids_kernel(const int64_t* __restrict__ off, int n_events,
                                  int32_t* __restrict__ ev) {
@@ -398,7 +381,17 @@ __global__ void event_ids_kernel(const int64_t* __restrict__ off, int n_events,
     for (int64_t i = off[e] + threadIdx.x; i < off[e + 1]; i += blockDim.x) ev[i] = e;
 }
 
-// ---- exclusive scans of the two count arrays, input size on the device ----
+// generation 0's input range per event: the sampled records of the event
+__global__ void dk_first_gen_kernel(const int64_t* __restrict__ evoff, int n_events,
+                                    int64_t* __restrict__ first, int64_t* __restrict__ last) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_events) return;
+    const bool any = evoff[e + 1] > evoff[e];
+    first[e] = any ? evoff[e] : -1;
+    last[e] = any ? evoff[e + 1] : -1;
+}
+
+// ---- exclusive scans of the packed counts, input size on the device ----
 
 constexpr int kDkScanThreads = 256;
 constexpr int kDkScanPer = 16;
@@ -436,7 +429,8 @@ __device__ long long dk_block_excl(long long v, long long* s_warp, long long* to
 
 // Exclusive scan of the packed counts (stable << 32 | unstable): one int64
 // scan gives both offsets, since no partial sum of the unstable half reaches
-// 2^32 (it is bounded by the next-input capacity).
+// 2^32 (it is bounded by the next-input capacity).  Generation gen's scan
+// lands at off_all + meta_ib + gen (n + 1 entries, the last the total).
 // tile sums: tiles[t] for the tiles of 4096 inputs
 __global__ void __launch_bounds__(kDkScanThreads)
 dk_tile_sum_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ meta, uint32_t gen,
@@ -459,7 +453,7 @@ dk_tile_sum_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ me
 // one block: tile sums -> tile offsets (in place), the total to off[n]
 __global__ void __launch_bounds__(kDkScanThreads)
 dk_tile_offset_kernel(int64_t* __restrict__ tiles, const int64_t* __restrict__ meta, uint32_t gen,
-                      int64_t* __restrict__ off) {
+                      int64_t* __restrict__ off_all) {
     __shared__ long long s_warp[33];
     const int64_t n = meta_n(meta, gen);
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
@@ -472,16 +466,17 @@ dk_tile_offset_kernel(int64_t* __restrict__ tiles, const int64_t* __restrict__ m
         if (i < nt) tiles[i] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) off[n] = carry;
+    if (threadIdx.x == 0) off_all[meta_ib(meta, gen) + gen + n] = carry;
 }
 
 __global__ void __launch_bounds__(kDkScanThreads)
 dk_tile_scan_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ meta, uint32_t gen,
-                    const int64_t* __restrict__ tiles, int64_t* __restrict__ off) {
+                    const int64_t* __restrict__ tiles, int64_t* __restrict__ off_all) {
     __shared__ long long s_in[kDkScanThreads * (kDkScanPer + 1)];
     __shared__ long long s_warp[33];
     const int64_t n = meta_n(meta, gen);
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
+    int64_t* off = off_all + meta_ib(meta, gen) + gen;
     for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
         const int64_t t0 = tl * kDkTile;
         for (int k = 0; k < kDkScanPer; k++) {
@@ -506,17 +501,21 @@ dk_tile_scan_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ m
     }
 }
 
-// sizes of the next generation: the stable products go to the arena after
-// this generation's, the unstable ones are the next input; a generation
-// that does not fit (arena or next input) sets a flag, records what it
-// needed and stops the chain
-__global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ off,
-                                  int64_t s_cap, int64_t u_cap, uint32_t g_max) {
+// Sizes of the next generation: its inputs (this generation's unstable
+// products) follow this generation's in the per-input arrays, and the stable
+// products so far give the final lists' length.  A generation that does not
+// fit (final lists, one generation's records, all inputs) or would exceed
+// g_max sets a flag, records what it needed and ends the chain.
+__global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, const int64_t* __restrict__ off_all,
+                                  int64_t s_cap, int64_t u_cap, int64_t i_cap, uint32_t g_max) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int64_t n = meta[kDecayMetaNIn + gen];
+    const int64_t ib = meta[kDecayMetaIBase + gen];
     const int64_t sb = meta[kDecayMetaSBase + gen];
-    const int64_t st = off[n] >> 32, ut = off[n] & 0xFFFFFFFFll;
-    int64_t next_n = ut, next_sb = sb + st;
+    const int64_t tot = off_all[ib + gen + n];
+    const int64_t st = tot >> 32, ut = tot & 0xFFFFFFFFll;
+    int64_t next_n = ut;
+    const int64_t next_sb = sb + st, next_ib = ib + n;
     if (meta[kDecayMetaFlags] == 0 && next_sb > s_cap) {
         meta[kDecayMetaFlags] |= 1;
         meta[kDecayMetaNeedS] = next_sb;
@@ -525,107 +524,156 @@ __global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, cons
         meta[kDecayMetaFlags] |= 2;
         meta[kDecayMetaNeedU] = ut;
     }
-    if (meta[kDecayMetaFlags] == 0 && gen + 1 >= g_max && ut > 0) meta[kDecayMetaFlags] |= 4;
-    if (meta[kDecayMetaFlags] != 0) {
-        next_n = 0;
-        next_sb = sb;
+    if (meta[kDecayMetaFlags] == 0 && next_ib + ut > i_cap) {
+        meta[kDecayMetaFlags] |= 8;
+        meta[kDecayMetaNeedI] = next_ib + ut;
     }
+    if (meta[kDecayMetaFlags] == 0 && gen + 1 >= g_max && ut > 0) meta[kDecayMetaFlags] |= 4;
+    if (meta[kDecayMetaFlags] != 0) next_n = 0;
     meta[kDecayMetaNIn + gen + 1] = next_n;
     meta[kDecayMetaSBase + gen + 1] = next_sb;
+    meta[kDecayMetaIBase + gen + 1] = next_ib;
     if (ut > meta[kDecayMetaMaxU]) meta[kDecayMetaMaxU] = ut;
+}
+
+// The next generation's inputs: the particle id and event of every unstable
+// product, in the order of the unstable scan.
+__global__ void __launch_bounds__(kDecayThreads)
+dk_daughters_kernel(DecayTablesDev t, uint32_t gen, const int64_t* __restrict__ meta,
+                    const int32_t* __restrict__ chan_all, const int64_t* __restrict__ off_all,
+                    int32_t* __restrict__ ev_all, int32_t* __restrict__ pid_all) {
+    if (meta[kDecayMetaFlags] != 0) return;
+    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen), nb = meta_ib(meta, gen + 1);
+    const int32_t* chan = chan_all + ib;
+    const int64_t* off = off_all + ib + gen;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t c = chan[i];
+        if (c < 0) continue;
+        const DecayChannel& ch = t.channels[c & 0xFFFF];
+        int64_t pu = -1;
+        int e = 0;
+        for (int k = 0; k < ch.n_daughters; k++) {
+            const int di = ch.daughter[k];
+            if (daughter_stable(t, di)) continue;
+            if (pu < 0) {
+                pu = nb + (off[i] & 0xFFFFFFFFll);
+                e = ev_all[ib + i];
+            }
+            pid_all[pu] = t.particles[di].pid;
+            ev_all[pu] = e;
+            pu++;
+        }
+    }
+}
+
+// Per event: its stable products in this generation (scnt) and its input
+// range in the next one (the unstable products of its inputs, contiguous
+// because the inputs are grouped by event).
+__global__ void dk_next_bounds_kernel(const int64_t* __restrict__ meta, uint32_t gen,
+                                      const int64_t* __restrict__ off_all, int n_events, uint32_t g_max,
+                                      int64_t* __restrict__ first, int64_t* __restrict__ last,
+                                      int64_t* __restrict__ scnt) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_events || meta[kDecayMetaFlags] != 0) return;
+    const int64_t r = static_cast<int64_t>(gen) * n_events + e;
+    const int64_t f = first[r];
+    int64_t sc = 0;
+    if (f >= 0) {
+        const int64_t* off = off_all + meta_ib(meta, gen) + gen;
+        const int64_t a = off[f], b = off[last[r]];
+        sc = (b >> 32) - (a >> 32);
+        const int64_t ua = a & 0xFFFFFFFFll, ub = b & 0xFFFFFFFFll;
+        if (ub > ua && gen + 1 < g_max) {
+            first[r + n_events] = ua;
+            last[r + n_events] = ub;
+        }
+    }
+    scnt[r] = sc;
 }
 
 // ---- the final lists ----------------------------------------------------
 
-// per event: the hadrons of its generations' outputs (rows g < n_gen of the
-// per-generation bounds, -1 where the event has none)
-__global__ void dk_event_totals_kernel(const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
-                                       int n_gen, int n_events, int32_t* __restrict__ tot) {
+// per event: its stable products over generations g < n_gen
+__global__ void dk_event_totals_kernel(const int64_t* __restrict__ scnt, int n_gen, int n_events,
+                                       int32_t* __restrict__ tot) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_events) return;
     int64_t k = 0;
-    for (int g = 0; g < n_gen; g++) {
-        const int64_t f = gfirst[static_cast<int64_t>(g) * n_events + e];
-        if (f >= 0) k += glast[static_cast<int64_t>(g) * n_events + e] - f;
-    }
+    for (int g = 0; g < n_gen; g++) k += scnt[static_cast<int64_t>(g) * n_events + e];
     tot[e] = static_cast<int32_t>(k);
 }
 
-// base[g][e]: where event e's products of generation g start in the final list
-__global__ void dk_event_bases_kernel(const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
-                                      const int64_t* __restrict__ off, int n_gen, int n_events,
-                                      int64_t* __restrict__ base) {
+// shift[g][e] = final place of event e's first stable product of generation
+// g, less the stable scan offset of the event's first input in g
+__global__ void dk_shift_kernel(const int64_t* __restrict__ scnt, const int64_t* __restrict__ first,
+                                const int64_t* __restrict__ off_all, const int64_t* __restrict__ meta,
+                                const int64_t* __restrict__ evoff, int n_gen, int n_events,
+                                int64_t* __restrict__ shift) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_events) return;
-    int64_t b = off[e];
+    int64_t b = evoff[e];
     for (int g = 0; g < n_gen; g++) {
         const int64_t r = static_cast<int64_t>(g) * n_events + e;
-        base[r] = b;
-        if (gfirst[r] >= 0) b += glast[r] - gfirst[r];
+        const int64_t f = first[r];
+        if (f >= 0) shift[r] = b - (off_all[meta_ib(meta, static_cast<uint32_t>(g)) + g + f] >> 32);
+        b += scnt[r];
     }
-}
-
-// the final list: block (e, g) copies event e's products of generation g,
-// arena[gfirst[g][e] ..) to final[base[g][e] ..), as 8-byte words
-__global__ void dk_gather_kernel(const HadronRec* __restrict__ arena, int n_events,
-                                 const int64_t* __restrict__ gfirst, const int64_t* __restrict__ glast,
-                                 const int64_t* __restrict__ base, HadronRec* __restrict__ out) {
-    const int64_t r = static_cast<int64_t>(blockIdx.y) * n_events + blockIdx.x;
-    const int64_t f = gfirst[r];
-    if (f < 0) return;
-    const int64_t words = 5 * (glast[r] - f);
-    const uint2* src = reinterpret_cast<const uint2*>(arena + f);
-    uint2* dst = reinterpret_cast<uint2*>(out + base[r]);
-    for (int64_t k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
 }
 
 }  // namespace
 
-cudaError_t launch_event_ids(const int64_t* off, int n_events, int32_t* ev, cudaStream_t s) {
+cudaError_t launch_decay_first_generation(const int64_t* evoff, int n_events, const DecayBuffers& b,
+                                          cudaStream_t s) {
     if (n_events <= 0) return cudaSuccess;
-    event_ids_kernel<<<n_events, 128, 0, s>>>(off, n_events, ev);
+    event_ids_kernel<<<n_events, 128, 0, s>>>(evoff, n_events, b.ev);
+    dk_first_gen_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(evoff, n_events, b.first, b.last);
     return cudaGetLastError();
 }
 
-cudaError_t launch_decay_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                                    const DecayBuffers& b, int n_events, int num_sms, cudaStream_t s) {
-    // grid-stride kernels launched with what fits on the SMs at once: eight
-    // blocks of 256 for the light ones, three for the write pass (80 registers)
-    const int grid = num_sms * 8, grid_write = num_sms * 3;
-    const size_t ev_bytes = sizeof(int64_t) * static_cast<size_t>(n_events);
-    const int64_t* nin = b.meta + kDecayMetaNIn + gen;
-    cudaError_t e = cudaMemsetAsync(b.first, 0xFF, ev_bytes, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b.last, 0xFF, ev_bytes, s);
-    if (e != cudaSuccess) return e;
-    dk_bounds_kernel<<<grid, kDecayThreads, 0, s>>>(b.in_ev, nullptr, nin, b.first, b.last);
-    decay_count_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.meta,
+cudaError_t launch_decay_count_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                          const DecayBuffers& b, int n_events, int num_sms,
+                                          cudaStream_t s) {
+    // grid-stride kernels launched with what fits on the SMs at once (eight
+    // blocks of 256)
+    const int grid = num_sms * 8;
+    const int64_t* first = b.first + static_cast<int64_t>(gen) * n_events;
+    decay_count_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, b.rec0, b.pid, b.ev, first, b.meta,
                                                       b.chan, b.cnt);
     dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles);
     dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.off);
     dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles, b.off);
-    dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.g_max);
-    decay_write_kernel<<<grid_write, kDecayThreads, 0, s>>>(cfg, t, gen, b.in, b.in_ev, b.first, b.chan,
-                                                      b.meta, b.off, b.arena, b.out_u, b.out_u_ev,
-                                                      b.failures);
-    // this generation's range of the arena, per event
-    int64_t* gf = b.gfirst + static_cast<int64_t>(gen) * n_events;
-    int64_t* gl = b.glast + static_cast<int64_t>(gen) * n_events;
-    dk_gen_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.first, b.last, b.off, b.meta, gen,
-                                                                n_events, gf, gl);
+    dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.i_cap, b.g_max);
+    dk_daughters_kernel<<<grid, kDecayThreads, 0, s>>>(t, gen, b.meta, b.chan, b.off, b.ev, b.pid);
+    dk_next_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.meta, gen, b.off, n_events, b.g_max,
+                                                                 b.first, b.last, b.scnt);
     return cudaGetLastError();
 }
 
-cudaError_t launch_decay_assemble(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
-                                  int64_t* tiles, int64_t* off, int64_t* base, HadronRec* out, int grid,
-                                  cudaStream_t s) {
+cudaError_t launch_decay_layout(const DecayBuffers& b, int n_gen, int n_events, int32_t* ev_tot,
+                                int64_t* tiles, int64_t* evoff, cudaStream_t s) {
     if (n_events <= 0) return cudaSuccess;
     const unsigned eb = static_cast<unsigned>((n_events + 255) / 256);
-    dk_event_totals_kernel<<<eb, 256, 0, s>>>(b.gfirst, b.glast, n_gen, n_events, ev_tot);
-    cudaError_t e = launch_offsets_scan(ev_tot, n_events, tiles, off, s);
+    dk_event_totals_kernel<<<eb, 256, 0, s>>>(b.scnt, n_gen, n_events, ev_tot);
+    cudaError_t e = launch_offsets_scan(ev_tot, n_events, tiles, evoff, s);
     if (e != cudaSuccess) return e;
-    dk_event_bases_kernel<<<eb, 256, 0, s>>>(b.gfirst, b.glast, off, n_gen, n_events, base);
-    dk_gather_kernel<<<dim3(static_cast<unsigned>(n_events), static_cast<unsigned>(n_gen)), 256, 0, s>>>(
-        b.arena, n_events, b.gfirst, b.glast, base, out);
+    dk_shift_kernel<<<eb, 256, 0, s>>>(b.scnt, b.first, b.off, b.meta, evoff, n_gen, n_events, b.shift);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decay_write_generation(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
+                                          int64_t n, int64_t ib, const HadronRec* in, HadronRec* out_u,
+                                          const DecayBuffers& b, int n_events, int num_sms,
+                                          HadronRec* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    // three blocks of 256 fit per SM at 80 registers; small generations get
+    // one warp per 32 inputs at most
+    const int64_t want = (n + kDecayThreads - 1) / kDecayThreads;
+    const int grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms) * 3));
+    const int64_t r = static_cast<int64_t>(gen) * n_events;
+    decay_write_kernel<<<grid, kDecayThreads, 0, s>>>(cfg, t, gen, n, in, b.ev + ib, b.first + r,
+                                                      b.chan + ib, b.off + ib + gen, b.shift + r, out,
+                                                      out_u, b.failures);
     return cudaGetLastError();
 }
 
