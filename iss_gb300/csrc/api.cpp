@@ -94,6 +94,7 @@ struct iss_handle {
         dk_off, dk_etiles, dk_evoff;
     DevBuf<unsigned long long> dk_fail;
     int64_t dk_scap_hint = 0, dk_ucap_hint = 0, dk_icap_hint = 0;   // sizes the last call needed
+    int dk_gen_hint = 0;                           // generations the last call had
     int32_t dk_reruns = 0;                         // decay passes rerun in the last call
     int64_t cdf_len = 0, guide_len = 0, n_tiles = 0;
     int hydro_mode = 2;
@@ -751,11 +752,11 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
     }
     const int G = kDecayMaxGenerations;
     // first sizes: what the last call needed, else gpu_decay_arena_factor
-    // (default 1.5) times the sampled hadrons for the final lists,
+    // (default 2.0) times the sampled hadrons for the final lists,
     // gpu_decay_next_factor (0.5) for one generation's records and the
     // sampled hadrons plus twice that for the inputs of all generations; too
     // small only costs a rerun of the count sweep
-    const double fa = h->params.get_or("gpu_decay_arena_factor", 1.5);
+    const double fa = h->params.get_or("gpu_decay_arena_factor", 2.0);
     const double fu = h->params.get_or("gpu_decay_next_factor", 0.5);
     if (!(fa > 0.0) || !(fu > 0.0))
         return fail(h, ISS_ERR_INVALID_ARG, "gpu_decay_arena_factor / gpu_decay_next_factor must be > 0");
@@ -823,11 +824,14 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         b.g_max = static_cast<uint32_t>(G);
         CUDA_TRY(h, launch_decay_first_generation(h->dk_evoff.ptr, E, b, s));
         // count sweep: batches of generations, one wait (and a copy of the
-        // sizes) per batch
+        // sizes) per batch; the first batch has as many generations as the
+        // last call had, so that a repeated workload waits once
         int g = 0;
+        int batch = h->dk_gen_hint > 0 ? std::min(h->dk_gen_hint, kDecayBatch) : kDecayBatch;
         for (;;) {
-            for (int k = 0; k < kDecayBatch && g < G; k++, g++)
+            for (int k = 0; k < batch && g < G; k++, g++)
                 CUDA_TRY(h, launch_decay_count_generation(c, t, static_cast<uint32_t>(g), b, E, h->num_sms, s));
+            batch = kDecayBatch;
             CUDA_TRY(h, cudaMemcpyAsync(meta_h.data(), h->dk_meta.ptr, 8 * meta_h.size(),
                                         cudaMemcpyDeviceToHost, s));
             CUDA_TRY(h, cudaStreamSynchronize(s));
@@ -871,6 +875,7 @@ iss_status run_decays(iss_handle* h, unsigned long long* failures_out) {
         h->dk_scap_hint = std::max(h->dk_scap_hint, total + total / 8 + 4096);
         h->dk_ucap_hint = std::max(h->dk_ucap_hint, meta_h[kDecayMetaMaxU] + meta_h[kDecayMetaMaxU] / 8 + 4096);
         h->dk_icap_hint = std::max(h->dk_icap_hint, inputs + inputs / 8 + 4096);
+        h->dk_gen_hint = n_gen;
         std::swap(h->dk_final.ptr, h->d_hadrons.ptr);
         std::swap(h->dk_final.cap, h->d_hadrons.cap);
         h->n_hadrons = total;

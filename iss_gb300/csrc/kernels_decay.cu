@@ -12,8 +12,8 @@
 // The count sweep runs the generations on particle ids alone: a hadron's
 // channel and the kinds of its products do not depend on momenta.  Per
 // generation a count kernel (channel choice; stable and unstable products per
-// hadron), one packed exclusive scan and a daughters kernel (ids and events
-// of the unstable products: the next generation's input) give the sizes of
+// hadron) and one packed exclusive scan, which also writes the ids and events
+// of the unstable products (the next generation's input), give the sizes of
 // every generation and, per event, its range of inputs and its number of
 // stable products.  That fixes each event's final list, and the place of
 // every generation's stable products in it, before any kinematics run.
@@ -144,16 +144,19 @@ __device__ __forceinline__ int64_t meta_ib(const int64_t* __restrict__ meta, uin
 
 // Count kernel of generation gen: the channel cache and the packed counts of
 // every input.  The particle id comes from the sampled records (generation 0)
-// or from the ids the daughters kernel wrote (later generations).
+// or from the ids the previous generation's scan wrote (later generations).
 __global__ void __launch_bounds__(kDecayThreads)
 decay_count_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, const HadronRec* __restrict__ rec0,
                    const int32_t* __restrict__ pid_all, const int32_t* __restrict__ ev_all,
                    const int64_t* __restrict__ first, const int64_t* __restrict__ meta,
                    int32_t* __restrict__ chan_all, int64_t* __restrict__ cnt) {
     __shared__ int2 s_hash[kDecayHash];
+    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen);
+    // blocks without inputs leave before staging the table (late generations
+    // are small)
+    if (static_cast<int64_t>(blockIdx.x) * blockDim.x >= n) return;
     for (int j = threadIdx.x; j < kDecayHash; j += blockDim.x) s_hash[j] = t.hash[j];
     __syncthreads();
-    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen);
     const int32_t* ev = ev_all + ib;
     int32_t* chan = chan_all + ib;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
@@ -210,31 +213,63 @@ __device__ __forceinline__ void boost(const Lorentz& L, float E, float px, float
     *oz = pz + c * L.uz;
 }
 
-// the products of hadron m of event e (index ie in its event's generation
-// list) through channel `channel` of particle `type`: stable ones from
-// out_s[ps], unstable ones from out_u[pu]
+// the products of hadron *mp of event e (index ie in its event's
+// generation list) through channel `channel` of particle `type`: stable ones
+// from out_s[ps], unstable ones from out_u[pu].  The decay point and the
+// mother's velocity come first, so that each daughter is boosted and stored
+// as soon as its rest-frame momentum is known.
 __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDev& t, uint32_t gen,
-                                       const HadronRec& m, int e, uint32_t ie, int type, int channel,
-                                       int64_t ps, int64_t pu, HadronRec* __restrict__ out_s,
+                                       const HadronRec* __restrict__ mp_rec, int e, uint32_t ie, int type,
+                                       int channel, int64_t ps, int64_t pu, HadronRec* __restrict__ out_s,
                                        HadronRec* __restrict__ out_u,
                                        unsigned long long* __restrict__ failures) {
     const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
     const DecayChannel& ch = t.channels[channel];
-    DecayPlan d;
-    d.channel = channel;
-    d.type = type;
-    d.n = ch.n_daughters;
-    const DecayParticle& mp = t.particles[d.type];
+    const int n = ch.n_daughters;
+    const DecayParticle& mp = t.particles[type];
     const float M = mp.mass;       // pole mass (the reference does not sample Breit-Wigner)
     float md[3];
-    for (int k = 0; k < d.n; k++) {
+    for (int k = 0; k < n; k++) {
         const int di = ch.daughter[k];
         md[k] = di >= 0 ? t.particles[di].mass : 0.0f;
     }
-    float E[3], px[3], py[3], pz[3];
-    float life;
     const uint4 w1 = dblock(1u, ie, eg, gen, cfg.key0, cfg.key1);
-    if (d.n == 2) {
+    float dt, dx, dy, dz;
+    Lorentz L;
+    {
+        const HadronRec m = *mp_rec;
+        // life time gamma / Gamma in fm (src/particle_decay.cpp:396-401)
+        float life = 1e10f;
+        if (mp.width > 1e-10f) {
+            const float tau0 = m.E / M / mp.width;
+            life = -tau0 * __logf(u01f_pos(w1.w)) * 0.19733f;
+        }
+        const float inv = 1.0f / m.E;
+        dt = m.t + life;
+        dx = m.x + m.px * inv * life;
+        dy = m.y + m.py * inv * life;
+        dz = m.z + m.pz * inv * life;
+        L = velocity(m);
+    }
+    auto emit = [&](int k, float E, float px, float py, float pz) {
+        HadronRec r;
+        const int di = ch.daughter[k];
+        r.pid = di >= 0 ? t.particles[di].pid : 0;
+        r.mass = md[k];
+        boost(L, E, px, py, pz, &r.E, &r.px, &r.py, &r.pz);
+        r.t = dt;
+        r.x = dx;
+        r.y = dy;
+        r.z = dz;
+        if (daughter_stable(t, di)) {
+            store_rec(out_s + ps, r);
+            ps++;
+        } else {
+            store_rec(out_u + pu, r);
+            pu++;
+        }
+    };
+    if (n == 2) {
         const float m1 = md[0], m2 = md[1];
         const float a = M * M - m1 * m1 - m2 * m2;
         const float p = sqrtf(fmaxf(a * a - 4.0f * m1 * m1 * m2 * m2, 0.0f)) / (2.0f * M);
@@ -242,14 +277,9 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         __sincosf(kTwoPiD * (u01f(w1.x) - 0.5f), &sphi, &cphi);
         const float cth = 2.0f * (u01f(w1.y) - 0.5f);
         const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
-        px[0] = p * sth * cphi;
-        py[0] = p * sth * sphi;
-        pz[0] = p * cth;
-        E[0] = sqrtf(p * p + m1 * m1);
-        px[1] = -px[0];
-        py[1] = -py[0];
-        pz[1] = -pz[0];
-        E[1] = sqrtf(p * p + m2 * m2);
+        const float px = p * sth * cphi, py = p * sth * sphi, pz = p * cth;
+        emit(0, sqrtf(p * p + m1 * m1), px, py, pz);
+        emit(1, sqrtf(p * p + m2 * m2), -px, -py, -pz);
     } else {
         // phase space by rejection on (E1, E2) (src/particle_decay.cpp:445-458)
         const float m1 = md[0], m2 = md[1], m3 = md[2];
@@ -282,44 +312,21 @@ __device__ __noinline__ void decay_one(const DevConfig& cfg, const DecayTablesDe
         __sincosf(kTwoPiD * (u01f(w1.y) - 0.5f), &sksi, &cksi);
         const float cth = 2.0f * u01f(w1.z) - 1.0f;
         const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
-        px[0] = -p1 * sth * cksi;
-        py[0] = p1 * sth * sksi;
-        pz[0] = p1 * cth;
-        px[1] = tp2x * (cphi * cth * cksi - sphi * sksi) - tp2z * sth * cksi;
-        py[1] = tp2x * (-cphi * cth * sksi - sphi * cksi) + tp2z * sth * sksi;
-        pz[1] = tp2x * (cphi * sth) + tp2z * cth;
-        px[2] = tp3x * (cphi * cth * cksi - sphi * sksi) - tp3z * sth * cksi;
-        py[2] = tp3x * (-cphi * cth * sksi - sphi * cksi) + tp3z * sth * sksi;
-        pz[2] = tp3x * cphi * sth + tp3z * cth;
-        for (int k = 0; k < 3; k++)
-            E[k] = sqrtf(md[k] * md[k] + px[k] * px[k] + py[k] * py[k] + pz[k] * pz[k]);
-    }
-    // life time gamma / Gamma in fm (src/particle_decay.cpp:396-401)
-    life = 1e10f;
-    if (mp.width > 1e-10f) {
-        const float tau0 = m.E / M / mp.width;
-        life = -tau0 * __logf(u01f_pos(w1.w)) * 0.19733f;
-    }
-    const float inv = 1.0f / m.E;
-    const float dt = m.t + life, dx = m.x + m.px * inv * life, dy = m.y + m.py * inv * life,
-                dz = m.z + m.pz * inv * life;
-    const Lorentz L = velocity(m);
-    for (int k = 0; k < d.n; k++) {
-        HadronRec r;
-        const int di = ch.daughter[k];
-        r.pid = di >= 0 ? t.particles[di].pid : 0;
-        r.mass = md[k];
-        boost(L, E[k], px[k], py[k], pz[k], &r.E, &r.px, &r.py, &r.pz);
-        r.t = dt;
-        r.x = dx;
-        r.y = dy;
-        r.z = dz;
-        if (daughter_stable(t, di)) {
-            store_rec(out_s + ps, r);
-            ps++;
-        } else {
-            store_rec(out_u + pu, r);
-            pu++;
+        {
+            const float px = -p1 * sth * cksi, py = p1 * sth * sksi, pz = p1 * cth;
+            emit(0, sqrtf(md[0] * md[0] + px * px + py * py + pz * pz), px, py, pz);
+        }
+        {
+            const float px = tp2x * (cphi * cth * cksi - sphi * sksi) - tp2z * sth * cksi;
+            const float py = tp2x * (-cphi * cth * sksi - sphi * cksi) + tp2z * sth * sksi;
+            const float pz = tp2x * (cphi * sth) + tp2z * cth;
+            emit(1, sqrtf(md[1] * md[1] + px * px + py * py + pz * pz), px, py, pz);
+        }
+        {
+            const float px = tp3x * (cphi * cth * cksi - sphi * sksi) - tp3z * sth * cksi;
+            const float py = tp3x * (-cphi * cth * sksi - sphi * cksi) + tp3z * sth * sksi;
+            const float pz = tp3x * cphi * sth + tp3z * cth;
+            emit(2, sqrtf(md[2] * md[2] + px * px + py * py + pz * pz), px, py, pz);
         }
     }
 }
@@ -349,7 +356,7 @@ decay_write_kernel(DevConfig cfg, DecayTablesDev t, uint32_t gen, int64_t n,
         const int32_t c = chan[i];
         const int e = ev[i];
         const int64_t o = off[i];
-        decay_one(cfg, t, gen, in[i], e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF,
+        decay_one(cfg, t, gen, in + i, e, static_cast<uint32_t>(i - first[e]), c >> 16, c & 0xFFFF,
                   shift[e] + (o >> 32), o & 0xFFFFFFFFll, out, out_u, failures);
     };
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
@@ -469,14 +476,38 @@ dk_tile_offset_kernel(int64_t* __restrict__ tiles, const int64_t* __restrict__ m
     if (threadIdx.x == 0) off_all[meta_ib(meta, gen) + gen + n] = carry;
 }
 
+// the next generation's inputs made by input c (a decaying hadron of event
+// e): the particle id and event of each unstable product, from slot pu on;
+// slots at or past i_cap are skipped (the generation then fails the size
+// check and the call reruns)
+__device__ void write_daughters(const DecayTablesDev& t, int32_t c, int e, int64_t pu, int64_t i_cap,
+                                int32_t* __restrict__ ev_all, int32_t* __restrict__ pid_all) {
+    const DecayChannel& ch = t.channels[c & 0xFFFF];
+    for (int k = 0; k < ch.n_daughters; k++) {
+        const int di = ch.daughter[k];
+        if (daughter_stable(t, di)) continue;
+        if (pu < i_cap) {
+            pid_all[pu] = t.particles[di].pid;
+            ev_all[pu] = e;
+        }
+        pu++;
+    }
+}
+
+// The scan of each tile, and the next generation's inputs: a thread scans 16
+// consecutive inputs and writes the products of those with unstable ones
+// (whose inputs follow this generation's, at meta_ib + n); the offsets go
+// back through shared memory to coalesced stores.
 __global__ void __launch_bounds__(kDkScanThreads)
-dk_tile_scan_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ meta, uint32_t gen,
-                    const int64_t* __restrict__ tiles, int64_t* __restrict__ off_all) {
+dk_tile_scan_kernel(DecayTablesDev t, const int64_t* __restrict__ c, const int64_t* __restrict__ meta,
+                    uint32_t gen, const int64_t* __restrict__ tiles, const int32_t* __restrict__ chan_all,
+                    int32_t* __restrict__ ev_all, int32_t* __restrict__ pid_all, int64_t i_cap,
+                    int64_t* __restrict__ off_all) {
     __shared__ long long s_in[kDkScanThreads * (kDkScanPer + 1)];
     __shared__ long long s_warp[33];
-    const int64_t n = meta_n(meta, gen);
+    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen), nb = ib + n;
     const int64_t nt = (n + kDkTile - 1) / kDkTile;
-    int64_t* off = off_all + meta_ib(meta, gen) + gen;
+    int64_t* off = off_all + ib + gen;
     for (int64_t tl = blockIdx.x; tl < nt; tl += gridDim.x) {
         const int64_t t0 = tl * kDkTile;
         for (int k = 0; k < kDkScanPer; k++) {
@@ -485,17 +516,26 @@ dk_tile_scan_kernel(const int64_t* __restrict__ c, const int64_t* __restrict__ m
             s_in[(e / kDkScanPer) * (kDkScanPer + 1) + e % kDkScanPer] = i < n ? c[i] : 0;
         }
         __syncthreads();
-        const long long* mine = s_in + threadIdx.x * (kDkScanPer + 1);
+        long long* mine = s_in + threadIdx.x * (kDkScanPer + 1);
         long long acc = 0;
 #pragma unroll
         for (int k = 0; k < kDkScanPer; k++) acc += mine[k];
         long long tot;
         long long run = tiles[tl] + dk_block_excl(acc, s_warp, &tot);
         const int64_t e0 = t0 + static_cast<int64_t>(threadIdx.x) * kDkScanPer;
-#pragma unroll
         for (int k = 0; k < kDkScanPer; k++) {
-            if (e0 + k < n) off[e0 + k] = run;
-            run += mine[k];
+            const long long v = mine[k];
+            if ((v & 0xFFFFFFFFll) != 0)
+                write_daughters(t, chan_all[ib + e0 + k], ev_all[ib + e0 + k], nb + (run & 0xFFFFFFFFll),
+                                i_cap, ev_all, pid_all);
+            mine[k] = run;
+            run += v;
+        }
+        __syncthreads();
+        for (int k = 0; k < kDkScanPer; k++) {
+            const int e = k * kDkScanThreads + threadIdx.x;
+            const int64_t i = t0 + e;
+            if (i < n) off[i] = s_in[(e / kDkScanPer) * (kDkScanPer + 1) + e % kDkScanPer];
         }
         __syncthreads();
     }
@@ -534,37 +574,6 @@ __global__ void dk_advance_kernel(int64_t* __restrict__ meta, uint32_t gen, cons
     meta[kDecayMetaSBase + gen + 1] = next_sb;
     meta[kDecayMetaIBase + gen + 1] = next_ib;
     if (ut > meta[kDecayMetaMaxU]) meta[kDecayMetaMaxU] = ut;
-}
-
-// The next generation's inputs: the particle id and event of every unstable
-// product, in the order of the unstable scan.
-__global__ void __launch_bounds__(kDecayThreads)
-dk_daughters_kernel(DecayTablesDev t, uint32_t gen, const int64_t* __restrict__ meta,
-                    const int32_t* __restrict__ chan_all, const int64_t* __restrict__ off_all,
-                    int32_t* __restrict__ ev_all, int32_t* __restrict__ pid_all) {
-    if (meta[kDecayMetaFlags] != 0) return;
-    const int64_t n = meta_n(meta, gen), ib = meta_ib(meta, gen), nb = meta_ib(meta, gen + 1);
-    const int32_t* chan = chan_all + ib;
-    const int64_t* off = off_all + ib + gen;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int32_t c = chan[i];
-        if (c < 0) continue;
-        const DecayChannel& ch = t.channels[c & 0xFFFF];
-        int64_t pu = -1;
-        int e = 0;
-        for (int k = 0; k < ch.n_daughters; k++) {
-            const int di = ch.daughter[k];
-            if (daughter_stable(t, di)) continue;
-            if (pu < 0) {
-                pu = nb + (off[i] & 0xFFFFFFFFll);
-                e = ev_all[ib + i];
-            }
-            pid_all[pu] = t.particles[di].pid;
-            ev_all[pu] = e;
-            pu++;
-        }
-    }
 }
 
 // Per event: its stable products in this generation (scnt) and its input
@@ -642,9 +651,9 @@ cudaError_t launch_decay_count_generation(const DevConfig& cfg, const DecayTable
                                                       b.chan, b.cnt);
     dk_tile_sum_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles);
     dk_tile_offset_kernel<<<1, kDkScanThreads, 0, s>>>(b.tiles, b.meta, gen, b.off);
-    dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(b.cnt, b.meta, gen, b.tiles, b.off);
+    dk_tile_scan_kernel<<<grid, kDkScanThreads, 0, s>>>(t, b.cnt, b.meta, gen, b.tiles, b.chan, b.ev, b.pid,
+                                                        b.i_cap, b.off);
     dk_advance_kernel<<<1, 32, 0, s>>>(b.meta, gen, b.off, b.s_cap, b.u_cap, b.i_cap, b.g_max);
-    dk_daughters_kernel<<<grid, kDecayThreads, 0, s>>>(t, gen, b.meta, b.chan, b.off, b.ev, b.pid);
     dk_next_bounds_kernel<<<(n_events + 255) / 256, 256, 0, s>>>(b.meta, gen, b.off, n_events, b.g_max,
                                                                  b.first, b.last, b.scnt);
     return cudaGetLastError();
