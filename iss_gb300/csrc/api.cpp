@@ -114,6 +114,9 @@ struct iss_handle {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;     // device->host copies of iss_gpu_generate_into
+    // the captured generate's second branch (the counts beside the CDF scan)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<cudaEvent_t> chunk_ev;      // end of each sampling chunk
     std::vector<cudaEvent_t> copy_ev;       // streamed generates: end of each chunk's copy
     iss_hadron_t* stream_host = nullptr;    // streamed generates: two page-locked chunk buffers
@@ -234,6 +237,9 @@ struct iss_handle {
             d_spid.release();
             d_lpairs.release();
             if (copy_stream) cudaStreamDestroy(copy_stream);
+            if (aux_stream) cudaStreamDestroy(aux_stream);
+            if (ev_fork) cudaEventDestroy(ev_fork);
+            if (ev_join) cudaEventDestroy(ev_join);
             if (stream) cudaStreamDestroy(stream);
         }
     }
@@ -1003,9 +1009,14 @@ void record(iss_handle* h, int ev, bool capturing) {
         cudaEventRecord(h->ev[ev], h->stream);
 }
 
-// the device sequence of one generate, with device-side sizes (no host sync)
+// The device sequence of one generate, with device-side sizes (no host
+// sync).  The counts need only the per-species totals, which the CDF's tile
+// offsets give, so they run on a second branch beside the CDF scan; the
+// sampler waits for both.  kEvCounts then marks the join: the counts phase
+// reports the part of the counts the scan did not cover.
 cudaError_t enqueue_generate(iss_handle* h, const DevConfig& c) {
     cudaStream_t s = h->stream;
+    cudaStream_t a = h->aux_stream;
     const int64_t n = h->n_cells;
     const int S = c.n_species;
     const int64_t nseg = static_cast<int64_t>(c.n_events) * S;
@@ -1020,18 +1031,24 @@ cudaError_t enqueue_generate(iss_handle* h, const DevConfig& c) {
     record(h, kEvPrologue, true);
     GTRY(launch_yields(c, cells, h->d_species.ptr, h->d_yields.ptr, h->d_ymax.ptr, s));
     record(h, kEvYields, true);
-    GTRY(launch_cdf(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S, h->d_ymax.ptr,
-                    h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
-                    h->d_guide.ptr, s));
-    record(h, kEvCdf, true);
-    GTRY(cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), s));
+    GTRY(launch_cdf_head(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S, h->d_ymax.ptr,
+                         h->d_tile_sum.ptr, h->d_tile_off.ptr, h->d_qtot.ptr, h->d_totals.ptr, h->d_cdf.ptr,
+                         h->d_guide.ptr, s));
+    GTRY(cudaEventRecord(h->ev_fork, s));
+    GTRY(cudaStreamWaitEvent(a, h->ev_fork, 0));
+    GTRY(cudaMemsetAsync(h->d_error.ptr, 0, sizeof(int), a));
     GTRY(launch_counts(c, h->d_species.ptr, h->d_totals.ptr, h->d_pois.ptr, h->d_counts.ptr,
-                       h->d_items.ptr, h->d_error.ptr, s));
-    GTRY(launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, s));
-    GTRY(launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, s));
+                       h->d_items.ptr, h->d_error.ptr, a));
+    GTRY(launch_offsets_scan(h->d_counts.ptr, nseg, h->d_off_tiles.ptr, h->d_offsets.ptr, a));
+    GTRY(launch_offsets_scan(h->d_items.ptr, nseg, h->d_off_tiles.ptr, h->d_item_off.ptr, a));
     GTRY(launch_graph_limits(h->d_offsets.ptr, h->d_item_off.ptr, nseg, h->graph_cap_units,
-                             h->graph_cap_items, h->d_limits.ptr, s));
-    GTRY(launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, s, h->d_limits.ptr));
+                             h->graph_cap_items, h->d_limits.ptr, a));
+    GTRY(launch_item_map(h->d_items.ptr, h->d_item_off.ptr, nseg, h->d_item_seg.ptr, a, h->d_limits.ptr));
+    GTRY(cudaEventRecord(h->ev_join, a));
+    GTRY(launch_cdf_scan(h->d_yields.ptr, n, h->d_surf.ptr, c.n_surfaces, h->n_tiles, S, h->d_ymax.ptr,
+                         h->d_tile_off.ptr, h->d_qtot.ptr, h->d_cdf.ptr, h->d_guide.ptr, s));
+    record(h, kEvCdf, true);
+    GTRY(cudaStreamWaitEvent(s, h->ev_join, 0));
     record(h, kEvCounts, true);
     GTRY(cudaMemsetAsync(h->d_work.ptr, 0, sizeof(unsigned long long), s));
     GTRY(cudaMemsetAsync(h->d_counters.ptr, 0, sizeof(SampleCounters), s));
@@ -1075,6 +1092,16 @@ iss_status capture_graph(iss_handle* h, int64_t n_items) {
     c.run = h->d_run.ptr;
     c.chunk_events = std::max(E, 1);
     cudaStream_t s = h->stream;
+    if (!h->aux_stream) {
+        // the counts branch at the highest priority: its blocks go first
+        // whenever the CDF scan's blocks leave room (the graph keeps stream
+        // priorities as node priorities)
+        int least = 0, greatest = 0;
+        CUDA_TRY(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CUDA_TRY(h, cudaStreamCreateWithPriority(&h->aux_stream, cudaStreamNonBlocking, greatest));
+    }
+    for (cudaEvent_t* e : {&h->ev_fork, &h->ev_join})
+        if (!*e) CUDA_TRY(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     cudaGraph_t graph = nullptr;
     CUDA_TRY(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     const cudaError_t ce = enqueue_generate(h, c);
@@ -1089,7 +1116,8 @@ iss_status capture_graph(iss_handle* h, int64_t n_items) {
                         cudaGetErrorString(ce != cudaSuccess ? ce : ee);
         return ISS_OK;
     }
-    const cudaError_t ie = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+    const cudaError_t ie =
+        cudaGraphInstantiateWithFlags(&h->graph_exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) {
         h->graph_exec = nullptr;

@@ -27,6 +27,16 @@ cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int 
                        int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
                        unsigned long long* tile_off, unsigned long long* qtot, double* totals,
                        unsigned long long* cdf, int32_t* guide, cudaStream_t stream);
+// the same in two parts: tile sums and tile offsets (which also give qtot and
+// totals), then the scan that writes the CDF rows and guide tables
+cudaError_t launch_cdf_head(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                            int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
+                            unsigned long long* tile_off, unsigned long long* qtot, double* totals,
+                            unsigned long long* cdf, int32_t* guide, cudaStream_t stream);
+cudaError_t launch_cdf_scan(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                            int64_t n_tiles, int S, const uint32_t* ymax, const unsigned long long* tile_off,
+                            const unsigned long long* qtot, unsigned long long* cdf, int32_t* guide,
+                            cudaStream_t stream);
 
 // kernels_sample.cu
 // two launches: Poisson constants and inversion tables of every (surface,

@@ -653,10 +653,10 @@ cudaError_t launch_yields(const DevConfig& cfg, const CellArrays& cells, const S
 
 int cdf_num_tiles(int64_t n) { return static_cast<int>((n + kScanTile - 1) / kScanTile); }
 
-cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
-                       int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
-                       unsigned long long* tile_off, unsigned long long* qtot, double* totals,
-                       unsigned long long* cdf, int32_t* guide, cudaStream_t stream) {
+cudaError_t launch_cdf_head(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                            int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
+                            unsigned long long* tile_off, unsigned long long* qtot, double* totals,
+                            unsigned long long* cdf, int32_t* guide, cudaStream_t stream) {
     if (n_tiles <= 0 || S <= 0 || n_surf <= 0) return cudaSuccess;
     const int rows = n_surf * S;
     const unsigned grid = static_cast<unsigned>(n_tiles);
@@ -664,9 +664,28 @@ cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int 
                                                           tile_sum);
     cdf_tile_offset_kernel<<<rows, kScanThreads, 0, stream>>>(surf, S, tile_sum, ymax, tile_off,
                                                              qtot, totals, cdf, guide);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cdf_scan(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                            int64_t n_tiles, int S, const uint32_t* ymax, const unsigned long long* tile_off,
+                            const unsigned long long* qtot, unsigned long long* cdf, int32_t* guide,
+                            cudaStream_t stream) {
+    if (n_tiles <= 0 || S <= 0 || n_surf <= 0) return cudaSuccess;
+    const unsigned grid = static_cast<unsigned>(n_tiles);
     cdf_tile_scan_kernel<<<grid, kScanThreads, 0, stream>>>(yields, N, surf, n_surf, S, ymax,
                                                            tile_off, qtot, cdf, guide);
     return cudaGetLastError();
+}
+
+cudaError_t launch_cdf(const float* yields, int64_t N, const SurfSeg* surf, int n_surf,
+                       int64_t n_tiles, int S, uint32_t* ymax, unsigned long long* tile_sum,
+                       unsigned long long* tile_off, unsigned long long* qtot, double* totals,
+                       unsigned long long* cdf, int32_t* guide, cudaStream_t stream) {
+    const cudaError_t e = launch_cdf_head(yields, N, surf, n_surf, n_tiles, S, ymax, tile_sum, tile_off,
+                                          qtot, totals, cdf, guide, stream);
+    if (e != cudaSuccess) return e;
+    return launch_cdf_scan(yields, N, surf, n_surf, n_tiles, S, ymax, tile_off, qtot, cdf, guide, stream);
 }
 
 }  // namespace iss
