@@ -425,6 +425,9 @@ off_tile_scan_kernel(const int32_t* __restrict__ counts, int64_t n,
 
 struct Prop {
     float T, m, a, mt, Kmax, W, w32, w3, qa;
+    // two-term Bose proposal (prop_bose2): W1 the weight of the e^-E~ term
+    // (W = W1 + that of e^-2E~), r2 = 4 e^a; W1 = W for a one-term proposal
+    float W1, r2;
     float mut, cpoly, rmax;
     int compat, sign;
     // flux geometry in the LRF: dsigma_mu = (d0, D n); e1 _|_ n is rebuilt
@@ -702,18 +705,51 @@ __device__ float compat_ratio(const Prop& p, float Et) {
     return num / den;
 }
 
+// The two-term Bose proposal of bosons (the plain sampler's): |p| from
+// (K^2 + 2 m~ K + m~^2/2) (e^-K + e^-a e^-2K), i.e. p^2-weighted
+// e^-E~ + e^-2E~, the first two terms of the Bose-Einstein series.  The
+// e^-2K term is a Gamma(3), Gamma(2), Gamma(1) mixture at rate 2 with weights
+// (1, 2 m~, m~^2) e^-a / 4.  Against this proposal the statistics factor is
+// f_BE / (e^-E~ + e^-2E~) = 1 / (1 - e^-2E~), largest at K = 0, so the try
+// accepts with qa / (1 - e^-2E~), qa = 1 - e^-2a (for pions about 0.86 on
+// average, against 0.67 with the one-term proposal).  Fermions keep the
+// one-term proposal (W1 = W).
+__device__ __forceinline__ void prop_bose2(Prop& p) {
+    p.W1 = p.W;
+    p.r2 = 0.0f;
+    if (p.sign != -1) return;
+    const float ea = __expf(-p.a);
+    p.W = p.W1 + 0.25f * ea * (1.0f + p.mt) * (1.0f + p.mt);
+    p.r2 = 4.0f / ea;
+    p.qa = p.a > 0.025f ? 1.0f - ea * ea : -expm1f(-2.0f * p.a);
+}
+
 // One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
-// the uniform used for the rapidity of boost-invariant surfaces.
-template <int kMode = 0>
+// the uniform used for the rapidity of boost-invariant surfaces.  kBose2:
+// the proposal of prop_bose2 (the plain sampler); otherwise the one-term
+// proposal the learned sampler's densities assume.
+template <int kMode = 0, bool kBose2 = false>
 __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, const Unit& u,
                                          float4& pl, float& u_rap, unsigned& violations) {
     const uint32_t c3 = static_cast<uint32_t>(u.s) | (kTagTry << 16);
     const uint4 A = block(2u * u.t, u.i, u.eg, c3, cfg.key0, cfg.key1);
     const float sel = u01f(A.x) * p.W;
     float prod = u01f_pos(A.y);
-    if (sel < p.w32) prod *= u01f_pos(A.z);
-    if (sel < p.w3) prod *= u01f_pos(A.w);
-    const float K = -logf(prod);
+    float K;
+    if constexpr (kBose2) {
+        // term 1 (sel < W1): Gamma(3) below 2, Gamma(2) below 2 + 2 m~; term 2
+        // rescaled to [0, (1 + m~)^2): Gamma(3) below 1, Gamma(2) below 1 + 2 m~
+        const bool t2 = sel >= p.W1;
+        const float s = t2 ? (sel - p.W1) * p.r2 : sel;
+        const float th3 = t2 ? 1.0f : 2.0f;
+        if (s < th3 + 2.0f * p.mt) prod *= u01f_pos(A.z);
+        if (s < th3) prod *= u01f_pos(A.w);
+        K = -logf(prod) * (t2 ? 0.5f : 1.0f);
+    } else {
+        if (sel < p.w32) prod *= u01f_pos(A.z);
+        if (sel < p.w3) prod *= u01f_pos(A.w);
+        K = -logf(prod);
+    }
     if (K > p.Kmax) return false;
     const uint4 B = block(2u * u.t + 1u, u.i, u.eg, c3, cfg.key0, cfg.key1);
     const float k2 = K * (K + 2.0f * p.mt);
@@ -722,10 +758,15 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     const float a_pE = Et * ptil / (k2 + 0.5f * p.mt * p.mt);
     const float Etil = p.a + K;
     const float em = expf(-Etil);
-    // 1 - e^-Etil from em where that is accurate (Etil > 0.05: relative
+    // 1 - e^-Etil (1 - e^-2Etil) from em where that is accurate (relative
     // error below 3e-6); expm1f near Bose condensation only
-    const float a_q = (p.sign == -1) ? p.qa / (Etil > 0.05f ? 1.0f - em : -expm1f(-Etil))
-                                     : 1.0f / (1.0f + em);
+    float a_q;
+    if (kBose2)
+        a_q = (p.sign == -1) ? p.qa / (Etil > 0.025f ? 1.0f - em * em : -expm1f(-2.0f * Etil))
+                             : 1.0f / (1.0f + em);
+    else
+        a_q = (p.sign == -1) ? p.qa / (Etil > 0.05f ? 1.0f - em : -expm1f(-Etil))
+                             : 1.0f / (1.0f + em);
     float a_c = 1.0f;
     if (kMode == 0 && p.compat) {
         a_c = compat_ratio(p, Etil) / p.rmax;
@@ -1270,22 +1311,26 @@ __device__ void emit_efa(const DevConfig& cfg, const CellArrays& cells, const Pr
 template <int kAlg> struct PropOf { using type = Prop; };
 template <> struct PropOf<2> { using type = PropEfa; };
 
+// bose2: the hadron takes the plain proposal (prop_bose2); false for those
+// of the learned proposal, whose densities assume the one-term proposal
 template <int kMode>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
-                                          const SpeciesDev& sp, int l, Prop& p, bool) {
-    return setup_prop<kMode>(cfg, cells, sp, l, p);
+                                          const SpeciesDev& sp, int l, Prop& p, bool, bool bose2) {
+    const bool ok = setup_prop<kMode>(cfg, cells, sp, l, p);
+    if (bose2) prop_bose2(p);
+    return ok;
 }
 template <int kMode>
 __device__ __forceinline__ bool setup_any(const DevConfig& cfg, const CellArrays& cells,
-                                          const SpeciesDev& sp, int l, PropEfa& p, bool keep_max) {
+                                          const SpeciesDev& sp, int l, PropEfa& p, bool keep_max, bool) {
     return setup_efa(cfg, cells, sp, l, p, keep_max);
 }
-template <int kMode>
+template <int kMode, bool kBose2>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const Prop& p, const Unit& u, float4& pl,
                                         float& u_rap, unsigned& viol) {
-    return try_once<kMode>(cfg, p, u, pl, u_rap, viol);
+    return try_once<kMode, kBose2>(cfg, p, u, pl, u_rap, viol);
 }
-template <int kMode>
+template <int kMode, bool kBose2>
 __device__ __forceinline__ bool try_any(const DevConfig& cfg, const PropEfa& p, const Unit& u,
                                         float4& pl, float& u_rap, unsigned& viol) {
     return try_efa(cfg, p, u, pl, u_rap, viol);
@@ -1544,7 +1589,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
                                    : nullptr;
                 }
-                if (!setup_any<kMode>(cfg, cells, species[u.s], l, p, false)) {
+                if (!setup_any<kMode>(cfg, cells, species[u.s], l, p, false, !kLearned || !u.lp)) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     for (int q = 0; q < (kLcc ? u.mult : 1); q++)
@@ -1563,10 +1608,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     n_ltries++;
                     n_lhad += ok;
                 } else {
-                    ok = try_once<kMode>(cfg, p, u, pl, u_rap, n_viol);
+                    ok = try_once<kMode, true>(cfg, p, u, pl, u_rap, n_viol);
                 }
             } else {
-                ok = try_any<kMode>(cfg, p, u, pl, u_rap, n_viol);
+                ok = try_any<kMode, true>(cfg, p, u, pl, u_rap, n_viol);
             }
             u.t++;
             u.tries_cell++;
@@ -1592,7 +1637,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
                     // (the lab-frame sampler keeps the hadron's maximum for
                     // its partner, src/emissionfunction.cpp:3503-3509)
-                    if (!setup_any<kMode>(cfg, cells, sp2, u.cell, p, true)) {
+                    if (!setup_any<kMode>(cfg, cells, sp2, u.cell, p, true, true)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
                         write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);

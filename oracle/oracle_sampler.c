@@ -10,7 +10,9 @@
  *   FSSW::add_one_sampled_particle,       src/FSSW.cpp:1969-1996
  *
  * The GPU proposes |p| from an exact Gamma mixture matching (E^2 - m^2/2)
- * exp(-(E - mu)/T), the direction from the Cooper-Frye flux factor itself
+ * exp(-(E - mu)/T) (for bosons (E^2 - m^2/2) (exp(-(E - mu)/T) +
+ * exp(-2(E - mu)/T)), the first two terms of the Bose-Einstein series, whose
+ * second term is the same mixture at rate 2), the direction from the Cooper-Frye flux factor itself
  * (linear in the cosine of the angle to the spatial part of dsigma in the rest
  * frame, inverse CDF), and folds the quantum-statistics, pE/(E^2 - m^2/2),
  * |p|-dependent flux remainder and delta-f acceptances into one uniform per
@@ -65,7 +67,8 @@ typedef struct {
     double m, mt, mu, mut, a, T, beta;
     int boson;
     double Kmax, w3, w2, W;
-    double qa;             /* 1 - exp(-a) for bosons */
+    double W1, r2;         /* bosons: weight of the exp(-E~) term, 4 exp(a) */
+    double qa;             /* 1 - exp(-2a) for bosons */
     int compat;            /* reproduce the reference's truncated/buggy series */
     double rmax;
     double c_poly;         /* mu~^2 - m~^2/2 */
@@ -104,7 +107,17 @@ static void orc_setup(const orc_cfg* cfg, double m, int sign, double mu_raw, dou
     p->w3 = 2.0;
     p->w2 = 2.0 * p->mt;
     p->W = p->w3 + p->w2 + 0.5 * p->mt * p->mt;
+    p->W1 = p->W;
+    p->r2 = 0.0;
     p->qa = -expm1(-p->a);
+    if (p->boson) {
+        /* the exp(-2 E~) term: Gamma(3), Gamma(2), Gamma(1) at rate 2 with
+         * weights (1, 2 m~, m~^2) exp(-a) / 4 */
+        const double ea = exp(-p->a);
+        p->W = p->W1 + 0.25 * ea * (1.0 + p->mt) * (1.0 + p->mt);
+        p->r2 = 4.0 / ea;
+        p->qa = -expm1(-2.0 * p->a);
+    }
     p->compat = (cfg->compat_fermion && sampler == 0) ? 1 : 0;
     p->c_poly = p->mut * p->mut - 0.5 * p->mt * p->mt;
     p->rmax = 1.0;
@@ -163,9 +176,15 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     orc_hblock(hs, 2u * t + 1u, ORC_TAG_TRY, Bw);
     const double sel = orc_u01(A[0]) * p->W;
     double prod = orc_u01_pos(A[1]);
-    if (sel < p->w3 + p->w2) prod *= orc_u01_pos(A[2]);
-    if (sel < p->w3) prod *= orc_u01_pos(A[3]);
-    const double K = -log(prod);
+    /* term 1 (sel < W1): Gamma(3) below 2, Gamma(2) below 2 + 2 m~; term 2
+     * (bosons) rescaled to [0, (1 + m~)^2): Gamma(3) below 1, Gamma(2) below
+     * 1 + 2 m~, and K at rate 2 */
+    const int t2 = sel >= p->W1;
+    const double s = t2 ? (sel - p->W1) * p->r2 : sel;
+    const double th3 = t2 ? 1.0 : 2.0;
+    if (s < th3 + 2.0 * p->mt) prod *= orc_u01_pos(A[2]);
+    if (s < th3) prod *= orc_u01_pos(A[3]);
+    const double K = -log(prod) * (t2 ? 0.5 : 1.0);
     if (K > p->Kmax) return 0;
     const double k2 = K * (K + 2.0 * p->mt);
     const double Et = K + p->mt;                  /* E / T */
@@ -173,7 +192,9 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     const double a_pE = Et * ptil / (k2 + 0.5 * p->mt * p->mt);
     const double Etil = p->a + K;                 /* (E - mu) / T */
     const double em = exp(-Etil);
-    const double a_q = p->boson ? p->qa / (-expm1(-Etil)) : 1.0 / (1.0 + em);
+    /* bosons: f_BE / (exp(-E~) + exp(-2 E~)) = 1 / (1 - exp(-2 E~)), at most
+     * 1 / qa */
+    const double a_q = p->boson ? p->qa / (-expm1(-2.0 * Etil)) : 1.0 / (1.0 + em);
     double a_c = 1.0;
     if (p->compat) {
         a_c = orc_compat_ratio(p, Etil) / p->rmax;
