@@ -425,9 +425,10 @@ off_tile_scan_kernel(const int32_t* __restrict__ counts, int64_t n,
 
 struct Prop {
     float T, m, a, mt, Kmax, W, w32, w3, qa;
-    // two-term Bose proposal (prop_bose2): W1 the weight of the e^-E~ term
-    // (W = W1 + that of e^-2E~), r2 = 4 e^a; W1 = W for a one-term proposal
-    float W1, r2;
+    // three-term Bose proposal (prop_bose2): W1 the weight of the e^-E~
+    // term, W12 that of the first two (W adds e^-3E~), r2 = 4 e^a; W1 = W12 =
+    // W for a one-term proposal
+    float W1, W12, r2;
     float mut, cpoly, rmax;
     int compat, sign;
     // flux geometry in the LRF: dsigma_mu = (d0, D n); e1 _|_ n is rebuilt
@@ -705,23 +706,26 @@ __device__ float compat_ratio(const Prop& p, float Et) {
     return num / den;
 }
 
-// The two-term Bose proposal of bosons (the plain sampler's): |p| from
-// (K^2 + 2 m~ K + m~^2/2) (e^-K + e^-a e^-2K), i.e. p^2-weighted
-// e^-E~ + e^-2E~, the first two terms of the Bose-Einstein series.  The
-// e^-2K term is a Gamma(3), Gamma(2), Gamma(1) mixture at rate 2 with weights
-// (1, 2 m~, m~^2) e^-a / 4.  Against this proposal the statistics factor is
-// f_BE / (e^-E~ + e^-2E~) = 1 / (1 - e^-2E~), largest at K = 0, so the try
-// accepts with qa / (1 - e^-2E~), qa = 1 - e^-2a (for pions about 0.86 on
-// average, against 0.67 with the one-term proposal).  Fermions keep the
-// one-term proposal (W1 = W).
+// The Bose proposal of bosons (the plain sampler's): |p| from
+// (K^2 + 2 m~ K + m~^2/2) (e^-K + e^-a e^-2K + e^-2a e^-3K), i.e. p^2-weighted
+// e^-E~ + e^-2E~ + e^-3E~, the first three terms of the Bose-Einstein series.
+// Term n is a Gamma(3), Gamma(2), Gamma(1) mixture at rate n with weights
+// e^-(n-1)a (2/n^3, 2 m~/n^2, m~^2/(2n)), i.e. e^-(n-1)a (2/n^3) (1, n m~,
+// n^2 m~^2/4).  Against this proposal the statistics factor is
+// f_BE / (e^-E~ + e^-2E~ + e^-3E~) = 1 / (1 - e^-3E~), largest at K = 0, so
+// the try accepts with qa / (1 - e^-3E~), qa = 1 - e^-3a (for pions about 0.94
+// on average, against 0.67 with the one-term proposal).  Fermions keep the
+// one-term proposal (W1 = W12 = W).
 __device__ __forceinline__ void prop_bose2(Prop& p) {
     p.W1 = p.W;
+    p.W12 = p.W;
     p.r2 = 0.0f;
     if (p.sign != -1) return;
     const float ea = __expf(-p.a);
-    p.W = p.W1 + 0.25f * ea * (1.0f + p.mt) * (1.0f + p.mt);
+    p.W12 = p.W1 + 0.25f * ea * (1.0f + p.mt) * (1.0f + p.mt);
+    p.W = p.W12 + (2.0f / 27.0f) * ea * ea * (1.0f + 1.5f * p.mt) * (1.0f + 1.5f * p.mt);
     p.r2 = 4.0f / ea;
-    p.qa = p.a > 0.025f ? 1.0f - ea * ea : -expm1f(-2.0f * p.a);
+    p.qa = p.a > 0.0167f ? 1.0f - ea * ea * ea : -expm1f(-3.0f * p.a);
 }
 
 // One proposal.  On acceptance fills the LRF momentum (p0, px, py, pz) and
@@ -737,14 +741,17 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     float prod = u01f_pos(A.y);
     float K;
     if constexpr (kBose2) {
-        // term 1 (sel < W1): Gamma(3) below 2, Gamma(2) below 2 + 2 m~; term 2
-        // rescaled to [0, (1 + m~)^2): Gamma(3) below 1, Gamma(2) below 1 + 2 m~
-        const bool t2 = sel >= p.W1;
-        const float s = t2 ? (sel - p.W1) * p.r2 : sel;
-        const float th3 = t2 ? 1.0f : 2.0f;
-        if (s < th3 + 2.0f * p.mt) prod *= u01f_pos(A.z);
-        if (s < th3) prod *= u01f_pos(A.w);
-        K = -logf(prod) * (t2 ? 0.5f : 1.0f);
+        // term n rescaled to weights (1, n m~, n^2 m~^2/4): Gamma(3) below 1,
+        // Gamma(2) below 1 + n m~; the rescale is 1/2 for term 1, r2 = 4 e^a
+        // for term 2 and 27 e^2a / 2 = (27/32) r2^2 for term 3
+        const bool t2 = sel >= p.W1, t3 = sel >= p.W12;
+        // (the small factor first: r2^2 alone can overflow for heavy bosons)
+        const float s = t3 ? ((sel - p.W12) * p.r2) * (0.84375f * p.r2)
+                           : (t2 ? (sel - p.W1) * p.r2 : 0.5f * sel);
+        const float n = t3 ? 3.0f : (t2 ? 2.0f : 1.0f);
+        if (s < 1.0f + n * p.mt) prod *= u01f_pos(A.z);
+        if (s < 1.0f) prod *= u01f_pos(A.w);
+        K = -logf(prod) * (t3 ? (1.0f / 3.0f) : (t2 ? 0.5f : 1.0f));
     } else {
         if (sel < p.w32) prod *= u01f_pos(A.z);
         if (sel < p.w3) prod *= u01f_pos(A.w);
@@ -762,7 +769,7 @@ __device__ __forceinline__ bool try_once(const DevConfig& cfg, const Prop& p, co
     // error below 3e-6); expm1f near Bose condensation only
     float a_q;
     if (kBose2)
-        a_q = (p.sign == -1) ? p.qa / (Etil > 0.025f ? 1.0f - em * em : -expm1f(-2.0f * Etil))
+        a_q = (p.sign == -1) ? p.qa / (Etil > 0.0167f ? 1.0f - em * em * em : -expm1f(-3.0f * Etil))
                              : 1.0f / (1.0f + em);
     else
         a_q = (p.sign == -1) ? p.qa / (Etil > 0.05f ? 1.0f - em : -expm1f(-Etil))

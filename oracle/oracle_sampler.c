@@ -10,9 +10,9 @@
  *   FSSW::add_one_sampled_particle,       src/FSSW.cpp:1969-1996
  *
  * The GPU proposes |p| from an exact Gamma mixture matching (E^2 - m^2/2)
- * exp(-(E - mu)/T) (for bosons (E^2 - m^2/2) (exp(-(E - mu)/T) +
- * exp(-2(E - mu)/T)), the first two terms of the Bose-Einstein series, whose
- * second term is the same mixture at rate 2), the direction from the Cooper-Frye flux factor itself
+ * exp(-(E - mu)/T) (for bosons (E^2 - m^2/2) times the first three terms of
+ * the Bose-Einstein series, exp(-n (E - mu)/T) for n = 1, 2, 3, term n being
+ * the same mixture at rate n), the direction from the Cooper-Frye flux factor itself
  * (linear in the cosine of the angle to the spatial part of dsigma in the rest
  * frame, inverse CDF), and folds the quantum-statistics, pE/(E^2 - m^2/2),
  * |p|-dependent flux remainder and delta-f acceptances into one uniform per
@@ -67,8 +67,9 @@ typedef struct {
     double m, mt, mu, mut, a, T, beta;
     int boson;
     double Kmax, w3, w2, W;
-    double W1, r2;         /* bosons: weight of the exp(-E~) term, 4 exp(a) */
-    double qa;             /* 1 - exp(-2a) for bosons */
+    double W1, W12, r2;    /* bosons: weights of the exp(-E~) term and of the
+                              first two terms, 4 exp(a) */
+    double qa;             /* 1 - exp(-3a) for bosons */
     int compat;            /* reproduce the reference's truncated/buggy series */
     double rmax;
     double c_poly;         /* mu~^2 - m~^2/2 */
@@ -108,15 +109,17 @@ static void orc_setup(const orc_cfg* cfg, double m, int sign, double mu_raw, dou
     p->w2 = 2.0 * p->mt;
     p->W = p->w3 + p->w2 + 0.5 * p->mt * p->mt;
     p->W1 = p->W;
+    p->W12 = p->W;
     p->r2 = 0.0;
     p->qa = -expm1(-p->a);
     if (p->boson) {
-        /* the exp(-2 E~) term: Gamma(3), Gamma(2), Gamma(1) at rate 2 with
-         * weights (1, 2 m~, m~^2) exp(-a) / 4 */
+        /* term n: Gamma(3), Gamma(2), Gamma(1) at rate n with weights
+         * exp(-(n-1)a) (2/n^3) (1, n m~, n^2 m~^2/4) */
         const double ea = exp(-p->a);
-        p->W = p->W1 + 0.25 * ea * (1.0 + p->mt) * (1.0 + p->mt);
+        p->W12 = p->W1 + 0.25 * ea * (1.0 + p->mt) * (1.0 + p->mt);
+        p->W = p->W12 + (2.0 / 27.0) * ea * ea * (1.0 + 1.5 * p->mt) * (1.0 + 1.5 * p->mt);
         p->r2 = 4.0 / ea;
-        p->qa = -expm1(-2.0 * p->a);
+        p->qa = -expm1(-3.0 * p->a);
     }
     p->compat = (cfg->compat_fermion && sampler == 0) ? 1 : 0;
     p->c_poly = p->mut * p->mut - 0.5 * p->mt * p->mt;
@@ -176,15 +179,16 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     orc_hblock(hs, 2u * t + 1u, ORC_TAG_TRY, Bw);
     const double sel = orc_u01(A[0]) * p->W;
     double prod = orc_u01_pos(A[1]);
-    /* term 1 (sel < W1): Gamma(3) below 2, Gamma(2) below 2 + 2 m~; term 2
-     * (bosons) rescaled to [0, (1 + m~)^2): Gamma(3) below 1, Gamma(2) below
-     * 1 + 2 m~, and K at rate 2 */
-    const int t2 = sel >= p->W1;
-    const double s = t2 ? (sel - p->W1) * p->r2 : sel;
-    const double th3 = t2 ? 1.0 : 2.0;
-    if (s < th3 + 2.0 * p->mt) prod *= orc_u01_pos(A[2]);
-    if (s < th3) prod *= orc_u01_pos(A[3]);
-    const double K = -log(prod) * (t2 ? 0.5 : 1.0);
+    /* term n rescaled to weights (1, n m~, n^2 m~^2/4): Gamma(3) below 1,
+     * Gamma(2) below 1 + n m~, K at rate n; the rescale is 1/2 for term 1,
+     * 4 exp(a) for term 2 and 27 exp(2a) / 2 for term 3 */
+    const int t2 = sel >= p->W1, t3 = sel >= p->W12;
+    const double s = t3 ? (sel - p->W12) * (0.84375 * p->r2 * p->r2)
+                        : (t2 ? (sel - p->W1) * p->r2 : 0.5 * sel);
+    const double nt = t3 ? 3.0 : (t2 ? 2.0 : 1.0);
+    if (s < 1.0 + nt * p->mt) prod *= orc_u01_pos(A[2]);
+    if (s < 1.0) prod *= orc_u01_pos(A[3]);
+    const double K = -log(prod) / nt;
     if (K > p->Kmax) return 0;
     const double k2 = K * (K + 2.0 * p->mt);
     const double Et = K + p->mt;                  /* E / T */
@@ -192,9 +196,9 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     const double a_pE = Et * ptil / (k2 + 0.5 * p->mt * p->mt);
     const double Etil = p->a + K;                 /* (E - mu) / T */
     const double em = exp(-Etil);
-    /* bosons: f_BE / (exp(-E~) + exp(-2 E~)) = 1 / (1 - exp(-2 E~)), at most
-     * 1 / qa */
-    const double a_q = p->boson ? p->qa / (-expm1(-2.0 * Etil)) : 1.0 / (1.0 + em);
+    /* bosons: f_BE / (exp(-E~) + exp(-2 E~) + exp(-3 E~)) =
+     * 1 / (1 - exp(-3 E~)), at most 1 / qa */
+    const double a_q = p->boson ? p->qa / (-expm1(-3.0 * Etil)) : 1.0 / (1.0 + em);
     double a_c = 1.0;
     if (p->compat) {
         a_c = orc_compat_ratio(p, Etil) / p->rmax;
