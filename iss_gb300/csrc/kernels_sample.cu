@@ -1391,19 +1391,18 @@ cell_assign_kernel(DevConfig cfg_in, const unsigned long long* __restrict__ cdf,
         const unsigned long long Q = qtot[b * cfg.n_species + s];
         const uint32_t eg = cfg.event_offset + static_cast<uint32_t>(e);
         const uint32_t c3 = static_cast<uint32_t>(s) | (kTagCell << 16);
-        // 64 draws at a time: each lane takes two and issues both guide
-        // lookups before either search, so their latencies overlap
+        // 64 draws at a time: each lane takes the pair (2k, 2k + 1), whose
+        // 64-bit uniforms are the two halves of one Philox block with counter
+        // k (d_begin is even: item sizes are multiples of 32), and issues both
+        // guide lookups before either search, so their latencies overlap
         for (int64_t d_sub = d_begin; d_sub < d_end; d_sub += kAssignSub) {
-        const int64_t d0 = d_sub + lane, d1 = d0 + 32;
+        const int64_t d0 = d_sub + 2 * lane, d1 = d0 + 1;
         const bool v0 = d0 < d_end, v1 = d1 < d_end;
         unsigned long long r0 = 0, r1 = 0;
         if (v0) {
-            const uint4 w = block(0u, static_cast<uint32_t>(d0), eg, c3, cfg.key0, cfg.key1);
+            const uint4 w = block(0u, static_cast<uint32_t>(d0 >> 1), eg, c3, cfg.key0, cfg.key1);
             r0 = (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
-        }
-        if (v1) {
-            const uint4 w = block(0u, static_cast<uint32_t>(d1), eg, c3, cfg.key0, cfg.key1);
-            r1 = (static_cast<unsigned long long>(w.x) << 32) | static_cast<unsigned long long>(w.y);
+            r1 = (static_cast<unsigned long long>(w.z) << 32) | static_cast<unsigned long long>(w.w);
         }
         const int last = static_cast<int>(sg.n - 1);
         const unsigned j0 = static_cast<unsigned>(r0 >> (64 - sg.g));

@@ -354,8 +354,19 @@ int64_t orc_sample_replay(const orc_cfg* cfg, const orc_species* sp, int32_t n_s
                 orc_cell c;
                 while (!done) {
                     uint32_t wc[4];
-                    orc_hblock(&hs, (uint32_t)redraw, ORC_TAG_CELL, wc);
-                    const uint64_t r = ((uint64_t)wc[0] << 32) | (uint64_t)wc[1];
+                    uint64_t r;
+                    if (redraw == 0) {
+                        /* first cell: draws 2k and 2k + 1 share the block
+                         * with counter k, halves (x, y) and (z, w) */
+                        orc_hstream hp = hs;
+                        hp.i = (uint32_t)i >> 1;
+                        orc_hblock(&hp, 0u, ORC_TAG_CELL, wc);
+                        r = (i & 1) ? (((uint64_t)wc[2] << 32) | (uint64_t)wc[3])
+                                    : (((uint64_t)wc[0] << 32) | (uint64_t)wc[1]);
+                    } else {
+                        orc_hblock(&hs, (uint32_t)redraw, ORC_TAG_CELL, wc);
+                        r = ((uint64_t)wc[0] << 32) | (uint64_t)wc[1];
+                    }
                     const int64_t l = orc_search(row, n_cells, qtot[k], r);
                     orc_load_cell(lrf28, coef4, l, &c);
                     orc_prop p;

@@ -110,7 +110,16 @@ def test_training_rows_match_restatement(trained):
     assert (f_gpu == f_ref).mean() > 0.999
     K, nv = rest_frame_targets(had, lrf[cell], sp["mass"][[idx[int(q)] for q in had["pid"]]])
     assert np.allclose(t_gpu[:, 0], K, rtol=2e-3, atol=1e-5)
-    assert np.allclose(t_gpu[:, 1:], nv, atol=2e-3)
+    # the direction of a hadron almost at rest in its cell is ill-conditioned:
+    # its float32 lab momentum (E up to ~20 GeV at large rapidity) is rounded
+    # by ~1e-7 E, i.e. ~1e-7 E / |p_LRF| in the direction, amplified by the
+    # boost's cancellation; compare where E / |p_LRF| < 1000
+    mass = sp["mass"][[idx[int(q)] for q in had["pid"]]]
+    Trow = lrf[cell][:, 13].astype(np.float64)
+    p_lrf = Trow * np.sqrt(K * (K + 2.0 * mass / Trow))
+    ok = had["E"] / p_lrf < 1000.0
+    assert ok.mean() > 0.999, ok.mean()
+    assert np.allclose(t_gpu[ok, 1:], nv[ok], atol=2e-3)
 
 
 def test_trained_network_beats_the_plain_proposal(trained):
