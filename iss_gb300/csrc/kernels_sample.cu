@@ -1488,6 +1488,11 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
     if (k_end_dev) k_end = *k_end_dev;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    // the three-term Bose proposal (prop_bose2) in the lean mode without
+    // diffusion; the other modes keep the one-term proposal, whose fewer
+    // registers spill less there (finite density: sample phase 30.3 ms with
+    // the Bose terms, 28.3 ms without)
+    constexpr bool kBose = kAlg == 4 && kMode == 1;
     // the warp's current work item: units [next, end) of species cur_s in event cur_e
     // draws [next, end), records from seg_base; a segment's draws are
     // counted by an int32, so draw indices fit in an int
@@ -1595,7 +1600,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = sl >= 0 ? cfg.lpairs + (static_cast<int64_t>(sl) * cfg.n_cells + l) * kPairFloats
                                    : nullptr;
                 }
-                if (!setup_any<kMode>(cfg, cells, species[u.s], l, p, false, !kLearned || !u.lp)) {
+                if (!setup_any<kMode>(cfg, cells, species[u.s], l, p, false, kBose && (!kLearned || !u.lp))) {
                     atomicCAS(&ctrs->error_code, 0, 1);
                     ctrs->error_species = u.s;
                     for (int q = 0; q < (kLcc ? u.mult : 1); q++)
@@ -1614,10 +1619,10 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     n_ltries++;
                     n_lhad += ok;
                 } else {
-                    ok = try_once<kMode, true>(cfg, p, u, pl, u_rap, n_viol);
+                    ok = try_once<kMode, kBose>(cfg, p, u, pl, u_rap, n_viol);
                 }
             } else {
-                ok = try_any<kMode, true>(cfg, p, u, pl, u_rap, n_viol);
+                ok = try_any<kMode, kBose>(cfg, p, u, pl, u_rap, n_viol);
             }
             u.t++;
             u.tries_cell++;
@@ -1643,7 +1648,7 @@ sampler_kernel(DevConfig cfg_in, CellArrays cells, const SpeciesDev* __restrict_
                     u.lp = nullptr;   // the pair's envelope is the hadron's, not the partner's
                     // (the lab-frame sampler keeps the hadron's maximum for
                     // its partner, src/emissionfunction.cpp:3503-3509)
-                    if (!setup_any<kMode>(cfg, cells, sp2, u.cell, p, true, true)) {
+                    if (!setup_any<kMode>(cfg, cells, sp2, u.cell, p, true, kBose)) {
                         atomicCAS(&ctrs->error_code, 0, 1);
                         ctrs->error_species = u.s;
                         write_hadron(out, u.slot + 1, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);

@@ -10,9 +10,10 @@
  *   FSSW::add_one_sampled_particle,       src/FSSW.cpp:1969-1996
  *
  * The GPU proposes |p| from an exact Gamma mixture matching (E^2 - m^2/2)
- * exp(-(E - mu)/T) (for bosons (E^2 - m^2/2) times the first three terms of
- * the Bose-Einstein series, exp(-n (E - mu)/T) for n = 1, 2, 3, term n being
- * the same mixture at rate n), the direction from the Cooper-Frye flux factor itself
+ * exp(-(E - mu)/T) (for bosons without diffusion or the compat-fermion
+ * factor (E^2 - m^2/2) times the first three terms of the Bose-Einstein
+ * series, exp(-n (E - mu)/T) for n = 1, 2, 3, term n being the same mixture
+ * at rate n), the direction from the Cooper-Frye flux factor itself
  * (linear in the cosine of the angle to the spatial part of dsigma in the rest
  * frame, inverse CDF), and folds the quantum-statistics, pE/(E^2 - m^2/2),
  * |p|-dependent flux remainder and delta-f acceptances into one uniform per
@@ -69,7 +70,8 @@ typedef struct {
     double Kmax, w3, w2, W;
     double W1, W12, r2;    /* bosons: weights of the exp(-E~) term and of the
                               first two terms, 4 exp(a) */
-    double qa;             /* 1 - exp(-3a) for bosons */
+    double qa;             /* 1 - exp(-a), 1 - exp(-3a) with bose3 */
+    int bose3;             /* the three-term Bose proposal */
     int compat;            /* reproduce the reference's truncated/buggy series */
     double rmax;
     double c_poly;         /* mu~^2 - m~^2/2 */
@@ -112,7 +114,9 @@ static void orc_setup(const orc_cfg* cfg, double m, int sign, double mu_raw, dou
     p->W12 = p->W;
     p->r2 = 0.0;
     p->qa = -expm1(-p->a);
-    if (p->boson) {
+    /* the GPU's lean mode without diffusion (no compat-fermion factor) */
+    p->bose3 = p->boson && !cfg->compat_fermion && !cfg->include_diff;
+    if (p->bose3) {
         /* term n: Gamma(3), Gamma(2), Gamma(1) at rate n with weights
          * exp(-(n-1)a) (2/n^3) (1, n m~, n^2 m~^2/4) */
         const double ea = exp(-p->a);
@@ -198,7 +202,7 @@ static int orc_try(const orc_cfg* cfg, const orc_cell* c, const orc_prop* p, int
     const double em = exp(-Etil);
     /* bosons: f_BE / (exp(-E~) + exp(-2 E~) + exp(-3 E~)) =
      * 1 / (1 - exp(-3 E~)), at most 1 / qa */
-    const double a_q = p->boson ? p->qa / (-expm1(-3.0 * Etil)) : 1.0 / (1.0 + em);
+    const double a_q = p->boson ? p->qa / (-expm1((p->bose3 ? -3.0 : -1.0) * Etil)) : 1.0 / (1.0 + em);
     double a_c = 1.0;
     if (p->compat) {
         a_c = orc_compat_ratio(p, Etil) / p->rmax;
