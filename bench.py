@@ -46,6 +46,7 @@ the headline `value`.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -708,11 +709,20 @@ def run_gpu(args, ws, rank, local):
     # throughout the timed region
     clocks = ClockSampler(local)
     clocks.start()
+    # warm-up steps are the timed steps' sequence (L2 flush, generate): the
+    # first use of the flush loads its kernel, which must not fall in a
+    # timed step (the first timed step otherwise took 12-250 ms on the host)
     for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
         s.generate_samples()
     torch.cuda.synchronize()
 
-    # device-timed steps
+    # device-timed steps; the garbage collector stays out of the timed region
+    # (a collection over the objects of the set-up can pause a step's host
+    # clock by a few hundred ms)
+    gc.collect()
+    gc.disable()
     barrier()
     torch.cuda.synchronize()
     clocks.mark_begin()
@@ -741,6 +751,7 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier()
     wall = time.perf_counter() - wall0
+    gc.enable()
     clocks.mark_end()
     clk = clocks.stop()
     timings = s.timings()
@@ -945,7 +956,8 @@ def run_gpu(args, ws, rank, local):
                            # and inside iss_gpu_generate alone, against ms_per_step
                            "host_ms_per_step": {"min": min(step_wall),
                                                 "median": statistics.median(step_wall),
-                                                "max": max(step_wall)},
+                                                "max": max(step_wall),
+                                                "steps": [round(v, 3) for v in step_wall]},
                            "host_ms_generate": {"min": min(gen_wall),
                                                 "median": statistics.median(gen_wall),
                                                 "max": max(gen_wall)}},
