@@ -372,8 +372,8 @@ iss_status iss_gpu_learned_train(iss_handle* h, const iss_learned_train_t* optio
  * gpu_learned_alpha (default 0.8) x network mixture + (1 - alpha) x the
  * plain proposal q_P; the others keep the plain sampler.  M per (species,
  * cell) is gpu_learned_safety (default 1.15) times the largest ratio
- * P a / q over gpu_learned_pilot (default 64) pilot proposals, capped by
- * 1 / (1 - alpha).  Target: the plain sampler's P a (a <= 1 its acceptance).
+ * P a / q over gpu_learned_pilot pilot proposals (default 4 in exact mode,
+ * 64 with gpu_learned_exact = 0), capped by 1 / (1 - alpha).  Target: the plain sampler's P a (a <= 1 its acceptance).
  *   gpu_learned_exact = 1 (default): exact rejection for every M.  A try is
  *     the mixture branch with probability M / (M + c): x from q, accepted
  *     with min(1, P a / (M q)); else the excess branch: x from the plain

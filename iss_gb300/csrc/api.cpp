@@ -906,7 +906,12 @@ iss_status run_learned_pairs(iss_handle* h) {
                     "gpu_sampler = 1 needs network weights (iss_gpu_learned_train or "
                     "iss_gpu_learned_set_weights)");
     const double thr = h->params.get_or("gpu_learned_min_hadrons_per_cell", 1.0);
-    const int n_pilot = static_cast<int>(h->params.get_or("gpu_learned_pilot", 64));
+    // pilot proposals per pair: in exact mode M only trades the network's
+    // share of the tries against the excess branch's (the output is the
+    // target for every M), and few pilots measured fastest (4: 15.3 ms per
+    // step on the 200k-cell surface, 64: 23.9 ms); the pilot-envelope mode
+    // needs M close to the true sup, so it keeps 64
+    const int n_pilot = static_cast<int>(h->params.get_or("gpu_learned_pilot", c.lexact ? 4 : 64));
     const float safety = static_cast<float>(h->params.get_or("gpu_learned_safety", 1.15));
     if (n_pilot < 1 || n_pilot > 4096 || !(safety >= 1.0f))
         return fail(h, ISS_ERR_INVALID_ARG, "gpu_learned_pilot = %d, gpu_learned_safety = %g", n_pilot,
