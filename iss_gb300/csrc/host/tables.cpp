@@ -116,8 +116,9 @@ bool load_decay_table(const std::string& particle_table_path, int afterburner, D
                     if (d == 0) continue;
                     const int idx = find(d);
                     // neutral, non-strange mesons are their own antiparticles
-                    // (src/particle_decay.cpp:139-147); unknown daughters keep
-                    // their sign
+                    // (src/particle_decay.cpp:139-147); unknown daughters are
+                    // negated like the others and stay unknown (no product
+                    // record of theirs carries the sign)
                     if (idx >= 0 && raw[idx].baryon == 0 && raw[idx].charge == 0 &&
                         raw[idx].strange == 0)
                         c.daughter[k] = d;

@@ -99,6 +99,34 @@ int64_t orc_sample_replay(const orc_cfg* c, const orc_species* sp, int32_t n_sp,
                           const uint64_t* cdf, const uint64_t* qtot, const int32_t* counts,
                           orc_hadron* out, int64_t capacity, orc_stats* stats);
 
+/* Part 2c: resonance decays (oracle_decay.c).  The decay table as
+ * particle_decay::read_resonances_list reads it (src/particle_decay.cpp:33-160):
+ * one entry per particle, anti-baryons appended after their baryon; stable
+ * when the first channel has one daughter; daughters as indices of the first
+ * entry with their pid (-1: unknown); cum53 = ceil(2^53 x the FP64 partial
+ * sum of the particle's branching ratios in channel order). */
+typedef struct orc_dparticle {
+    int32_t pid;
+    double mass, width;
+    int32_t stable, first_channel, n_channels;
+} orc_dparticle;
+
+typedef struct orc_dchannel {
+    int32_t n_daughters;
+    int32_t daughter[5];
+    uint64_t cum53;
+} orc_dchannel;
+
+/* the final-state lists of events [0, n_events) whose sampled hadrons are
+ * in[ev_off[e] .. ev_off[e + 1]): out (capacity records) and out_off
+ * (n_events + 1); returns the number of records, -1 when out is too small,
+ * -2 on allocation failure; *failures counts 3-body decays without an
+ * accepted (E1, E2) */
+int64_t orc_decay_replay(const orc_dparticle* parts, int32_t n_parts, const orc_dchannel* chans,
+                         uint64_t seed, int64_t event_offset, int32_t n_events, const int64_t* ev_off,
+                         const orc_hadron* in, int64_t capacity, orc_hadron* out, int64_t* out_off,
+                         int64_t* failures);
+
 /* Part 3 */
 int64_t orc_reference_sampler(const orc_cfg* c, const orc_species* sp, int32_t n_sp,
                               const float* lrf28, const int32_t* keep, int64_t n_cells,

@@ -58,6 +58,15 @@ class Cfg(C.Structure):
                 ("b14_c2", C.c_void_p), ("ce_tb", C.c_void_p), ("qmu_tb", C.c_void_p)]
 
 
+class DParticle(C.Structure):
+    _fields_ = [("pid", C.c_int32), ("mass", C.c_double), ("width", C.c_double),
+                ("stable", C.c_int32), ("first_channel", C.c_int32), ("n_channels", C.c_int32)]
+
+
+class DChannel(C.Structure):
+    _fields_ = [("n_daughters", C.c_int32), ("daughter", C.c_int32 * 5), ("cum53", C.c_uint64)]
+
+
 class Stats(C.Structure):
     _fields_ = [("n_tries", C.c_int64), ("n_redraws", C.c_int64), ("n_failures", C.c_int64),
                 ("n_bound_violations", C.c_int64)]
@@ -88,6 +97,9 @@ def _setup(L):
     L.orc_sample_replay.argtypes = [C.POINTER(Cfg), v, C.c_int32, v, C.c_int64, v, v, v, v,
                                     v, C.c_int64, C.POINTER(Stats)]
     L.orc_sample_replay.restype = C.c_int64
+    L.orc_decay_replay.argtypes = [v, C.c_int32, v, C.c_uint64, C.c_int64, C.c_int32, v, v,
+                                   C.c_int64, v, v, C.POINTER(C.c_int64)]
+    L.orc_decay_replay.restype = C.c_int64
     if hasattr(L, "orc_reference_sampler"):
         L.orc_reference_sampler.argtypes = [C.POINTER(Cfg), v, C.c_int32, v, v, C.c_int64,
                                             C.c_int32, C.c_uint64, v, C.c_int64,
@@ -303,6 +315,92 @@ def sample_replay(oc: OracleConfig, sp, lrf, coef4, cdf_rows, cnt):
     if n < 0:
         raise RuntimeError(f"orc_sample_replay status {n}")
     return out[:n], st
+
+
+def decay_table(table_dir, afterburner):
+    """The decay table as particle_decay::read_resonances_list reads the pdg
+    file (src/particle_decay.cpp:33-160), restated: whitespace tokens
+    (pid, name, mass, width, g, B, S, charm, bottom, g_iso, Q, n_channels,
+    then per channel: pid, n_daughters, branching ratio, 5 daughter pids);
+    stable when the first channel has one daughter; every baryon (B = 1) is
+    followed by its anti-baryon, whose daughters are negated unless the
+    first entry read so far with that pid is a neutral non-strange meson.
+    Daughters become indices of the first entry with their pid (-1 unknown);
+    cum53 = ceil(2^53 x the FP64 partial sum of branching ratios)."""
+    import math
+    name = {2: "pdg-SMASH.dat", 1: "pdg-urqmd_v3.3+.dat"}.get(afterburner, "pdg-s95pv1.dat")
+    tok = open(os.path.join(table_dir, name)).read().split()
+    parts = []   # [pid, mass, width, B, S, Q, stable, channels]
+    k = 0
+    while k + 12 <= len(tok):
+        pid = int(tok[k])
+        mass, width = float(tok[k + 2]), float(tok[k + 3])
+        B, S, Q, nd = int(tok[k + 5]), int(tok[k + 6]), int(tok[k + 10]), int(tok[k + 11])
+        k += 12
+        ch = []
+        for _ in range(nd):
+            npart, br = int(tok[k + 1]), float(tok[k + 2])
+            ch.append((npart, br, [int(t) for t in tok[k + 3:k + 8]]))
+            k += 8
+        stable = 1 if ch and ch[0][0] == 1 else 0
+        parts.append([pid, mass, width, B, S, Q, stable, ch])
+        if B == 1:
+            anti = []
+            for npart, br, ds in ch:
+                nds = []
+                for d in ds:
+                    if d == 0:
+                        nds.append(0)
+                        continue
+                    hit = next((p for p in parts if p[0] == d), None)
+                    neutral = hit is not None and hit[3] == 0 and hit[5] == 0 and hit[4] == 0
+                    nds.append(d if neutral else -d)
+                anti.append((npart, br, nds))
+            parts.append([-pid, mass, width, -B, -S, -Q, stable, anti])
+    first = {}
+    for i, p in enumerate(parts):
+        first.setdefault(p[0], i)
+    dp = (DParticle * len(parts))()
+    chans = []
+    for i, p in enumerate(parts):
+        dp[i].pid, dp[i].mass, dp[i].width, dp[i].stable = p[0], p[1], p[2], p[6]
+        dp[i].first_channel, dp[i].n_channels = len(chans), len(p[7])
+        cum = 0.0
+        for npart, br, ds in p[7]:
+            cum += br
+            x = math.ceil(math.ldexp(cum, 53))
+            c = DChannel()
+            c.n_daughters = npart
+            for j in range(5):
+                c.daughter[j] = first.get(ds[j], -1) if (j < npart and ds[j] != 0) else -1
+            c.cum53 = 0 if x <= 0 else min(x, 2 ** 64 - 1)
+            chans.append(c)
+    dc = (DChannel * max(len(chans), 1))(*chans)
+    return dp, dc
+
+
+def decay_replay(table, seed, ev_off, hadrons, event_offset=0):
+    """Final-state lists of the events whose sampled hadrons are
+    hadrons[ev_off[e]:ev_off[e + 1]] (oracle_decay.c); returns (records,
+    event offsets, 3-body failures)."""
+    dp, dc = table
+    ev_off = np.ascontiguousarray(ev_off, dtype=np.int64)
+    had = np.ascontiguousarray(hadrons, dtype=HADRON_DTYPE)
+    n_ev = len(ev_off) - 1
+    cap = 4 * max(len(had), 1) + 64
+    while True:
+        out = np.zeros(cap, dtype=HADRON_DTYPE)
+        off = np.zeros(n_ev + 1, dtype=np.int64)
+        fails = C.c_int64(0)
+        n = lib().orc_decay_replay(C.cast(dp, C.c_void_p), len(dp), C.cast(dc, C.c_void_p),
+                                   int(seed) & 0xFFFFFFFFFFFFFFFF, int(event_offset), n_ev,
+                                   _p(ev_off), _p(had), cap, _p(out), _p(off), C.byref(fails))
+        if n == -1:
+            cap *= 2
+            continue
+        if n < 0:
+            raise RuntimeError(f"orc_decay_replay status {n}")
+        return out[:n], off, int(fails.value)
 
 
 def load_golden(name):

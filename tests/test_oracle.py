@@ -269,3 +269,47 @@ def test_gpu_algorithm_replay_matches_reference_samples(name, n_ev):
         z = (ma - mb) / np.sqrt(ma / n_ev + mb / int(g["n_events"]))
         pvals.append(2 * stats.norm.sf(abs(z)))
     assert min(pvals) > 0.01 / len(pvals), pvals
+
+
+def test_decay_replay_conserves_energy_and_ends_stable():
+    """The oracle's restatement of the resonance decays (oracle_decay.c):
+    every final hadron is stable under the strong interaction, two- and
+    three-body decays conserve each event's energy (pole masses), and each
+    event's stable primaries appear unchanged and in order in its list
+    (src/FSSW.cpp:1746-1779)."""
+    dp, dc = O.decay_table(S.TABLE_DIR, 0)
+    assert len(dp) == 320 and sum(p.stable for p in dp) == 24
+    first = {}
+    for i in range(len(dp)):
+        first.setdefault(dp[i].pid, i)
+    pids = [113, 223, 2214, 3124, 313, -2214, 221, 331, 211, 2212, -211, 111]
+    rng = np.random.default_rng(3)
+    rows, off = [], [0]
+    for e in range(60):
+        for _ in range(40):
+            pid = int(rng.choice(pids))
+            m = dp[first[pid]].mass
+            p = rng.normal(0.0, 0.5, 3)
+            rows.append((pid, m, np.sqrt(m * m + (p ** 2).sum()), p[0], p[1], p[2], 1.0, 0.0, 0.0, 0.0))
+        off.append(len(rows))
+    had = np.array(rows, dtype=O.HADRON_DTYPE)
+    out, roff, fails = O.decay_replay((dp, dc), 5, np.array(off), had)
+    assert fails == 0 and roff[-1] == len(out) > len(had)
+    stable = {dp[i].pid for i in range(len(dp)) if dp[i].stable}
+    assert set(np.unique(out["pid"]).tolist()) <= stable
+    e_in = np.add.reduceat(had["E"].astype(np.float64), np.array(off[:-1]))
+    e_out = np.add.reduceat(out["E"].astype(np.float64), roff[:-1])
+    assert np.max(np.abs(e_out - e_in) / e_in) < 1e-6
+    for e in range(60):
+        prim = had[off[e]:off[e + 1]]
+        keep = [r.tobytes() for r in prim[np.isin(prim["pid"], list(stable))]]
+        j = 0
+        for r in out[roff[e]:roff[e + 1]]:
+            if j < len(keep) and r.tobytes() == keep[j]:
+                j += 1
+        assert j == len(keep)
+    # the same seed gives the same lists; another seed other decays
+    out2, _, _ = O.decay_replay((dp, dc), 5, np.array(off), had)
+    assert out2.tobytes() == out.tobytes()
+    out3, _, _ = O.decay_replay((dp, dc), 6, np.array(off), had)
+    assert out3.tobytes() != out.tobytes()
