@@ -924,8 +924,8 @@ def run_gpu(args, ws, rank, local):
                     "peak_source": peak_kind,
                     "traffic": (traffic_per_h * per_launch_h) if traffic_per_h else None,
                     "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum per hadron "
-                                       f"of the autotuned shape on a 50k-cell case, {PROFILE}, times "
-                                       f"the hadrons of one step"),
+                                       f"of the autotuned shape on the 200k-cell surface with 200 events "
+                                       f"(cold cache), {PROFILE}, times the hadrons of one step"),
                     "issue": issue,
                     "algorithmic_bytes_per_launch": per_launch_h * ALG_BYTES_PER_HADRON,
                     "kernel_ms_per_launch": 1e3 * samp_sec / args.steps,
